@@ -1,0 +1,282 @@
+"""Oracle: test infrastructure, never product code.
+
+Two CPU implementations of the local SpGEMM / SpMSpV / MCL-select path are
+reachable from here, both used only as checkers by ``tests/``, by
+``__graft_entry__.smoke()`` and by the CPU-baseline leg of ``bench.py``:
+
+* ``port`` -- the project's own plain-C restatement of the reference's
+  algorithms (``oracle/oracle.c``), built everywhere by ``oracle/Makefile``;
+* ``ref``  -- the reference's own header templates compiled unchanged against
+  a single-rank MPI stand-in (``oracle/ref_harness.cpp``); it only exists where
+  the reference sources were present at build time.
+
+The product (``combblas_gb300``) never imports this package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_REF_SO = os.path.join(_HERE, "_ref", "libcombblas_ref.so")
+_PORT_SO = os.path.join(_HERE, "_ref", "libgbc_oracle.so")
+
+# semiring codes shared by both libraries
+SR_PLUSTIMES_F64 = 0
+SR_PLUSTIMES_F32 = 1
+SR_PLUSTIMES_I64 = 2
+SR_MINPLUS_F64 = 3
+SR_SELECT2NDMIN_I64 = 4
+SR_BOOL = 5
+SR_MINPLUS_I64 = 6
+
+SR_DTYPE = {
+    SR_PLUSTIMES_F64: np.float64,
+    SR_PLUSTIMES_F32: np.float32,
+    SR_PLUSTIMES_I64: np.int64,
+    SR_MINPLUS_F64: np.float64,
+    SR_SELECT2NDMIN_I64: np.int64,
+    SR_BOOL: np.bool_,
+    SR_MINPLUS_I64: np.int64,
+}
+
+# variant codes of ref_spgemm
+V_HYBRID = 0
+V_HEAP = 1
+V_HASH_SORTED = 2
+V_HASH_UNSORTED = 3
+V_HYBRID_CSC = 4
+V_PSPGEMM = 5
+
+_P64 = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+_P32 = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+
+def build(ref_path: str | None = None, quiet: bool = True) -> None:
+    """Compile the oracle libraries in place (``make -C oracle``)."""
+    import subprocess
+
+    cmd = ["make", "-C", _HERE, "-j4"]
+    if ref_path:
+        cmd.append(f"REF={ref_path}")
+    subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL if quiet else None)
+
+
+def have_ref() -> bool:
+    return os.path.exists(_REF_SO)
+
+
+_ref_lib = None
+_port_lib = None
+
+
+def _ref():
+    global _ref_lib
+    if _ref_lib is None:
+        lib = C.CDLL(_REF_SO)
+        lib.ref_spgemm.restype = C.c_int64
+        lib.ref_spgemm.argtypes = [C.c_int, C.c_int, C.c_int64, C.c_int64, C.c_int64, _P64, _P64, C.c_void_p,
+                                   _P64, _P64, C.c_void_p, C.c_int]
+        lib.ref_result_copy.restype = None
+        lib.ref_result_copy.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.ref_result_seconds.restype = C.c_double
+        lib.ref_colstats.restype = C.c_int64
+        lib.ref_colstats.argtypes = [C.c_int, C.c_int64, C.c_int64, C.c_int64, _P64, _P64, _P64, _P64, _P64]
+        lib.ref_spmspv_bucket.restype = C.c_int64
+        lib.ref_spmspv_bucket.argtypes = [C.c_int64, C.c_int64, _P64, _P64, _P32, _P64, C.c_int32, C.c_int]
+        lib.ref_bfs_selectmin.restype = C.c_int
+        lib.ref_bfs_selectmin.argtypes = [C.c_int64, _P64, _P64, C.c_int64, _P64, C.c_void_p]
+        lib.ref_mcl_expand.restype = C.c_int64
+        lib.ref_mcl_expand.argtypes = [C.c_int64, _P64, _P64, np.ctypeslib.ndpointer(dtype=np.float32),
+                                       C.c_float, C.c_int64, C.c_int64, C.c_float]
+        lib.ref_num_threads.restype = C.c_int
+        _ref_lib = lib
+    return _ref_lib
+
+
+def _vals_ptr(M, dtype):
+    if M.values is None:
+        return None, None
+    v = np.ascontiguousarray(M.values, dtype=dtype)
+    return v, v.ctypes.data_as(C.c_void_p)
+
+
+def _fetch(lib, nnz, dtype, with_cols=True):
+    rows = np.empty(nnz, np.int64)
+    cols = np.empty(nnz, np.int64) if with_cols else None
+    vals = np.empty(nnz, dtype)
+    lib.ref_result_copy(rows.ctypes.data_as(C.c_void_p),
+                        cols.ctypes.data_as(C.c_void_p) if with_cols else None,
+                        vals.ctypes.data_as(C.c_void_p))
+    return rows, cols, vals
+
+
+# ------------------------------------------------------------------ reference
+def ref_spgemm(A, B, sr: int, variant: int = V_HYBRID, reps: int = 1):
+    """Run the reference's own local multiply.  Returns (rows, cols, vals,
+    seconds) in the order the reference emits them (SpTuples order)."""
+    lib = _ref()
+    dt = SR_DTYPE[sr]
+    av, ap = _vals_ptr(A, dt)
+    bv, bp = _vals_ptr(B, dt)
+    nnz = lib.ref_spgemm(variant, sr, A.nrow, A.ncol, B.ncol, np.ascontiguousarray(A.colptr),
+                         np.ascontiguousarray(A.rowidx), ap, np.ascontiguousarray(B.colptr),
+                         np.ascontiguousarray(B.rowidx), bp, reps)
+    if nnz < 0:
+        raise ValueError("bad semiring/variant")
+    rows, cols, vals = _fetch(lib, nnz, dt)
+    return rows, cols, vals, lib.ref_result_seconds()
+
+
+def ref_colstats(A, B, which: int):
+    """Per nonempty column of B: 0 = estimateFLOP, 1 = estimateNNZ_Hash."""
+    lib = _ref()
+    out = np.zeros(max(B.ncol, 1), np.int64)
+    nzc = lib.ref_colstats(which, A.nrow, A.ncol, B.ncol, np.ascontiguousarray(A.colptr),
+                           np.ascontiguousarray(A.rowidx), np.ascontiguousarray(B.colptr),
+                           np.ascontiguousarray(B.rowidx), out)
+    return out[:nzc]
+
+
+def ref_spmspv(A, indx: np.ndarray, numx: np.ndarray, buckets: int = 32):
+    lib = _ref()
+    indx = np.ascontiguousarray(indx, np.int32)
+    numx = np.ascontiguousarray(numx, np.int64)
+    nnz = lib.ref_spmspv_bucket(A.nrow, A.ncol, np.ascontiguousarray(A.colptr), np.ascontiguousarray(A.rowidx),
+                                indx, numx, len(indx), buckets)
+    rows, _, vals = _fetch(lib, nnz, np.int64, with_cols=False)
+    return rows, vals
+
+
+def ref_bfs(A, source: int, with_levels: bool = True):
+    lib = _ref()
+    n = A.ncol
+    parents = np.empty(n, np.int64)
+    levels = np.empty(n, np.int64) if with_levels else None
+    it = lib.ref_bfs_selectmin(n, np.ascontiguousarray(A.colptr), np.ascontiguousarray(A.rowidx), int(source),
+                               parents, levels.ctypes.data_as(C.c_void_p) if with_levels else None)
+    return parents, levels, it, lib.ref_result_seconds()
+
+
+def ref_mcl_expand(A, thr: float, select: int, recover_num: int = 0, recover_pct: float = 0.9):
+    lib = _ref()
+    nnz = lib.ref_mcl_expand(A.ncol, np.ascontiguousarray(A.colptr), np.ascontiguousarray(A.rowidx),
+                             np.ascontiguousarray(A.values, np.float32), thr, select, recover_num, recover_pct)
+    rows, cols, vals = _fetch(lib, nnz, np.float32)
+    return rows, cols, vals, lib.ref_result_seconds()
+
+
+def ref_num_threads() -> int:
+    return _ref().ref_num_threads()
+
+
+# ----------------------------------------------------------------------- port
+def _port():
+    global _port_lib
+    if _port_lib is None:
+        lib = C.CDLL(_PORT_SO)
+        lib.gbc_o_spgemm.restype = C.c_int64
+        lib.gbc_o_spgemm.argtypes = [C.c_int, C.c_int, C.c_int64, C.c_int64, C.c_int64, _P64, _P64, C.c_void_p,
+                                     _P64, _P64, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.gbc_o_result.restype = None
+        lib.gbc_o_result.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.gbc_o_spmspv.restype = C.c_int64
+        lib.gbc_o_spmspv.argtypes = [C.c_int64, _P64, _P64, _P32, _P64, C.c_int32, C.c_int]
+        lib.gbc_o_bfs.restype = C.c_int
+        lib.gbc_o_bfs.argtypes = [C.c_int64, _P64, _P64, C.c_int64, _P64, C.c_void_p]
+        lib.gbc_o_mcl_select.restype = C.c_int64
+        lib.gbc_o_mcl_select.argtypes = [C.c_int64, _P64, _P64, np.ctypeslib.ndpointer(dtype=np.float32),
+                                         C.c_float, C.c_int64]
+        lib.gbc_o_num_threads.restype = C.c_int
+        _port_lib = lib
+    return _port_lib
+
+
+def _port_csc(lib, ncol, nnz, dtype):
+    cp = np.empty(ncol + 1, np.int64)
+    rows = np.empty(nnz, np.int64)
+    vals = np.empty(nnz, dtype)
+    lib.gbc_o_result(cp.ctypes.data_as(C.c_void_p), rows.ctypes.data_as(C.c_void_p),
+                     vals.ctypes.data_as(C.c_void_p))
+    return cp, rows, vals
+
+
+def port_spgemm(A, B, sr: int, sorted: bool = True, want_counts: bool = False):
+    """C = A*B by the C restatement.  Returns a CSC (generators.CSC-like
+    tuple: colptr, rowidx, values) and optionally (flop, nnz) per column."""
+    lib = _port()
+    dt = SR_DTYPE[sr]
+    av, ap = _vals_ptr(A, dt)
+    bv, bp = _vals_ptr(B, dt)
+    if ap is None:
+        av = np.ones(A.nnz, dt)
+        ap = av.ctypes.data_as(C.c_void_p)
+    if bp is None:
+        bv = np.ones(B.nnz, dt)
+        bp = bv.ctypes.data_as(C.c_void_p)
+    flop = np.empty(B.ncol, np.int64)
+    cnt = np.empty(B.ncol, np.int64)
+    nnz = lib.gbc_o_spgemm(sr, int(sorted), A.nrow, A.ncol, B.ncol, np.ascontiguousarray(A.colptr),
+                           np.ascontiguousarray(A.rowidx), ap, np.ascontiguousarray(B.colptr),
+                           np.ascontiguousarray(B.rowidx), bp, flop.ctypes.data_as(C.c_void_p),
+                           cnt.ctypes.data_as(C.c_void_p))
+    if nnz < 0:
+        raise ValueError("bad semiring")
+    cp, rows, vals = _port_csc(lib, B.ncol, nnz, dt)
+    if want_counts:
+        return (cp, rows, vals), (flop, cnt)
+    return cp, rows, vals
+
+
+def port_spmspv(A, indx, numx, buckets: int = 32):
+    lib = _port()
+    indx = np.ascontiguousarray(indx, np.int32)
+    numx = np.ascontiguousarray(numx, np.int64)
+    ny = lib.gbc_o_spmspv(A.nrow, np.ascontiguousarray(A.colptr), np.ascontiguousarray(A.rowidx), indx, numx,
+                          len(indx), buckets)
+    rows = np.empty(ny, np.int64)
+    vals = np.empty(ny, np.int64)
+    lib.gbc_o_result(None, rows.ctypes.data_as(C.c_void_p), vals.ctypes.data_as(C.c_void_p))
+    return rows, vals
+
+
+def port_bfs(A, source: int, with_levels: bool = True):
+    lib = _port()
+    n = A.ncol
+    parents = np.empty(n, np.int64)
+    levels = np.empty(n, np.int64) if with_levels else None
+    it = lib.gbc_o_bfs(n, np.ascontiguousarray(A.colptr), np.ascontiguousarray(A.rowidx), int(source), parents,
+                       levels.ctypes.data_as(C.c_void_p) if with_levels else None)
+    return parents, levels, it
+
+
+def port_mcl_select(Ccp, Cri, Cv, thr: float, select: int):
+    lib = _port()
+    n = len(Ccp) - 1
+    nnz = lib.gbc_o_mcl_select(n, np.ascontiguousarray(Ccp, np.int64), np.ascontiguousarray(Cri, np.int64),
+                               np.ascontiguousarray(Cv, np.float32), thr, select)
+    return _port_csc(lib, n, nnz, np.float32)
+
+
+def port_num_threads() -> int:
+    return _port().gbc_o_num_threads()
+
+
+# ------------------------------------------------------------------- helpers
+def tuples_to_csc(rows, cols, vals, ncol):
+    """Canonicalise a tuple list (any order) to CSC with rows sorted within
+    each column (the comparison form for unsorted hash outputs)."""
+    order = np.lexsort((rows, cols))
+    rows, cols, vals = rows[order], cols[order], vals[order]
+    cp = np.zeros(ncol + 1, np.int64)
+    cp[1:] = np.cumsum(np.bincount(cols, minlength=ncol))
+    return cp, rows, vals
+
+
+def canonical_csc(cp, rows, vals):
+    """Sort rows within each column (stable)."""
+    ncol = len(cp) - 1
+    cols = np.repeat(np.arange(ncol, dtype=np.int64), np.diff(cp))
+    return tuples_to_csc(np.asarray(rows), cols, np.asarray(vals), ncol)

@@ -1,0 +1,348 @@
+// Test infrastructure (oracle only): a ctypes-callable harness around the
+// reference's own, unmodified header templates, compiled from the reference
+// sources in place against the single-rank MPI stand-in in oracle/mpistub.
+// Nothing here is product code; the tests and the CPU baseline leg of the
+// benchmark are its only users.
+//
+// Entry points mirror the reference calls they wrap:
+//   ref_spgemm           -> LocalHybridSpGEMM (mtSpGEMM.h:213), LocalSpGEMM
+//                           (mtSpGEMM.h:74), LocalSpGEMMHash (mtSpGEMM.h:463),
+//                           CSC LocalHybridSpGEMM (mtSpGEMM.h:1148),
+//                           PSpGEMM on a 1x1 grid (SpParMat.h:464)
+//   ref_colstats         -> estimateFLOP (mtSpGEMM.h:1057),
+//                           estimateNNZ_Hash (mtSpGEMM.h:806)
+//   ref_spmspv_bucket    -> SpMXSpV_Bucket (SpImpl.cpp:389)
+//   ref_bfs_selectmin    -> the BFS_CSC level loop of
+//                           Applications/SpMSpV-IPDPS2017/SpMSpVBench.cpp:105-156
+//   ref_mcl_expand       -> MemEfficientSpGEMM + MCLPruneRecoverySelect
+//                           (ParFriends.h:452,185)
+#include "CombBLAS/CombBLAS.h"
+#include "CombBLAS/mtSpGEMM.h"
+
+#include <chrono>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+using namespace combblas;
+
+int cblas_splits = 1;
+double cblas_alltoalltime, cblas_allgathertime, cblas_localspmvtime, cblas_mergeconttime, cblas_transvectime;
+double mcl_Abcasttime, mcl_Bbcasttime, mcl_localspgemmtime, mcl_multiwaymergetime, mcl_kselecttime,
+    mcl_prunecolumntime, mcl_symbolictime;
+double mcl3d_conversiontime, mcl3d_symbolictime, mcl3d_Abcasttime, mcl3d_Bbcasttime, mcl3d_SUMMAtime,
+    mcl3d_localspgemmtime, mcl3d_SUMMAmergetime, mcl3d_reductiontime, mcl3d_3dmergetime, mcl3d_kselecttime;
+
+// Same meaning as SelectMinSR in Applications/SpMSpV-IPDPS2017/SpMSpVBench.cpp:79-100:
+// add = min, multiply returns the vector value, identity -1.
+struct HarnessSelectMinSR {
+    typedef int64_t T_promote;
+    static T_promote id() { return -1; }
+    static bool returnedSAID() { return false; }
+    static T_promote add(const T_promote &a, const T_promote &b) { return std::min(a, b); }
+    static T_promote multiply(const bool &, const T_promote &x) { return x; }
+    static void axpy(bool, const T_promote &x, T_promote &y) { y = std::min(y, x); }
+};
+
+// Same meaning as Applications/FastSV.h:25-44 (Select2ndMinSR).
+template <typename T1, typename T2>
+struct HarnessSelect2ndMinSR {
+    typedef typename promote_trait<T1, T2>::T_promote T_promote;
+    static T_promote id() { return std::numeric_limits<T_promote>::max(); }
+    static bool returnedSAID() { return false; }
+    static MPI_Op mpi_op() { return MPI_MIN; }
+    static T_promote add(const T_promote &a, const T_promote &b) { return std::min(a, b); }
+    static T_promote multiply(const T1 &, const T2 &b) { return static_cast<T_promote>(b); }
+    static void axpy(const T1 a, const T2 &x, T_promote &y) { y = add(y, multiply(a, x)); }
+};
+
+namespace {
+
+struct Result {
+    std::vector<int64_t> rows, cols;
+    std::vector<char> vals;  // raw bytes, element size given by the semiring
+    double seconds = 0.0;
+};
+Result g_res;
+
+template <typename NT>
+std::vector<std::tuple<int64_t, int64_t, NT>> csc_to_tuples(int64_t n, const int64_t *cp, const int64_t *ri,
+                                                             const void *vals)
+{
+    std::vector<std::tuple<int64_t, int64_t, NT>> t;
+    t.reserve(cp[n]);
+    const NT *v = static_cast<const NT *>(vals);
+    for (int64_t j = 0; j < n; ++j)
+        for (int64_t p = cp[j]; p < cp[j + 1]; ++p) t.emplace_back(ri[p], j, v ? v[p] : NT(1));
+    return t;
+}
+
+template <typename NT>
+SpDCCols<int64_t, NT> *make_dcsc(int64_t m, int64_t n, const int64_t *cp, const int64_t *ri, const void *vals)
+{
+    auto t = csc_to_tuples<NT>(n, cp, ri, vals);
+    auto *arr = new std::tuple<int64_t, int64_t, NT>[t.size()];
+    std::copy(t.begin(), t.end(), arr);
+    SpTuples<int64_t, NT> tup((int64_t)t.size(), m, n, arr, /*sorted=*/true, /*isOpNew=*/false);
+    return new SpDCCols<int64_t, NT>(tup, false);
+}
+
+template <typename NT>
+SpCCols<int64_t, NT> *make_csc(int64_t m, int64_t n, const int64_t *cp, const int64_t *ri, const void *vals)
+{
+    auto t = csc_to_tuples<NT>(n, cp, ri, vals);
+    auto *arr = new std::tuple<int64_t, int64_t, NT>[t.size()];
+    std::copy(t.begin(), t.end(), arr);
+    SpTuples<int64_t, NT> tup((int64_t)t.size(), m, n, arr, true, false);
+    return new SpCCols<int64_t, NT>(tup, false);
+}
+
+template <typename NT>
+void store_tuples(SpTuples<int64_t, NT> *C)
+{
+    int64_t nnz = C->getnnz();
+    g_res.rows.resize(nnz);
+    g_res.cols.resize(nnz);
+    g_res.vals.resize(nnz * sizeof(NT));
+    NT *v = reinterpret_cast<NT *>(g_res.vals.data());
+    for (int64_t i = 0; i < nnz; ++i) {
+        g_res.rows[i] = C->rowindex(i);
+        g_res.cols[i] = C->colindex(i);
+        v[i] = C->numvalue(i);
+    }
+}
+
+template <typename NT>
+void store_dcsc(const SpDCCols<int64_t, NT> &C)
+{
+    int64_t nnz = C.getnnz();
+    g_res.rows.resize(nnz);
+    g_res.cols.resize(nnz);
+    g_res.vals.resize(nnz * sizeof(NT));
+    NT *v = reinterpret_cast<NT *>(g_res.vals.data());
+    if (nnz == 0) return;
+    Dcsc<int64_t, NT> *d = C.GetDCSC();
+    int64_t q = 0;
+    for (int64_t i = 0; i < d->nzc; ++i)
+        for (int64_t p = d->cp[i]; p < d->cp[i + 1]; ++p, ++q) {
+            g_res.rows[q] = d->ir[p];
+            g_res.cols[q] = d->jc[i];
+            v[q] = d->numx[p];
+        }
+}
+
+double now() { return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count(); }
+
+template <typename SR, typename NT>
+int64_t run_spgemm(int variant, int64_t m, int64_t k, int64_t n, const int64_t *Acp, const int64_t *Ari,
+                   const void *Av, const int64_t *Bcp, const int64_t *Bri, const void *Bv, int reps)
+{
+    if (variant == 4) {  // CSC overload
+        std::unique_ptr<SpCCols<int64_t, NT>> A(make_csc<NT>(m, k, Acp, Ari, Av));
+        std::unique_ptr<SpCCols<int64_t, NT>> B(make_csc<NT>(k, n, Bcp, Bri, Bv));
+        SpTuples<int64_t, NT> *C = nullptr;
+        double best = 1e300;
+        for (int r = 0; r < reps; ++r) {
+            delete C;
+            double t0 = now();
+            C = LocalHybridSpGEMM<SR, NT>(*A, *B, false, false);
+            best = std::min(best, now() - t0);
+        }
+        g_res.seconds = best;
+        store_tuples(C);
+        int64_t nnz = C->getnnz();
+        delete C;
+        return nnz;
+    }
+    std::unique_ptr<SpDCCols<int64_t, NT>> A(make_dcsc<NT>(m, k, Acp, Ari, Av));
+    std::unique_ptr<SpDCCols<int64_t, NT>> B(make_dcsc<NT>(k, n, Bcp, Bri, Bv));
+    if (variant == 5) {  // PSpGEMM on a 1x1 grid: Mult_AnXBn_Synch + SpTuples->DCSC
+        auto grid = std::make_shared<CommGrid>(MPI_COMM_WORLD, 1, 1);
+        typedef SpParMat<int64_t, NT, SpDCCols<int64_t, NT>> PM;
+        PM PA(new SpDCCols<int64_t, NT>(*A), grid);
+        PM PB(new SpDCCols<int64_t, NT>(*B), grid);
+        double best = 1e300;
+        PM PC(grid);
+        for (int r = 0; r < reps; ++r) {
+            double t0 = now();
+            PC = PSpGEMM<SR>(PA, PB);
+            best = std::min(best, now() - t0);
+        }
+        g_res.seconds = best;
+        store_dcsc(PC.seq());
+        return PC.seq().getnnz();
+    }
+    SpTuples<int64_t, NT> *C = nullptr;
+    double best = 1e300;
+    for (int r = 0; r < reps; ++r) {
+        delete C;
+        double t0 = now();
+        switch (variant) {
+            case 0: C = LocalHybridSpGEMM<SR, NT>(*A, *B, false, false); break;
+            case 1: C = LocalSpGEMM<SR, NT>(*A, *B, false, false); break;
+            case 2: C = LocalSpGEMMHash<SR, NT>(*A, *B, false, false, true); break;
+            case 3: C = LocalSpGEMMHash<SR, NT>(*A, *B, false, false, false); break;
+            default: return -1;
+        }
+        best = std::min(best, now() - t0);
+    }
+    g_res.seconds = best;
+    store_tuples(C);
+    int64_t nnz = C->getnnz();
+    delete C;
+    return nnz;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Semiring codes: 0 PlusTimes<double>, 1 PlusTimes<float>, 2 PlusTimes<int64>,
+// 3 MinPlus<double>, 4 Select2ndMin<int64>, 5 PlusTimes<bool> (or/and),
+// 6 MinPlus<int64>.
+// Variant codes: 0 LocalHybridSpGEMM (DCSC), 1 LocalSpGEMM (heap),
+// 2 LocalSpGEMMHash sorted, 3 LocalSpGEMMHash unsorted, 4 CSC
+// LocalHybridSpGEMM, 5 PSpGEMM on a 1x1 grid.
+int64_t ref_spgemm(int variant, int sr, int64_t m, int64_t k, int64_t n, const int64_t *Acp, const int64_t *Ari,
+                   const void *Av, const int64_t *Bcp, const int64_t *Bri, const void *Bv, int reps)
+{
+    if (reps < 1) reps = 1;
+    switch (sr) {
+        case 0: return run_spgemm<PlusTimesSRing<double, double>, double>(variant, m, k, n, Acp, Ari, Av, Bcp, Bri, Bv, reps);
+        case 1: return run_spgemm<PlusTimesSRing<float, float>, float>(variant, m, k, n, Acp, Ari, Av, Bcp, Bri, Bv, reps);
+        case 2: return run_spgemm<PlusTimesSRing<int64_t, int64_t>, int64_t>(variant, m, k, n, Acp, Ari, Av, Bcp, Bri, Bv, reps);
+        case 3: return run_spgemm<MinPlusSRing<double, double>, double>(variant, m, k, n, Acp, Ari, Av, Bcp, Bri, Bv, reps);
+        case 4: return run_spgemm<HarnessSelect2ndMinSR<int64_t, int64_t>, int64_t>(variant, m, k, n, Acp, Ari, Av, Bcp, Bri, Bv, reps);
+        case 5: return run_spgemm<PlusTimesSRing<bool, bool>, bool>(variant, m, k, n, Acp, Ari, Av, Bcp, Bri, Bv, reps);
+        case 6: return run_spgemm<MinPlusSRing<int64_t, int64_t>, int64_t>(variant, m, k, n, Acp, Ari, Av, Bcp, Bri, Bv, reps);
+        default: return -1;
+    }
+}
+
+void ref_result_copy(int64_t *rows, int64_t *cols, void *vals)
+{
+    if (rows) std::memcpy(rows, g_res.rows.data(), g_res.rows.size() * sizeof(int64_t));
+    if (cols) std::memcpy(cols, g_res.cols.data(), g_res.cols.size() * sizeof(int64_t));
+    if (vals) std::memcpy(vals, g_res.vals.data(), g_res.vals.size());
+}
+
+double ref_result_seconds() { return g_res.seconds; }
+
+// which = 0: estimateFLOP per nonempty column of B; 1: estimateNNZ_Hash.
+// Pattern-only (values ignored).  Returns nzc(B).
+int64_t ref_colstats(int which, int64_t m, int64_t k, int64_t n, const int64_t *Acp, const int64_t *Ari,
+                     const int64_t *Bcp, const int64_t *Bri, int64_t *out)
+{
+    std::unique_ptr<SpDCCols<int64_t, double>> A(make_dcsc<double>(m, k, Acp, Ari, nullptr));
+    std::unique_ptr<SpDCCols<int64_t, double>> B(make_dcsc<double>(k, n, Bcp, Bri, nullptr));
+    if (A->isZero() || B->isZero()) return 0;
+    int64_t nzc = B->GetDCSC()->nzc;
+    int64_t *flop = estimateFLOP(*A, *B);
+    if (which == 0) {
+        std::memcpy(out, flop, nzc * sizeof(int64_t));
+    } else {
+        int64_t *nnz = estimateNNZ_Hash(*A, *B, flop);
+        std::memcpy(out, nnz, nzc * sizeof(int64_t));
+        delete[] nnz;
+    }
+    delete[] flop;
+    return nzc;
+}
+
+// y = A x over SelectMinSR with the CSC bucket algorithm.  x: int32 indices,
+// int64 values.  Result in g_res.rows (row ids) and g_res.vals (int64).
+int64_t ref_spmspv_bucket(int64_t m, int64_t n, const int64_t *Acp, const int64_t *Ari, const int32_t *indx,
+                          const int64_t *numx, int32_t veclen, int buckets)
+{
+    std::unique_ptr<SpCCols<int64_t, bool>> A(make_csc<bool>(m, n, Acp, Ari, nullptr));
+    PreAllocatedSPA<int64_t> SPA(*A, buckets);
+    std::vector<int32_t> indy;
+    std::vector<int64_t> numy;
+    double t0 = now();
+    SpMXSpV_Bucket<HarnessSelectMinSR>(*A->GetCSC(), (int32_t)m, indx, numx, veclen, indy, numy, SPA);
+    g_res.seconds = now() - t0;
+    g_res.rows.assign(indy.begin(), indy.end());
+    g_res.cols.clear();
+    g_res.vals.resize(numy.size() * sizeof(int64_t));
+    std::memcpy(g_res.vals.data(), numy.data(), numy.size() * sizeof(int64_t));
+    return (int64_t)indy.size();
+}
+
+// BFS from `source` over the symmetric pattern A, as the BFS_CSC loop of
+// SpMSpVBench.cpp:105-156: fringe.setNumToInd(); SpMV<SelectMinSR>;
+// EWiseMult(fringe, parents, exclude=true, -1); parents.Set(fringe).
+// parents_out[n] receives the parent array (-1 = unreached); returns the
+// number of level iterations.  levels_out[n] (optional) receives the loop
+// iteration (1-based) at which each vertex first received a parent (0 for
+// the source itself if it never receives one, -1 if unreached).
+int ref_bfs_selectmin(int64_t n, const int64_t *Acp, const int64_t *Ari, int64_t source, int64_t *parents_out,
+                      int64_t *levels_out)
+{
+    auto grid = std::make_shared<CommGrid>(MPI_COMM_WORLD, 1, 1);
+    typedef SpParMat<int64_t, bool, SpCCols<int64_t, bool>> ParCSC;
+    ParCSC A(make_csc<bool>(n, n, Acp, Ari, nullptr), grid);
+    int nthreads = 1;
+#ifdef THREADED
+#pragma omp parallel
+    {
+        nthreads = omp_get_num_threads();
+    }
+#endif
+    PreAllocatedSPA<int64_t> SPA(A.seq(), nthreads * 4);
+    FullyDistVec<int64_t, int64_t> parents(grid, n, (int64_t)-1);
+    FullyDistSpVec<int64_t, int64_t> fringe(grid, n);
+    std::vector<int64_t> level(n, -1);
+    if (levels_out) level[source] = 0;
+    double t0 = now();
+    fringe.SetElement(source, source);
+    int iterations = 0;
+    while (fringe.getnnz() > 0) {
+        fringe.setNumToInd();
+        SpMV<HarnessSelectMinSR>(A, fringe, fringe, false, SPA);
+        fringe = EWiseMult(fringe, parents, true, (int64_t)-1);
+        parents.Set(fringe);
+        iterations++;
+        if (levels_out) {
+            const std::vector<int64_t> &ind = fringe.GetLocalInd();
+            for (int64_t v : ind)
+                if (level[v] < 0) level[v] = iterations;
+        }
+    }
+    g_res.seconds = now() - t0;
+    for (int64_t i = 0; i < n; ++i) parents_out[i] = parents.GetElement(i);
+    if (levels_out) std::memcpy(levels_out, level.data(), n * sizeof(int64_t));
+    return iterations;
+}
+
+// MCL expansion on a 1x1 grid as MCL.cpp:573 calls it with one phase:
+// MemEfficientSpGEMM<PlusTimesSRing<float,float>>(A, A, phases=1,
+// hardThreshold, selectNum, recoverNum, recoverPct, kselectVersion=1,
+// computationKernel=1, perProcessMemory).  Result in g_res (DCSC order).
+int64_t ref_mcl_expand(int64_t n, const int64_t *Acp, const int64_t *Ari, const float *Av, float thr,
+                       int64_t select, int64_t recover_num, float recover_pct)
+{
+    auto grid = std::make_shared<CommGrid>(MPI_COMM_WORLD, 1, 1);
+    typedef SpParMat<int64_t, float, SpDCCols<int64_t, float>> PM;
+    PM A(make_dcsc<float>(n, n, Acp, Ari, Av), grid);
+    PM B(A);
+    double t0 = now();
+    PM C = MemEfficientSpGEMM<PlusTimesSRing<float, float>, float, SpDCCols<int64_t, float>>(
+        A, B, 1, thr, select, recover_num, recover_pct, 1, 1, (int64_t)0);
+    g_res.seconds = now() - t0;
+    store_dcsc(C.seq());
+    return C.seq().getnnz();
+}
+
+int ref_num_threads()
+{
+    int nthreads = 1;
+#ifdef THREADED
+#pragma omp parallel
+    {
+        nthreads = omp_get_num_threads();
+    }
+#endif
+    return nthreads;
+}
+
+}  // extern "C"
