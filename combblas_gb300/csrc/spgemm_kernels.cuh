@@ -1,0 +1,132 @@
+// Shared pieces of the SpGEMM kernels: launch constants, the operand view,
+// block-wide scans and the chunked walk over B-column entries.
+#pragma once
+
+#include <stdint.h>
+
+#include "gbc_internal.cuh"
+
+namespace gbc {
+
+constexpr int kThreads = 256;            // threads per SpGEMM block
+constexpr int kWarps = kThreads / 32;    // owner warps per block
+constexpr int kBuckets = kWarps;         // one staging bucket per owner warp
+constexpr int kStage = 2048;             // products staged per sub-batch
+constexpr int kRounds = kStage / kThreads;
+constexpr int kTileRows = 16384;         // rows of the dense accumulator tile
+constexpr int kSymRows = 1 << 20;        // rows covered by one symbolic bitmap
+constexpr int kMaxMaskWords = 64;        // tile-mask words per column (64 tiles each)
+
+// Device view of the operands after preparation.  Rows of A are int32 and
+// split into T tiles of R rows; tptr[k*(T+1)+t] is the first position in
+// column k of A whose row is >= t*R, so A(tile t, k) is the contiguous range
+// [tptr[k][t], tptr[k][t+1]).
+struct SpgemmArgs {
+    int64_t m, kdim, n, nb;
+    int R, T, mask_words;
+    const int64_t *acp;
+    const int32_t *arow;
+    const uint32_t *tptr;
+    const int64_t *bcp;
+    const int32_t *brow;
+    const int64_t *flop;
+    int32_t *err;
+};
+
+// Block-wide exclusive sum (kThreads threads); *total gets the block total.
+__device__ __forceinline__ int64_t block_exclusive_sum64(int64_t v, int64_t *total)
+{
+    __shared__ int64_t ws[kWarps];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int64_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int64_t s = lane < kWarps ? ws[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < kWarps; o <<= 1) {
+            int64_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < kWarps) ws[lane] = s;
+    }
+    __syncthreads();
+    int64_t base = wid ? ws[wid - 1] : 0;
+    if (total) *total = ws[kWarps - 1];
+    __syncthreads();
+    return base + x - v;
+}
+
+// One chunk of up to kThreads consecutive entries of a B column: for entry
+// b, the A segment [s[b], s[b] + len) restricted to row tiles [t0, t1), and
+// off[] the exclusive prefix of the segment lengths (off[kThreads] = total).
+struct ChunkSmem {
+    uint32_t s[kThreads];
+    int32_t off[kThreads + 1];
+};
+
+template <typename V>
+__device__ __forceinline__ int load_chunk(const SpgemmArgs &a, ChunkSmem &ch, int64_t cb, int64_t be, int t0, int t1,
+                                          const V *bval, V *ch_bv, V one)
+{
+    const int tid = threadIdx.x;
+    const int64_t b = cb + tid;
+    int len = 0;
+    if (b < be) {
+        const int k = a.brow[b];
+        const uint32_t *tp = a.tptr + (int64_t)k * (a.T + 1);
+        const uint32_t s = tp[t0], e = tp[t1];
+        ch.s[tid] = s;
+        len = (int)(e - s);
+        if (ch_bv) ch_bv[tid] = bval ? bval[b] : one;
+    }
+    int64_t tot;
+    const int off = (int)block_exclusive_sum64(len, &tot);
+    ch.off[tid] = off;
+    if (tid == kThreads - 1) ch.off[kThreads] = off + len;
+    __syncthreads();
+    return (int)tot;
+}
+
+__device__ __forceinline__ int load_chunk(const SpgemmArgs &a, ChunkSmem &ch, int64_t cb, int64_t be, int t0, int t1,
+                                          bool, const void *)
+{
+    return load_chunk<int>(a, ch, cb, be, t0, t1, nullptr, nullptr, 0);
+}
+
+// Index b of the chunk entry holding flattened product j (off[b] <= j < off[b+1]).
+__device__ __forceinline__ int chunk_find(const ChunkSmem &ch, int j)
+{
+    int lo = 0, hi = kThreads;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (ch.off[mid] <= j)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+inline size_t numeric_smem_bytes(int R, size_t vsize)
+{
+    size_t b = (size_t)R * vsize;          // accumulator
+    b += (size_t)(R / 32) * 4;             // touched bitmap
+    b = (b + 15) & ~size_t(15);
+    b += (size_t)kStage * vsize;           // staged values
+    b += (size_t)kStage * 2;               // staged row offsets
+    return b;
+}
+
+int prepare_operands(Workspace &ws, const DevMatrix &A, const DevMatrix &B, SpgemmArgs &a, int64_t **acp_out);
+
+template <class SR>
+int spgemm_learned(Context *ctx, const DevMatrix &A, const DevMatrix &B, const gbc_spgemm_opts &opt, int vt,
+                   gbc_result **C, gbc_spgemm_stats *st);
+
+}  // namespace gbc

@@ -1,0 +1,148 @@
+/* gbcomb -- GB300-native node-local sparse kernels for CombBLAS.
+ *
+ * C ABI of the shared library built from combblas_gb300/csrc (libgbcomb.so).
+ * Plain pointers and sizes only.  Every entry point returns an int status
+ * (GBC_OK = 0, negative on error; gbc_last_error() gives the message).
+ *
+ * Matrices are column-compressed with int64 indices, exactly the arrays the
+ * reference keeps:
+ *   DCSC (SpDCCols/Dcsc, dcsc.h:125-131): cp[nzc+1], jc[nzc] (ids of the
+ *        nonempty columns, ascending), ir[nnz] (row ids, ascending within a
+ *        column), numx[nnz];
+ *   CSC  (SpCCols/Csc, csc.h:70-74): jc == NULL, cp has ncol+1 entries.
+ * Inputs may live in host memory (copied to the device inside the call) or
+ * device memory (GBC_DEVICE); results stay on the device and are copied out
+ * with gbc_result_copy().
+ */
+#ifndef GBCOMB_H
+#define GBCOMB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define GBC_OK 0
+#define GBC_EINVAL (-1)      /* bad argument or malformed matrix */
+#define GBC_ENOMEM (-2)      /* device allocation failed */
+#define GBC_ECUDA (-3)       /* CUDA runtime error */
+#define GBC_EOVERFLOW (-4)   /* a size exceeds what the kernels index */
+#define GBC_ETIMEOUT (-5)    /* a bounded device wait gave up */
+#define GBC_EUNSUPPORTED (-6)
+
+/* where a matrix's arrays live */
+#define GBC_HOST 0
+#define GBC_DEVICE 1
+
+/* semirings (Semirings.h and the applications' own) */
+#define GBC_SR_PLUSTIMES 0    /* PlusTimesSRing (Semirings.h:212-232) */
+#define GBC_SR_MINPLUS 1      /* MinPlusSRing (Semirings.h:235-255) */
+#define GBC_SR_SELECT2NDMIN 2 /* Select2ndMinSR (Applications/FastSV.h:25-44) */
+#define GBC_SR_BOOL 3         /* PlusTimesSRing<bool,bool>: or / and */
+
+/* value types */
+#define GBC_F64 0
+#define GBC_F32 1
+#define GBC_I64 2
+#define GBC_BOOL 3 /* 1 byte, 0 or 1 */
+
+/* output row order inside a column */
+#define GBC_SORTED 1   /* LocalHybridSpGEMM / LocalSpGEMMHash(sort=true) */
+#define GBC_UNSORTED 0 /* LocalSpGEMMHash(sort=false); this library still sorts */
+
+/* sizing mode of the SpGEMM */
+#define GBC_SIZING_EXACT 0   /* symbolic pass + numeric pass (two-phase) */
+#define GBC_SIZING_LEARNED 1 /* MLP-predicted capacities, overflow re-run exactly */
+
+typedef struct gbc_context gbc_context;
+typedef struct gbc_result gbc_result;
+
+typedef struct {
+    int64_t nrow, ncol; /* global dimensions */
+    int64_t nzc;        /* number of stored columns (== ncol for CSC) */
+    int64_t nnz;
+    const int64_t *cp;  /* [nzc+1] */
+    const int64_t *jc;  /* [nzc] column ids, or NULL for CSC */
+    const int64_t *ir;  /* [nnz] */
+    const void *num;    /* [nnz] values, or NULL for an all-ones pattern */
+    int where;          /* GBC_HOST or GBC_DEVICE */
+} gbc_matrix;
+
+typedef struct {
+    int sizing;      /* GBC_SIZING_EXACT / GBC_SIZING_LEARNED */
+    int sorted;      /* GBC_SORTED / GBC_UNSORTED */
+    int keep_empty;  /* 1: one output column per stored column of B (SpTuples
+                        view); 0: drop empty output columns (SpDCCols view) */
+    int reserved;
+} gbc_spgemm_opts;
+
+typedef struct {
+    int64_t flops;          /* sum over columns of estimateFLOP */
+    int64_t nnz;            /* nnz(C) */
+    int64_t overflow_cols;  /* learned sizing: columns re-run exactly */
+    int64_t alloc_entries;  /* entries allocated for C before trimming */
+    double ms_total;        /* device time of the call (CUDA events) */
+    double ms_symbolic;
+    double ms_numeric;
+} gbc_spgemm_stats;
+
+/* ---------------------------------------------------------------- context */
+int gbc_context_create(gbc_context **ctx, int device);
+int gbc_context_destroy(gbc_context *ctx);
+/* Use an existing cudaStream_t (passed as void*); NULL selects the
+ * context's own stream. */
+int gbc_context_set_stream(gbc_context *ctx, void *stream);
+int gbc_context_synchronize(gbc_context *ctx);
+const char *gbc_last_error(void);
+int gbc_version(void);
+
+/* ------------------------------------------------------------------ result */
+/* A result is a device matrix owned by the library until gbc_result_free. */
+int gbc_result_info(const gbc_result *r, int64_t *nrow, int64_t *ncol, int64_t *nzc, int64_t *nnz, int *valtype);
+/* Copy out; cp[nzc+1], jc[nzc], ir[nnz], num[nnz].  Any pointer may be NULL.
+ * `where` says whether the destination buffers are host or device memory. */
+int gbc_result_copy(const gbc_result *r, int64_t *cp, int64_t *jc, int64_t *ir, void *num, int where);
+/* Device pointers of the result arrays (valid until gbc_result_free). */
+int gbc_result_device_ptrs(const gbc_result *r, const int64_t **cp, const int64_t **jc, const int64_t **ir,
+                           const void **num);
+int gbc_result_free(gbc_result *r);
+
+/* ------------------------------------------------------------------ SpGEMM */
+/* C = A * B over semiring `sr` with value type `vt` (A and B share it).
+ * Replaces LocalHybridSpGEMM<SR,NTO>(const SpDCCols&, const SpDCCols&,
+ * clearA, clearB, aux) (mtSpGEMM.h:213-217), its CSC overload
+ * (mtSpGEMM.h:1148-1152), LocalSpGEMM (mtSpGEMM.h:74-78) and
+ * LocalSpGEMMHash(..., sort) (mtSpGEMM.h:463-467): same product, rows
+ * ascending within each output column. */
+int gbc_spgemm(gbc_context *ctx, int sr, int vt, const gbc_matrix *A, const gbc_matrix *B,
+               const gbc_spgemm_opts *opts, gbc_result **C, gbc_spgemm_stats *stats);
+
+/* Per-semiring, per-type instantiations of gbc_spgemm (int64 indices). */
+int gbc_spgemm_plustimes_f64_i64(gbc_context *ctx, const gbc_matrix *A, const gbc_matrix *B,
+                                 const gbc_spgemm_opts *opts, gbc_result **C, gbc_spgemm_stats *stats);
+int gbc_spgemm_plustimes_f32_i64(gbc_context *ctx, const gbc_matrix *A, const gbc_matrix *B,
+                                 const gbc_spgemm_opts *opts, gbc_result **C, gbc_spgemm_stats *stats);
+int gbc_spgemm_plustimes_i64_i64(gbc_context *ctx, const gbc_matrix *A, const gbc_matrix *B,
+                                 const gbc_spgemm_opts *opts, gbc_result **C, gbc_spgemm_stats *stats);
+int gbc_spgemm_minplus_f64_i64(gbc_context *ctx, const gbc_matrix *A, const gbc_matrix *B,
+                               const gbc_spgemm_opts *opts, gbc_result **C, gbc_spgemm_stats *stats);
+int gbc_spgemm_minplus_i64_i64(gbc_context *ctx, const gbc_matrix *A, const gbc_matrix *B,
+                               const gbc_spgemm_opts *opts, gbc_result **C, gbc_spgemm_stats *stats);
+int gbc_spgemm_select2ndmin_i64_i64(gbc_context *ctx, const gbc_matrix *A, const gbc_matrix *B,
+                                    const gbc_spgemm_opts *opts, gbc_result **C, gbc_spgemm_stats *stats);
+int gbc_spgemm_bool_i64(gbc_context *ctx, const gbc_matrix *A, const gbc_matrix *B, const gbc_spgemm_opts *opts,
+                        gbc_result **C, gbc_spgemm_stats *stats);
+
+/* Symbolic helpers: per stored column of B, flop = estimateFLOP
+ * (mtSpGEMM.h:1057-1134) and nnz = estimateNNZ_Hash (mtSpGEMM.h:806-933).
+ * Output arrays have B->nzc entries and live where `where` says. */
+int gbc_spgemm_colstats(gbc_context *ctx, const gbc_matrix *A, const gbc_matrix *B, int64_t *flop, int64_t *nnz,
+                        int where);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -144,7 +144,7 @@ static void col_nnz_hash(int64_t n, const int64_t *Acp, const int64_t *Ari, cons
 #define ADD_PT(a, b) ((a) + (b))
 #define MUL_BOOL(a, b) ((uint8_t)((a) && (b)))
 #define ADD_BOOL(a, b) ((uint8_t)((a) || (b)))
-#define ADD_MIN(a, b) ((a) < (b) ? (a) : (b))
+#define ADD_MIN(a, b) ((b) < (a) ? (b) : (a)) /* std::min */
 #define MUL_S2(a, b) (b)
 #define MUL_MPF64(a, b) (((a) == DBL_MAXV || (b) == DBL_MAXV) ? DBL_MAXV : (a) + (b))
 #define MUL_MPI64(a, b) (((a) == INT64_MAX || (b) == INT64_MAX) ? INT64_MAX : (a) + (b))

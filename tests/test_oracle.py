@@ -1,0 +1,148 @@
+"""The oracle against the reference's own outputs (golden fixtures made by
+running the reference) -- CPU only."""
+import numpy as np
+import pytest
+
+from combblas_gb300 import generators as G
+from conftest import golden_matrix
+
+SR_TOL = {0: 1e-12, 1: 1e-5}  # PlusTimes fp64 / fp32 relative tolerance vs the hybrid's heap columns
+
+
+def typed(M, sr, seed, O):
+    dt = O.SR_DTYPE[sr]
+    rng = np.random.default_rng(seed)
+    if dt == np.bool_:
+        return M.with_values(np.ones(M.nnz, np.bool_))
+    if dt == np.int64:
+        return M.with_values(rng.integers(1, 50, M.nnz).astype(np.int64))
+    if M.values is None:
+        return M.with_values((1.0 - rng.random(M.nnz)).astype(dt))
+    return M.astype(dt)
+
+
+def prod_cases(g):
+    keys = sorted({k.rsplit("/", 1)[0] for k in g.files if k.startswith("prod/") and k.endswith("/rows")})
+    return keys
+
+
+def check_csc(cp, rows, vals, g, key, sr, variant, ncol, O, exact_values):
+    gcp, grows, gvals = O.tuples_to_csc(g[f"{key}/rows"], g[f"{key}/cols"], g[f"{key}/vals"], ncol)
+    if variant == O.V_HASH_UNSORTED:
+        cp, rows, vals = O.canonical_csc(cp, rows, vals)
+    assert np.array_equal(cp, gcp), key
+    assert np.array_equal(rows, grows), key
+    if exact_values or sr not in SR_TOL:
+        assert np.array_equal(vals, gvals), key
+    else:
+        rel = np.abs(vals - gvals) / np.maximum(np.abs(gvals), np.finfo(gvals.dtype).tiny)
+        assert rel.max(initial=0) <= SR_TOL[sr], (key, rel.max())
+
+
+def test_port_matches_reference_products(oracle_lib, golden):
+    O = oracle_lib
+    g = golden
+    for key in prod_cases(g):
+        _, name, kind, sr = key.split("/")
+        sr = int(g[f"{key}/sr"])
+        variant = int(g[f"{key}/variant"])
+        if name == "galerkin4":
+            continue
+        if name == "rand_dcsc":
+            A = typed(golden_matrix(g, "rand_dcsc"), sr, 3, O)
+            B = typed(golden_matrix(g, "rand_dcsc_B"), sr, 4, O)
+        else:
+            M = golden_matrix(g, name)
+            A = typed(M, sr, 1, O)
+            B = A if kind != "AAt" else typed(G.transpose(M), sr, 2, O)
+        sorted_ = variant != O.V_HASH_UNSORTED
+        cp, rows, vals = O.port_spgemm(A, B, sr, sorted=sorted_)
+        # the port follows the hash path's summation order: bit-exact against
+        # the hash variants, within tolerance of the hybrid/heap ones
+        exact = variant in (O.V_HASH_SORTED, O.V_HASH_UNSORTED)
+        check_csc(cp, rows, vals, g, key, sr, variant, B.ncol, O, exact)
+        if variant == O.V_HASH_UNSORTED:
+            # slot order of the unsorted hash gather is reproduced exactly
+            _, prow, pval = O.port_spgemm(A, B, sr, sorted=False)
+            assert np.array_equal(prow, g[f"{key}/rows"]) and np.array_equal(pval, g[f"{key}/vals"])
+
+
+def test_port_galerkin(oracle_lib, golden):
+    O = oracle_lib
+    g = golden
+    A = golden_matrix(g, "poisson4")
+    R = golden_matrix(g, "agg4")
+    Rt = G.transpose(R)
+    cp, rows, vals = O.port_spgemm(A, Rt, O.SR_PLUSTIMES_F64)
+    AR = G.CSC(A.nrow, Rt.ncol, cp, rows, vals)
+    cp2, rows2, vals2 = O.port_spgemm(R, AR, O.SR_PLUSTIMES_F64)
+    key = "prod/galerkin4/RAR/0"
+    check_csc(cp2, rows2, vals2, g, key, 0, 0, AR.ncol, O, exact_values=True)
+
+
+def test_port_colstats(oracle_lib, golden):
+    O = oracle_lib
+    for name in ("seven", "nonsym", "torus", "bcsstk01", "rmat8"):
+        M = golden_matrix(golden, name)
+        (_, _, _), (flop, nnz) = O.port_spgemm(M, M, O.SR_PLUSTIMES_F64, want_counts=True)
+        nz = np.diff(M.colptr) > 0
+        assert np.array_equal(flop[nz], golden[f"colstats/{name}/flop"])
+        assert np.array_equal(nnz[nz], golden[f"colstats/{name}/nnz"])
+
+
+def test_port_bfs(oracle_lib, golden):
+    O = oracle_lib
+    for name in ("seven_sym", "torus", "rmat8"):
+        M = golden_matrix(golden, name).with_values(None)
+        for s in golden[f"bfs/{name}/sources"]:
+            par, lev, it = O.port_bfs(M, int(s))
+            assert np.array_equal(par, golden[f"bfs/{name}/{s}/parents"]), (name, s)
+            assert np.array_equal(lev, golden[f"bfs/{name}/{s}/levels"]), (name, s)
+            assert it == int(golden[f"bfs/{name}/{s}/iters"])
+
+
+def test_port_spmspv(oracle_lib, golden):
+    O = oracle_lib
+    M = golden_matrix(golden, "rmat8").with_values(None)
+    yr, yv = O.port_spmspv(M, golden["spmspv/rmat8/x_ind"], golden["spmspv/rmat8/x_val"])
+    assert np.array_equal(yr, golden["spmspv/rmat8/y_ind"])
+    assert np.array_equal(yv, golden["spmspv/rmat8/y_val"])
+
+
+def test_port_mcl(oracle_lib, golden):
+    O = oracle_lib
+    M = golden_matrix(golden, "mcl4096")
+    for thr, k in ((1e-4, 30), (1e-3, 12)):
+        cp, rows, vals = O.port_spgemm(M, M, O.SR_PLUSTIMES_F32, sorted=False)
+        scp, srows, svals = O.port_mcl_select(cp, rows, vals, thr, k)
+        scp, srows, svals = O.canonical_csc(scp, srows, svals)
+        key = f"mcl/mcl4096/{thr:g}/{k}"
+        gcp, grows, gvals = O.tuples_to_csc(golden[f"{key}/rows"], golden[f"{key}/cols"], golden[f"{key}/vals"],
+                                            M.ncol)
+        assert np.array_equal(scp, gcp) and np.array_equal(srows, grows) and np.array_equal(svals, gvals)
+
+
+def test_reference_build_reproduces_golden(oracle_lib, golden):
+    """Where the reference was compiled (this container), it still produces
+    the committed fixtures."""
+    O = oracle_lib
+    if not O.have_ref():
+        pytest.skip("reference sources not present")
+    M = golden_matrix(golden, "rmat8")
+    A = typed(M, O.SR_PLUSTIMES_F64, 1, O)
+    r, c, v, _ = O.ref_spgemm(A, A, O.SR_PLUSTIMES_F64)
+    key = "prod/rmat8/AA/0"
+    assert np.array_equal(r, golden[f"{key}/rows"]) and np.array_equal(v, golden[f"{key}/vals"])
+
+
+def test_oracle_detects_planted_error(oracle_lib, golden):
+    """A mistake planted in the oracle's output (on the CPU) is caught by the
+    comparison used throughout the tests."""
+    O = oracle_lib
+    M = golden_matrix(golden, "rmat8")
+    A = typed(M, O.SR_PLUSTIMES_F64, 1, O)
+    cp, rows, vals = O.port_spgemm(A, A, O.SR_PLUSTIMES_F64, sorted=True)
+    vals = vals.copy()
+    vals[len(vals) // 2] *= 1.0 + 1e-9
+    with pytest.raises(AssertionError):
+        check_csc(cp, rows, vals, golden, "prod/rmat8/AA_hash_sorted/0", 0, O.V_HASH_SORTED, A.ncol, O, True)

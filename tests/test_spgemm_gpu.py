@@ -1,0 +1,177 @@
+"""GPU SpGEMM through the C ABI against the reference's golden outputs and
+the oracle's C restatement."""
+import numpy as np
+import pytest
+
+from combblas_gb300 import generators as G
+from combblas_gb300 import local
+from conftest import golden_matrix
+from test_oracle import prod_cases, typed
+
+pytestmark = pytest.mark.gpu
+
+SR_NAME = {0: ("plustimes", np.float64), 1: ("plustimes", np.float32), 2: ("plustimes", np.int64),
+           3: ("minplus", np.float64), 4: ("select2ndmin", np.int64), 5: ("bool", np.bool_),
+           6: ("minplus", np.int64)}
+TOL = {0: 1e-12, 1: 1e-5}  # PlusTimes fp64 / fp32 (relative), against the hybrid's heap columns
+
+
+def gpu_csc(A, B, sr, **kw):
+    name, dt = SR_NAME[sr]
+    R = local.spgemm(A, B, sr=name, dtype=dt, **kw)
+    return R.to_csc()
+
+
+def assert_same(cp, rows, vals, ecp, erows, evals, sr=None, exact=True, what=""):
+    assert np.array_equal(cp, ecp), what
+    assert np.array_equal(rows, erows), what
+    if exact or sr not in TOL:
+        assert np.array_equal(vals, evals), what
+    else:
+        rel = np.abs(vals - evals) / np.maximum(np.abs(evals), np.finfo(evals.dtype).tiny)
+        assert rel.max(initial=0) <= TOL[sr], (what, rel.max())
+
+
+def test_golden_products(gpu_ctx, oracle_lib, golden):
+    O = oracle_lib
+    g = golden
+    for key in prod_cases(g):
+        _, name, kind, _ = key.split("/")
+        sr = int(g[f"{key}/sr"])
+        variant = int(g[f"{key}/variant"])
+        if name == "galerkin4":
+            continue
+        if name == "rand_dcsc":
+            A = typed(golden_matrix(g, "rand_dcsc"), sr, 3, O)
+            B = typed(golden_matrix(g, "rand_dcsc_B"), sr, 4, O)
+        else:
+            M = golden_matrix(g, name)
+            A = typed(M, sr, 1, O)
+            B = A if kind != "AAt" else typed(G.transpose(M), sr, 2, O)
+        cp, rows, vals = gpu_csc(A, B, sr)
+        ecp, erows, evals = O.tuples_to_csc(g[f"{key}/rows"], g[f"{key}/cols"], g[f"{key}/vals"], B.ncol)
+        exact = variant in (O.V_HASH_SORTED, O.V_HASH_UNSORTED)
+        assert_same(cp, rows, vals, ecp, erows, evals, sr, exact, key)
+        # bit-exact against the oracle (same summation order)
+        pcp, prow, pval = O.port_spgemm(A, B, sr)
+        assert_same(cp, rows, vals, pcp, prow, pval, sr, True, key + " vs port")
+
+
+def test_golden_galerkin(gpu_ctx, oracle_lib, golden):
+    O = oracle_lib
+    A = golden_matrix(golden, "poisson4")
+    R = golden_matrix(golden, "agg4")
+    Rt = G.transpose(R)
+    cp, rows, vals = gpu_csc(A, Rt, 0)
+    AR = G.CSC(A.nrow, Rt.ncol, cp, rows, vals)
+    cp2, rows2, vals2 = gpu_csc(R, AR, 0)
+    key = "prod/galerkin4/RAR/0"
+    ecp, erows, evals = O.tuples_to_csc(golden[f"{key}/rows"], golden[f"{key}/cols"], golden[f"{key}/vals"], AR.ncol)
+    assert_same(cp2, rows2, vals2, ecp, erows, evals, 0, True, key)
+
+
+@pytest.mark.parametrize("scale,ef", [(12, 8), (14, 8), (15, 4)])
+def test_rmat_fp64_bitexact_vs_port(gpu_ctx, oracle_lib, scale, ef):
+    O = oracle_lib
+    A = G.rmat(scale, ef, seed=scale)
+    cp, rows, vals = gpu_csc(A, A, 0)
+    pcp, prow, pval = O.port_spgemm(A, A, O.SR_PLUSTIMES_F64)
+    assert_same(cp, rows, vals, pcp, prow, pval, 0, True, f"rmat{scale}")
+    # repeated runs are bit-identical
+    cp2, rows2, vals2 = gpu_csc(A, A, 0)
+    assert np.array_equal(vals, vals2) and np.array_equal(rows, rows2)
+
+
+@pytest.mark.parametrize("sr", [1, 2, 3, 4, 5, 6])
+def test_rmat_semirings_vs_port(gpu_ctx, oracle_lib, sr):
+    O = oracle_lib
+    A = typed(G.rmat(13, 6, seed=21), sr, 5, O)
+    cp, rows, vals = gpu_csc(A, A, sr)
+    pcp, prow, pval = O.port_spgemm(A, A, sr)
+    assert_same(cp, rows, vals, pcp, prow, pval, sr, True, f"sr{sr}")
+
+
+def test_tall_matrix_many_tiles(gpu_ctx, oracle_lib):
+    """m > 1M rows: several row tiles and several symbolic bitmaps."""
+    O = oracle_lib
+    A = G.random_sparse(1_500_000, 400, 2e-5, seed=2)
+    B = G.random_sparse(400, 300, 0.05, seed=3)
+    cp, rows, vals = gpu_csc(A, B, 0)
+    pcp, prow, pval = O.port_spgemm(A, B, O.SR_PLUSTIMES_F64)
+    assert_same(cp, rows, vals, pcp, prow, pval, 0, True, "tall")
+
+
+def test_dcsc_inputs_and_views(gpu_ctx, oracle_lib):
+    O = oracle_lib
+    A = G.random_sparse(500, 400, 0.01, seed=8, empty_cols=0.4)
+    B = G.random_sparse(400, 350, 0.02, seed=9, empty_cols=0.4)
+    Ad, Bd = local.DCSC.from_csc(A), local.DCSC.from_csc(B)
+    R = local.spgemm(Ad, Bd, keep_empty=True)
+    cp, jc, ir, num = R.to_host()
+    assert np.array_equal(jc, Bd.jc)  # SpTuples view: one column per stored column of B
+    full, rows, vals = R.to_csc()
+    pcp, prow, pval = O.port_spgemm(A, B, O.SR_PLUSTIMES_F64)
+    assert_same(full, rows, vals, pcp, prow, pval, 0, True, "dcsc")
+    R2 = local.spgemm(Ad, Bd, keep_empty=False)  # SpDCCols view drops empty output columns
+    cp2, jc2, ir2, num2 = R2.to_host()
+    nzcols = np.nonzero(np.diff(pcp))[0]
+    assert np.array_equal(jc2, nzcols) and np.array_equal(ir2, prow) and np.array_equal(num2, pval)
+
+
+def test_device_resident_inputs(gpu_ctx, oracle_lib):
+    O = oracle_lib
+    A = G.rmat(11, 8, seed=4)
+    Ad = local.DeviceMatrix.from_host(A)
+    cp, rows, vals = local.spgemm(Ad, Ad).to_csc()
+    pcp, prow, pval = O.port_spgemm(A, A, O.SR_PLUSTIMES_F64)
+    assert_same(cp, rows, vals, pcp, prow, pval, 0, True, "device")
+
+
+def test_edge_cases(gpu_ctx, oracle_lib):
+    O = oracle_lib
+    # empty operands -> empty product with the right shape (mtSpGEMM.h:224-227)
+    Z = G.CSC(50, 40, np.zeros(41, np.int64), np.zeros(0, np.int64), np.zeros(0))
+    B = G.random_sparse(40, 30, 0.1, seed=1)
+    R = local.spgemm(Z, B)
+    assert R.nnz == 0 and R.nrow == 50 and R.ncol == 30
+    # 1x1
+    one = G.CSC(1, 1, np.array([0, 1]), np.array([0]), np.array([3.0]))
+    cp, rows, vals = local.spgemm(one, one).to_csc()
+    assert list(rows) == [0] and list(vals) == [9.0]
+    # a fully dense column in A and in B
+    A = G.random_sparse(300, 300, 0.01, seed=2)
+    dense_rows = np.arange(300)
+    rows = np.concatenate([A.rowidx, dense_rows])
+    cols = np.concatenate([A.col_ids(), np.full(300, 7)])
+    D = G.csc_from_coo(300, 300, rows, cols)
+    D.values = np.linspace(0.1, 1.0, D.nnz)
+    cp, rows, vals = local.spgemm(D, D).to_csc()
+    pcp, prow, pval = O.port_spgemm(D, D, O.SR_PLUSTIMES_F64)
+    assert_same(cp, rows, vals, pcp, prow, pval, 0, True, "dense column")
+
+
+def test_errors_are_reported(gpu_ctx):
+    from combblas_gb300._lib import GbcError
+
+    A = G.random_sparse(30, 20, 0.2, seed=1)
+    with pytest.raises(GbcError, match="inner dimensions"):
+        local.spgemm(A, A)
+    # rows not ascending within a column: rejected by the validation pass
+    bad = G.CSC(4, 2, np.array([0, 2, 3]), np.array([3, 1, 0]), np.ones(3))
+    sq = G.CSC(2, 2, np.array([0, 1, 2]), np.array([0, 1]), np.ones(2))
+    with pytest.raises(GbcError, match="ascending"):
+        local.spgemm(bad, sq)
+    # row id out of range
+    bad2 = G.CSC(4, 2, np.array([0, 1, 2]), np.array([1, 9]), np.ones(2))
+    with pytest.raises(GbcError, match="out of range"):
+        local.spgemm(bad2, sq)
+
+
+def test_colstats_vs_reference(gpu_ctx, golden):
+    for name in ("seven", "nonsym", "torus", "bcsstk01", "rmat8"):
+        M = golden_matrix(golden, name)
+        D = local.DCSC.from_csc(M)
+        flop = local.estimateFLOP(D, D)
+        nnz = local.estimateNNZ_Hash(D, D)
+        assert np.array_equal(flop, golden[f"colstats/{name}/flop"]), name
+        assert np.array_equal(nnz, golden[f"colstats/{name}/nnz"]), name
