@@ -1,0 +1,435 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 local SpGEMM / SpMSpV path.
+
+Default workload (the headline): C = A*A on an R-MAT of scale 20, edge
+factor 16 (a,b,c,d = .57,.19,.19,.05, symmetrized, no self-loops, seeded),
+PlusTimes over fp64 with int64 indices, computed in column phases because
+nnz(C) ~ 2.4e10 exceeds device memory; each phase's output is written to
+HBM and reduced to checksums.  Metric: Gmults/s (multiplications as the
+reference's estimateFLOP counts them, divided by time).  The same line also
+carries BFS GTEPS on the same graph (64 seeded roots, SelectMin parents).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload spgemm20|bfs20|spgemm14]
+
+--impl reference times the CPU implementation of the same path on the host
+cores (the oracle's C restatement of the reference's algorithm, OpenMP over
+all cores) on a bounded column sample of the same workload.
+
+N > 1 runs independent replicas, one per GPU (the path is not sharded here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SEED = 1
+BFS_ROOTS = 64
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, p[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- helpers
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def bytes_alg(nnzA, n, nnzC, s_i=8, s_v=8):
+    """Algorithmic bytes of one SpGEMM A*A: A and B read once, C written once."""
+    return 2 * (nnzA * (s_i + s_v) + (n + 1) * s_i) + nnzC * (s_i + s_v) + (n + 1) * s_i
+
+
+def column_sample(A, frac: float, seed: int = 7):
+    """B = A(:, cols) for a seeded random subset of columns (CSC)."""
+    from combblas_gb300.generators import CSC
+
+    rng = np.random.default_rng(seed)
+    k = max(1, int(A.ncol * frac))
+    cols = np.sort(rng.choice(A.ncol, k, replace=False))
+    cnt = np.diff(A.colptr)[cols]
+    cp = np.concatenate([[0], np.cumsum(cnt)]).astype(np.int64)
+    idx = np.concatenate([np.arange(A.colptr[c], A.colptr[c + 1]) for c in cols]) if k else np.zeros(0, np.int64)
+    return CSC(A.nrow, k, cp, A.rowidx[idx], None if A.values is None else A.values[idx]), cols
+
+
+def cpu_spgemm_rate(A, budget_s: float):
+    """Oracle (C restatement, all host threads) on a column sample sized for
+    ~budget_s seconds: returns (Gmults/s, sample description, threads)."""
+    import oracle as O
+
+    frac = 1.0 / 4096
+    while True:
+        B, cols = column_sample(A, frac)
+        t0 = time.perf_counter()
+        (_, _, _), (flop, cnt) = O.port_spgemm(A, B, O.SR_PLUSTIMES_F64, want_counts=True)
+        dt = time.perf_counter() - t0
+        if dt > budget_s / 4 or frac >= 1.0:
+            break
+        frac = min(1.0, frac * max(2.0, budget_s / 2 / max(dt, 1e-3)))
+    flops = int(flop.sum())
+    return flops / dt / 1e9, f"A*A(:,{len(cols)} seeded random columns) = {flops:.3e} mults in {dt:.2f}s", \
+        O.port_num_threads()
+
+
+def cpu_bfs_rate(A, roots, budget_s: float):
+    import oracle as O
+
+    P = A.with_values(None)
+    deg = np.diff(P.colptr)
+    edges, secs, used = 0, 0.0, 0
+    for r in roots:
+        t0 = time.perf_counter()
+        par, lev, it = O.port_bfs(P, int(r), with_levels=True)
+        secs += time.perf_counter() - t0
+        reached = (par >= 0)
+        reached[int(r)] = True
+        edges += int(deg[reached].sum()) // 2
+        used += 1
+        if secs > budget_s:
+            break
+    return edges / secs / 1e9, f"{used} BFS roots", O.port_num_threads()
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def max_over_ranks(x: float, world: int, device=None) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def make_graph(workload):
+    from combblas_gb300 import generators as G
+
+    scale, ef = (14, 8) if workload == "spgemm14" else (20, 16)
+    t0 = time.perf_counter()
+    A = G.rmat(scale, ef, seed=SEED)
+    log(f"generated R-MAT scale {scale} ef {ef}: n={A.ncol} nnz={A.nnz} in {time.perf_counter() - t0:.1f}s")
+    return A, scale, ef
+
+
+def bfs_roots(A, k=BFS_ROOTS):
+    deg = np.diff(A.colptr)
+    rng = np.random.default_rng(SEED + 100)
+    return rng.choice(np.nonzero(deg)[0], k, replace=False)
+
+
+# -------------------------------------------------------------- reference
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    A, scale, ef = make_graph(args.workload)
+    import oracle as O
+
+    O.build(quiet=True) if not os.path.exists(O._PORT_SO) else None
+    budget = 20.0
+    steps = []
+    desc, threads = "", 1
+    if args.workload == "bfs20":
+        roots = bfs_roots(A)
+        for s in range(args.warmup + args.steps):
+            v, desc, threads = cpu_bfs_rate(A, roots[s % len(roots):], budget / 4)
+            if s >= args.warmup:
+                steps.append(v)
+        metric, unit = "BFS GTEPS (R-MAT s20 ef16, SelectMin parents)", "GTEPS"
+    else:
+        for s in range(args.warmup + args.steps):
+            v, desc, threads = cpu_spgemm_rate(A, budget / 2)
+            if s >= args.warmup:
+                steps.append(v)
+        metric, unit = f"SpGEMM Gmults/s (R-MAT s{scale} ef{ef} A*A, PlusTimes fp64)", "Gmults/s"
+    val = float(np.median(steps))
+    line = {
+        "impl": "reference", "metric": metric, "value": val, "unit": unit, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded R-MAT)",
+        "config": {"workload": args.workload, "scale": scale, "edge_factor": ef, "seed": SEED},
+        "cpu_baseline": {"value": val, "unit": unit, "cores": threads, "kind": "port",
+                         "sample": desc + " per step; the reference's CPU algorithm as restated in oracle/oracle.c "
+                                          "(the reference sources are not on this machine)"},
+        "e2e": {"value": val, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------- ours
+def run_ours(args, world, rank, local):
+    import torch
+
+    torch.cuda.set_device(local)
+    from combblas_gb300 import _lib
+    from combblas_gb300 import bfs as B
+    from combblas_gb300 import local as LC
+
+    A, scale, ef = make_graph(args.workload)
+    ctx = LC.Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    hbm, peak_kind = peaks()
+    Ad = LC.DeviceMatrix.from_host(A)
+    torch.cuda.synchronize()
+    budget = args.phase_nnz
+    result: dict = {}
+
+    # ---- SpGEMM, inputs resident in HBM -------------------------------
+    def spgemm_step():
+        return LC.spgemm_phased(Ad, Ad, max_phase_nnz=budget, ctx=ctx)
+
+    if args.workload in ("spgemm20", "spgemm14"):
+        for _ in range(args.warmup):
+            st = spgemm_step()
+        torch.cuda.synchronize()
+        barrier(world)
+        clocks = ClockSampler(local)
+        clocks.start()
+        l0 = _lib.lib().gbc_launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        sym_ms = num_ms = 0.0
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            st = spgemm_step()
+            sym_ms += st.ms_symbolic
+            num_ms += st.ms_numeric
+        e1.record(stream)
+        torch.cuda.synchronize()
+        launches = _lib.lib().gbc_launch_count() - l0
+        ms = e0.elapsed_time(e1)
+        ck = clocks.stop()
+        ms = max_over_ranks(ms, world, "cuda")
+        barrier(world)
+        flops = st.flops
+        value = flops * args.steps * world / (ms * 1e-3) / 1e9
+        ba = bytes_alg(A.nnz, A.ncol, st.nnz)
+        # dominant kernel (numeric): algorithmic bytes over its launch time
+        # (A re-read per phase is counted once per phase launch)
+        ba_num = st.phases * (A.nnz * 16 + (A.ncol + 1) * 8) + (A.nnz * 16 + (A.ncol + 1) * 8) + \
+            st.nnz * 16 + (A.ncol + 1) * 8
+        achieved = ba_num / (num_ms / args.steps * 1e-3) / 1e9
+        result.update({
+            "metric": f"SpGEMM Gmults/s (R-MAT s{scale} ef{ef} A*A, PlusTimes fp64, exact two-phase sizing, "
+                      "column phases)",
+            "value": value, "unit": "Gmults/s", "ms_per_step": ms / args.steps,
+            "spgemm": {"flops": flops, "nnz_c": st.nnz, "phases": st.phases, "max_phase_nnz": st.max_phase_nnz,
+                       "ms_symbolic": sym_ms / args.steps, "ms_numeric": num_ms / args.steps,
+                       "row_checksum": st.row_checksum, "val_checksum": st.val_checksum,
+                       "bytes_alg": ba, "roofline_frac_whole_step": ba / (ms / args.steps * 1e-3) / 1e9 / hbm},
+            "roofline": {"bound": "hbm", "kernel": "k_numeric", "achieved": achieved, "peak": hbm,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": None, "traffic_note": "dram bytes per launch: see profiles/"},
+            "gpu_launches": launches,
+            "clocks": ck,
+        })
+        # ---- e2e: host (pinned) buffers through the public C ABI ---------
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        hcp, hir, hv = pin(A.colptr), pin(A.rowidx), pin(A.values)
+
+        class _H:
+            pass
+
+        Ah = _H()
+        Ah.nrow, Ah.ncol, Ah.colptr, Ah.rowidx, Ah.values = A.nrow, A.ncol, hcp.numpy(), hir.numpy(), hv.numpy()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            st_e = LC.spgemm_phased(Ah, Ah, max_phase_nnz=budget, ctx=ctx)
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        e2e_s = max_over_ranks(e2e_s, world, "cuda")
+        h2d = 2 * (hcp.numel() * 8 + hir.numel() * 8 + hv.numel() * 8)
+        d2h = st_e.phases * 0 + A.ncol * 8 + 64  # per-column counts read back to cut phases + stats
+        result["e2e"] = {"value": st_e.flops * args.steps * world / e2e_s / 1e9, "unit": "Gmults/s",
+                         "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                         "path": "gbc_spgemm_phased with host pinned A/B (H2D inside the call), checksums read back"}
+        assert st_e.nnz == st.nnz and st_e.row_checksum == st.row_checksum
+
+    # ---- BFS (configs[1]): 64 roots, level loop as a replayed CUDA graph --
+    g = B.Graph(A.with_values(None), ctx)
+    par = torch.empty(A.ncol, dtype=torch.int64, device="cuda")
+    lev = torch.empty(A.ncol, dtype=torch.int64, device="cuda")
+    roots = bfs_roots(A)
+    for r in roots[:3]:
+        B.bfs_device(g, int(r), par.data_ptr(), lev.data_ptr())
+    torch.cuda.synchronize()
+    edges = 0
+    l0 = _lib.lib().gbc_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if args.workload == "bfs20":
+        clocks = ClockSampler(local)
+        clocks.start()
+    e0.record(stream)
+    for r in roots:
+        st_b = B.bfs_device(g, int(r), par.data_ptr(), lev.data_ptr())
+        edges += st_b.edges
+    e1.record(stream)
+    torch.cuda.synchronize()
+    bfs_ms = e0.elapsed_time(e1)
+    gteps = edges / (bfs_ms * 1e-3) / 1e9
+    bfs_launches = _lib.lib().gbc_launch_count() - l0
+    result["bfs"] = {"gteps": gteps, "roots": len(roots), "ms_total": bfs_ms, "edges": edges,
+                     "semiring": "SelectMin (min parent)", "loop": "captured CUDA graph per level"}
+    if args.workload == "bfs20":
+        result.update({"metric": "BFS GTEPS (R-MAT s20 ef16, 64 roots, SelectMin parents)", "value": gteps * world,
+                       "unit": "GTEPS", "ms_per_step": bfs_ms / len(roots), "gpu_launches": bfs_launches,
+                       "clocks": clocks.stop()})
+        # e2e: host graph upload each step
+        t0 = time.perf_counter()
+        P = A.with_values(None)
+        e_edges = 0
+        for r in roots[:8]:
+            par_h, lev_h, st_h = B.bfs(P, int(r), ctx=ctx)
+            e_edges += st_h.edges
+        e2e_s = time.perf_counter() - t0
+        result["e2e"] = {"value": e_edges / e2e_s / 1e9, "unit": "GTEPS",
+                         "h2d_bytes_per_step": (A.colptr.nbytes + A.rowidx.nbytes),
+                         "d2h_bytes_per_step": 2 * A.ncol * 8}
+        achieved = edges * 2 * 4 / (bfs_ms * 1e-3) / 1e9
+        result["roofline"] = {"bound": "hbm", "kernel": "k_bfs_expand", "achieved": achieved, "peak": hbm,
+                              "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm, "traffic": None}
+
+    # ---- CPU baseline (rank 0, N=1 only) -------------------------------
+    if rank == 0 and world == 1 and not args.no_cpu:
+        if args.workload == "bfs20":
+            v, desc, th = cpu_bfs_rate(A, roots[:8], 15.0)
+            result["cpu_baseline"] = {"value": v, "unit": "GTEPS", "cores": th, "kind": "port", "sample": desc}
+        else:
+            v, desc, th = cpu_spgemm_rate(A, 15.0)
+            result["cpu_baseline"] = {"value": v, "unit": "Gmults/s", "cores": th, "kind": "port",
+                                      "sample": desc + " (oracle/oracle.c: the reference's hash-path algorithm)"}
+    line = {
+        "metric": result["metric"], "value": result["value"], "unit": result["unit"], "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": result["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.workload != "bfs20" else "int64",
+        "data": "synthetic (seeded R-MAT, numpy generator)",
+        "config": {"workload": args.workload, "scale": scale, "edge_factor": ef, "seed": SEED,
+                   "rmat_abcd": [0.57, 0.19, 0.19, 0.05], "index": "int64",
+                   "phase_budget_nnz": budget, "l2": "inputs and outputs larger than L2 (129 MB)",
+                   "parallelism": f"replicas x{world}"},
+    }
+    for k in ("roofline", "cpu_baseline", "e2e", "gpu_launches", "clocks", "spgemm", "bfs"):
+        if k in result:
+            line[k] = result[k]
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["spgemm20", "bfs20", "spgemm14"], default="spgemm20")
+    ap.add_argument("--phase-nnz", type=int, default=3 << 30)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        if not os.path.exists(os.path.join(ROOT, "combblas_gb300", "libgbcomb.so")):
+            from combblas_gb300 import build as BLD
+
+            BLD.build()
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

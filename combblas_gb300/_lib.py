@@ -54,6 +54,14 @@ class gbc_spgemm_stats(C.Structure):
     ]
 
 
+class gbc_phased_stats(C.Structure):
+    _fields_ = [
+        ("flops", C.c_int64), ("nnz", C.c_int64), ("phases", C.c_int64), ("max_phase_nnz", C.c_int64),
+        ("row_checksum", C.c_int64), ("val_checksum", C.c_double), ("ms_total", C.c_double),
+        ("ms_symbolic", C.c_double), ("ms_numeric", C.c_double),
+    ]
+
+
 class gbc_bfs_stats(C.Structure):
     _fields_ = [
         ("iterations", C.c_int64), ("reached", C.c_int64), ("edges", C.c_int64), ("ms", C.c_double),
@@ -66,6 +74,7 @@ _lib = None
 _SIGS = {
     "gbc_last_error": (C.c_char_p, []),
     "gbc_version": (C.c_int, []),
+    "gbc_launch_count": (C.c_int64, []),
     "gbc_context_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int]),
     "gbc_context_destroy": (C.c_int, [C.c_void_p]),
     "gbc_context_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -78,6 +87,8 @@ _SIGS = {
     "gbc_result_free": (C.c_int, [C.c_void_p]),
     "gbc_spgemm": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(gbc_matrix), C.POINTER(gbc_matrix),
                              C.POINTER(gbc_spgemm_opts), C.POINTER(C.c_void_p), C.POINTER(gbc_spgemm_stats)]),
+    "gbc_spgemm_phased": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(gbc_matrix), C.POINTER(gbc_matrix),
+                                    C.c_int64, C.POINTER(gbc_phased_stats)]),
     "gbc_spgemm_colstats": (C.c_int, [C.c_void_p, C.POINTER(gbc_matrix), C.POINTER(gbc_matrix), C.c_void_p,
                                       C.c_void_p, C.c_int]),
 }
@@ -86,6 +97,14 @@ for _n in ("plustimes_f64", "plustimes_f32", "plustimes_i64", "minplus_f64", "mi
                                                C.POINTER(gbc_spgemm_opts), C.POINTER(C.c_void_p),
                                                C.POINTER(gbc_spgemm_stats)])
 _SIGS["gbc_spgemm_bool_i64"] = _SIGS["gbc_spgemm_plustimes_f64_i64"]
+_SIGS.update({
+    "gbc_graph_create": (C.c_int, [C.c_void_p, C.POINTER(gbc_matrix), C.POINTER(C.c_void_p)]),
+    "gbc_graph_destroy": (C.c_int, [C.c_void_p]),
+    "gbc_spmspv_select2ndmin_i64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
+                                              C.c_void_p, C.POINTER(C.c_int32), C.c_int]),
+    "gbc_bfs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.POINTER(gbc_bfs_stats),
+                          C.c_int]),
+})
 
 # entry points added by later modules register here (see extend_signatures)
 _EXTRA: dict = {}

@@ -1,0 +1,68 @@
+"""SpMSpV over SelectMin and the BFS built on it -- host mirror of
+``SpMXSpV_Bucket`` (SpImpl.cpp:389) and the BFS_CSC level loop of
+Applications/SpMSpV-IPDPS2017/SpMSpVBench.cpp:128-156.  GPU only."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from .local import Context, DeviceMatrix, as_gbc_matrix, default_context
+
+
+class Graph:
+    """Square pattern matrix prepared once on the device (gbc_graph)."""
+
+    def __init__(self, A, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        keep: list = []
+        g = as_gbc_matrix(A, keep, None)
+        g.num = None
+        self.h = C.c_void_p()
+        L.check(L.lib().gbc_graph_create(self.ctx.h, C.byref(g), C.byref(self.h)))
+        self.n = int(A.ncol)
+        self.colptr = A.colptr if not isinstance(A, DeviceMatrix) else None
+
+    def close(self):
+        if self.h:
+            L.lib().gbc_graph_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def SpMXSpV(graph: Graph, indx: np.ndarray, numx: np.ndarray):
+    """y = A x over SelectMin: returns (indy int32 sorted, numy int64)."""
+    indx = np.ascontiguousarray(indx, np.int32)
+    numx = np.ascontiguousarray(numx, np.int64)
+    indy = np.empty(graph.n, np.int32)
+    numy = np.empty(graph.n, np.int64)
+    ny = C.c_int32()
+    L.check(L.lib().gbc_spmspv_select2ndmin_i64(graph.ctx.h, graph.h, indx.ctypes.data, numx.ctypes.data, len(indx),
+                                                indy.ctypes.data, numy.ctypes.data, C.byref(ny), L.GBC_HOST))
+    return indy[:ny.value].copy(), numy[:ny.value].copy()
+
+
+def bfs(A_or_graph, source: int, ctx: Context | None = None):
+    """BFS from ``source``: (parents int64[n], levels int64[n], stats)."""
+    g = A_or_graph if isinstance(A_or_graph, Graph) else Graph(A_or_graph, ctx)
+    parents = np.empty(g.n, np.int64)
+    levels = np.empty(g.n, np.int64)
+    st = L.gbc_bfs_stats()
+    L.check(L.lib().gbc_bfs(g.ctx.h, g.h, int(source), parents.ctypes.data, levels.ctypes.data, C.byref(st),
+                            L.GBC_HOST))
+    return parents, levels, st
+
+
+def bfs_device(graph: Graph, source: int, parents_ptr: int, levels_ptr: int):
+    """BFS writing into caller device buffers (int64[n] each); the level
+    loop then runs as a captured CUDA graph."""
+    st = L.gbc_bfs_stats()
+    L.check(L.lib().gbc_bfs(graph.ctx.h, graph.h, int(source), C.c_void_p(parents_ptr), C.c_void_p(levels_ptr),
+                            C.byref(st), L.GBC_DEVICE))
+    return st

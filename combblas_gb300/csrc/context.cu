@@ -1,6 +1,7 @@
 // Context, memory, results, uploads and device-wide scans of libgbcomb.
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 
 #include "gbc_internal.cuh"
@@ -8,6 +9,9 @@
 namespace gbc {
 
 static thread_local std::string g_err;
+static std::atomic<long long> g_launches{0};
+
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 void set_error(const std::string &msg) { g_err = msg; }
 
@@ -191,16 +195,16 @@ int exclusive_scan_i64(Workspace &ws, const int64_t *in, int64_t *out, int64_t n
     }
     int64_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
     if (tiles == 1) {
-        k_tile_scan<<<1, SCAN_THREADS, 0, s>>>(in, out, n, nullptr);
+        k_tile_scan<<<1, SCAN_THREADS, 0, s>>>(in, out, n, nullptr); ::gbc::note_launch();
         GBC_CUDA_TRY(cudaGetLastError());
         return GBC_OK;
     }
     int64_t *sums = nullptr;
     GBC_TRY(ws.alloc_n(&sums, tiles + 1));
-    k_tile_sums<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(in, n, sums);
+    k_tile_sums<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(in, n, sums); ::gbc::note_launch();
     GBC_CUDA_TRY(cudaGetLastError());
     GBC_TRY(exclusive_scan_i64(ws, sums, sums, tiles, s));
-    k_tile_scan<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(in, out, n, sums);
+    k_tile_scan<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(in, out, n, sums); ::gbc::note_launch();
     GBC_CUDA_TRY(cudaGetLastError());
     return GBC_OK;
 }
@@ -215,6 +219,8 @@ extern "C" {
 const char *gbc_last_error(void) { return g_err.c_str(); }
 
 int gbc_version(void) { return 1; }
+
+int64_t gbc_launch_count(void) { return (int64_t)g_launches.load(); }
 
 int gbc_context_create(gbc_context **out, int device)
 {

@@ -30,6 +30,10 @@ int fail(int code, const std::string &msg);
         if (_s != GBC_OK) return _s; \
     } while (0)
 
+// Count of kernel launches issued by this library (all contexts, this
+// process); reported by gbc_launch_count().
+void note_launch();
+
 // ---------------------------------------------------------------- context
 struct Context {
     int device = 0;

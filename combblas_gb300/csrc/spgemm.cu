@@ -223,127 +223,193 @@ __global__ void __launch_bounds__(kThreads) k_symbolic(SpgemmArgs a, int64_t *cn
 }
 
 // ----------------------------------------------------------------- numeric
+// One block per column (dynamic counter); for every row tile t the column
+// touches:
+//  * dense accumulator acc[R] and touched bitmap in shared memory;
+//  * the column's B entries are walked in chunks of kThreads; the chunk's A
+//    segments restricted to tile t form a flattened product list, processed
+//    in sub-batches of kSub products.  Segment ids of a sub-batch come from a
+//    block max-scan over segment-start markers;
+//  * staging: all threads load the sub-batch's rows and values with
+//    coalesced reads (one load per product), multiply by B(k,j) and store
+//    them to shared memory in flattened (k-major) order;
+//  * folding: every warp walks every 32-product window of the staged list
+//    but folds only the rows of its 32-row stripes (stripe mod kWarps), in
+//    window order.  A window inside one A segment has distinct rows; a
+//    window spanning segments groups equal rows with __match_any_sync and the
+//    lowest lane folds the group in lane order.  Each output entry is thus
+//    the left fold acc = add(mrhs, acc) over k ascending.
+constexpr int kSub = 4096;
+constexpr int kSubPerThread = kSub / kThreads;
+
+// Inclusive max-scan of seg[0..n) (uint8 segment-start markers, 0 where no
+// segment starts) seeded with `seed`: seg[j] = id of the segment holding j.
+__device__ __forceinline__ void seg_max_scan(uint8_t *seg, int seed)
+{
+    __shared__ int ws[kWarps];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    uint8_t loc[kSubPerThread];
+    *reinterpret_cast<uint4 *>(loc) = *reinterpret_cast<const uint4 *>(seg + tid * kSubPerThread);
+    int run = 0;
+#pragma unroll
+    for (int u = 0; u < kSubPerThread; ++u) run = max(run, (int)loc[u]);
+    int x = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x = max(x, y);
+    }
+    if (lane == 31) ws[wid] = x;
+    __syncthreads();
+    int pre = seed;
+    for (int w = 0; w < wid; ++w) pre = max(pre, ws[w]);
+    int excl = __shfl_up_sync(0xffffffffu, x, 1);
+    if (lane > 0) pre = max(pre, excl);
+    int cur = pre;
+#pragma unroll
+    for (int u = 0; u < kSubPerThread; ++u) {
+        cur = max(cur, (int)loc[u]);
+        loc[u] = (uint8_t)cur;
+    }
+    *reinterpret_cast<uint4 *>(seg + tid * kSubPerThread) = *reinterpret_cast<const uint4 *>(loc);
+    __syncthreads();
+}
+
 template <class SR>
-__global__ void __launch_bounds__(kThreads) k_numeric(SpgemmArgs a, const void *aval_v, const void *bval_v,
-                                                      const uint64_t *tmask, const int64_t *ccp, int64_t *cir,
-                                                      void *cval_v, unsigned long long *work)
+__global__ void __launch_bounds__(kThreads, 1) k_numeric(SpgemmArgs a, const void *aval_v, const void *bval_v,
+                                                         const uint64_t *tmask, const int64_t *ccp, int64_t *cir,
+                                                         void *cval_v, unsigned long long *work)
 {
     typedef typename SR::V V;
     extern __shared__ __align__(16) unsigned char smem[];
-    V *acc = reinterpret_cast<V *>(smem);                                 // [R]
-    uint32_t *bm = reinterpret_cast<uint32_t *>(acc + a.R);               // [R/32]
-    V *sval = reinterpret_cast<V *>(bm + (a.R >> 5));                     // [kStage]
-    uint16_t *srow = reinterpret_cast<uint16_t *>(sval + kStage);         // [kStage]
+    V *acc = reinterpret_cast<V *>(smem);                            // [R]
+    V *sval = acc + a.R;                                             // [kSub]
+    uint32_t *bm = reinterpret_cast<uint32_t *>(sval + kSub);        // [R/32]
+    uint16_t *srow = reinterpret_cast<uint16_t *>(bm + (a.R >> 5));  // [kSub]
+    uint8_t *seg = reinterpret_cast<uint8_t *>(srow + kSub);         // [kSub]
     __shared__ ChunkSmem ch;
     __shared__ V ch_bv[kThreads];
-    __shared__ int32_t s_cnt[kBuckets * kRounds * kWarps + 1];
+    __shared__ int32_t s_cnt[kWarps * kSubPerThread * kWarps + 1];  // [owner][round][warp]
     __shared__ int64_t s_col;
     const V *aval = static_cast<const V *>(aval_v);
     const V *bval = static_cast<const V *>(bval_v);
     V *cval = static_cast<V *>(cval_v);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned lt = (1u << lane) - 1;
     const int words = a.R >> 5;
+    constexpr int NC = kWarps * kSubPerThread * kWarps;
 
     for (;;) {
-        if (tid == 0) s_col = (int64_t)atomicAdd(work, 1ull);
+        if (tid == 0) s_col = a.col_begin + (int64_t)atomicAdd(work, 1ull);
         __syncthreads();
-        int64_t i = s_col;
+        const int64_t i = s_col;
         __syncthreads();
-        if (i >= a.nb) break;
-        int64_t bs = a.bcp[i], be = a.bcp[i + 1];
-        int64_t out = ccp[i];
-        const int64_t lim = ccp[i + 1];
+        if (i >= a.col_end) break;
+        const int64_t bs = a.bcp[i], be = a.bcp[i + 1];
+        // ccp is indexed relative to the first column of this pass
+        int64_t out = ccp[i - a.col_begin];
+        const int64_t lim = ccp[i - a.col_begin + 1];
         for (int mw = 0; mw < a.mask_words; ++mw) {
             uint64_t msk = tmask[i * a.mask_words + mw];
             while (msk) {
-                int t = mw * 64 + __ffsll((long long)msk) - 1;
+                const int t = mw * 64 + __ffsll((long long)msk) - 1;
                 msk &= msk - 1;
-                int row0 = t * a.R;
+                const int row0 = t * a.R;
                 for (int w = tid; w < words; w += kThreads) bm[w] = 0;
                 __syncthreads();
                 for (int64_t cb = bs; cb < be; cb += kThreads) {
-                    int L = load_chunk<V>(a, ch, cb, be, t, t + 1, bval, ch_bv, SR::one());
-                    for (int q = 0; q < L; q += kStage) {
-                        // 1. load this sub-batch (round-major), owner = 32-row stripe mod 8
-                        int rows_[kRounds];
-                        V vals_[kRounds];
-                        int own_[kRounds];
-                        int rnk_[kRounds];
+                    const int L = load_chunk<V>(a, ch, cb, be, t, t + 1, bval, ch_bv, SR::one());
+                    const int myoff = ch.off[tid], mylen = ch.off[tid + 1] - myoff;
+                    for (int q = 0; q < L; q += kSub) {
+                        const int n = min(kSub, L - q);
+                        // 1. segment ids of products q .. q+n-1
+                        *reinterpret_cast<uint4 *>(seg + tid * kSubPerThread) = make_uint4(0, 0, 0, 0);
+                        __syncthreads();
+                        if (mylen > 0 && myoff >= q && myoff < q + n) seg[myoff - q] = (uint8_t)tid;
+                        __syncthreads();
+                        seg_max_scan(seg, chunk_find(ch, q));
+                        // 2. load (round-major, all loads in flight), owner = 32-row stripe mod kWarps
+                        int o_[kSubPerThread];
+                        V v_[kSubPerThread];
 #pragma unroll
-                        for (int r = 0; r < kRounds; ++r) {
-                            int j = q + r * kThreads + tid;
-                            int o = -1;
-                            V v = V();
-                            if (j < L) {
-                                int b = chunk_find(ch, j);
-                                int64_t idx = ch.s[b] + (j - ch.off[b]);
-                                o = a.arow[idx] - row0;
-                                V av = aval ? aval[idx] : SR::one();
-                                v = SR::mul(av, ch_bv[b]);
+                        for (int r = 0; r < kSubPerThread; ++r) {
+                            const int j = r * kThreads + tid;
+                            o_[r] = -1;
+                            if (j < n) {
+                                const int b = seg[j];
+                                const int64_t idx = (int64_t)ch.s[b] + (q + j - ch.off[b]);
+                                o_[r] = a.arow[idx] - row0;
+                                const V av = aval ? aval[idx] : SR::one();
+                                v_[r] = SR::mul(av, ch_bv[b]);
                             }
-                            rows_[r] = o;
-                            vals_[r] = v;
-                            int ow = o >= 0 ? ((o >> 5) & (kWarps - 1)) : kBuckets;
-                            own_[r] = ow;
-                            int rk = 0;
+                        }
+                        // 3. stable partition by owner: rank within (round, warp) from 3 ballots
+                        int rk_[kSubPerThread];
 #pragma unroll
-                            for (int bk = 0; bk < kBuckets; ++bk) {
-                                unsigned m = __ballot_sync(0xffffffffu, ow == bk);
-                                if (ow == bk) rk = __popc(m & ((1u << lane) - 1));
-                                if (lane == 0) s_cnt[(bk * kRounds + r) * kWarps + warp] = __popc(m);
+                        for (int r = 0; r < kSubPerThread; ++r) {
+                            const bool act = o_[r] >= 0;
+                            const int w = (o_[r] >> 5) & (kWarps - 1);
+                            const unsigned va = __ballot_sync(0xffffffffu, act);
+                            const unsigned b0 = __ballot_sync(0xffffffffu, act && (w & 1));
+                            const unsigned b1 = __ballot_sync(0xffffffffu, act && (w & 2));
+                            const unsigned b2 = __ballot_sync(0xffffffffu, act && (w & 4));
+                            const unsigned same = va & ((w & 1) ? b0 : ~b0) & ((w & 2) ? b1 : ~b1) & ((w & 4) ? b2 : ~b2);
+                            rk_[r] = __popc(same & lt);
+                            // lanes 0..kWarps-1 publish the size of owner `lane`'s group (0 if absent)
+                            if (lane < kWarps) {
+                                const unsigned sl = va & ((lane & 1) ? b0 : ~b0) & ((lane & 2) ? b1 : ~b1) &
+                                                    ((lane & 4) ? b2 : ~b2);
+                                s_cnt[(lane * kSubPerThread + r) * kWarps + warp] = __popc(sl);
                             }
-                            rnk_[r] = rk;
                         }
                         __syncthreads();
-                        // 2. exclusive scan of the (bucket, round, warp) counts
+                        // 4. exclusive scan of the (owner, round, warp) counts
                         {
-                            constexpr int N = kBuckets * kRounds * kWarps;
-                            constexpr int PER = (N + kThreads - 1) / kThreads;
+                            constexpr int PER = (NC + kThreads - 1) / kThreads;
                             int loc[PER];
                             int sum = 0;
 #pragma unroll
                             for (int u = 0; u < PER; ++u) {
-                                int idx = tid * PER + u;
-                                loc[u] = idx < N ? s_cnt[idx] : 0;
+                                loc[u] = s_cnt[tid * PER + u];
                                 sum += loc[u];
                             }
                             int64_t tot64;
                             int base = (int)block_exclusive_sum64(sum, &tot64);
 #pragma unroll
                             for (int u = 0; u < PER; ++u) {
-                                int idx = tid * PER + u;
-                                if (idx < N) s_cnt[idx] = base;
+                                s_cnt[tid * PER + u] = base;
                                 base += loc[u];
                             }
-                            if (tid == 0) s_cnt[N] = (int)tot64;
+                            if (tid == 0) s_cnt[NC] = (int)tot64;
                         }
                         __syncthreads();
-                        // 3. scatter into the staging buffer
+                        // 5. scatter into owner buckets
 #pragma unroll
-                        for (int r = 0; r < kRounds; ++r) {
-                            if (own_[r] < kBuckets) {
-                                int pos = s_cnt[(own_[r] * kRounds + r) * kWarps + warp] + rnk_[r];
-                                srow[pos] = (uint16_t)rows_[r];
-                                sval[pos] = vals_[r];
+                        for (int r = 0; r < kSubPerThread; ++r) {
+                            if (o_[r] >= 0) {
+                                const int w = (o_[r] >> 5) & (kWarps - 1);
+                                const int pos = s_cnt[(w * kSubPerThread + r) * kWarps + warp] + rk_[r];
+                                srow[pos] = (uint16_t)o_[r];
+                                sval[pos] = v_[r];
                             }
                         }
                         __syncthreads();
-                        // 4. each warp folds its own bucket in staging order
+                        // 6. each warp folds its bucket in staging (= k) order
                         {
-                            int beg = s_cnt[(warp * kRounds) * kWarps];
-                            int end = s_cnt[((warp + 1) * kRounds) * kWarps];
+                            const int beg = s_cnt[(warp * kSubPerThread) * kWarps];
+                            const int end = s_cnt[((warp + 1) * kSubPerThread) * kWarps];
                             for (int p0 = beg; p0 < end; p0 += 32) {
-                                int p = p0 + lane;
-                                bool act = p < end;
-                                int o = act ? (int)srow[p] : (0x10000 + lane);
-                                unsigned grp = __match_any_sync(0xffffffffu, o);
-                                if (act && (__ffs(grp) - 1) == lane) {
-                                    uint32_t bit = 1u << (o & 31);
-                                    bool touched = (bm[o >> 5] & bit) != 0;
+                                const int p = p0 + lane;
+                                const bool act = p < end;
+                                const int o = act ? (int)srow[p] : (0x10000 + lane);
+                                const unsigned grp = __match_any_sync(0xffffffffu, o);
+                                if (act && (grp & lt) == 0) {
+                                    const uint32_t bit = 1u << (o & 31);
+                                    const bool touched = (bm[o >> 5] & bit) != 0;
                                     V cur = touched ? SR::add(sval[p], acc[o]) : sval[p];
                                     unsigned rest = grp & ~(1u << lane);
                                     while (rest) {
-                                        int m = __ffs(rest) - 1;
+                                        const int m = __ffs(rest) - 1;
                                         rest &= rest - 1;
                                         cur = SR::add(sval[p0 + m], cur);
                                     }
@@ -356,20 +422,21 @@ __global__ void __launch_bounds__(kThreads) k_numeric(SpgemmArgs a, const void *
                         __syncthreads();
                     }
                 }
-                // 5. write the tile's entries in row order
+                // write the tile's entries in row order: warp-cooperative over
+                // 32-word groups so stores stay contiguous
                 {
+                    int wl = 0;
                     const int wpt = (words + kThreads - 1) / kThreads;
                     const int w0 = min(words, tid * wpt), w1 = min(words, (tid + 1) * wpt);
-                    int wl = 0;
                     for (int w = w0; w < w1; ++w) wl += __popc(bm[w]);
                     int64_t tot;
                     int64_t pos = out + block_exclusive_sum64(wl, &tot);
                     for (int w = w0; w < w1; ++w) {
                         uint32_t x = bm[w];
                         while (x) {
-                            int bit = __ffs(x) - 1;
+                            const int bit = __ffs(x) - 1;
                             x &= x - 1;
-                            int o = w * 32 + bit;
+                            const int o = w * 32 + bit;
                             if (pos < lim) {
                                 cir[pos] = (int64_t)row0 + o;
                                 cval[pos] = acc[o];
@@ -443,24 +510,24 @@ int prepare_operands(Workspace &ws, const DevMatrix &A, const DevMatrix &B, Spge
     GBC_TRY(ws.alloc_n(&tptr, (size_t)A.ncol * (a.T + 1) + 1));
     if (A.jc) {
         GBC_TRY(ws.alloc_n(&acp, A.ncol + 1));
-        k_dense_colptr<<<(unsigned)((A.nzc + 1 + 255) / 256), 256, 0, s>>>(A.ncol, A.nzc, A.cp, A.jc, acp);
+        k_dense_colptr<<<(unsigned)((A.nzc + 1 + 255) / 256), 256, 0, s>>>(A.ncol, A.nzc, A.cp, A.jc, acp); ::gbc::note_launch();
         GBC_CUDA_TRY(cudaGetLastError());
     } else {
         acp = const_cast<int64_t *>(A.cp);
     }
     if (A.nzc > 0) {
         k_prep_a<<<grid_for(ctx, (A.nzc + 7) / 8, 8), 256, 0, s>>>(A.ncol, A.nrow, A.cp, A.jc, A.nzc, A.nnz,
-                                                                     A.ir, arow, tptr, a.T, a.R, err);
+                                                                     A.ir, arow, tptr, a.T, a.R, err); ::gbc::note_launch();
         GBC_CUDA_TRY(cudaGetLastError());
     }
     if (A.ncol > 0) {
-        k_fill_empty_tptr<<<(unsigned)((A.ncol + 255) / 256), 256, 0, s>>>(A.ncol, acp, tptr, a.T);
+        k_fill_empty_tptr<<<(unsigned)((A.ncol + 255) / 256), 256, 0, s>>>(A.ncol, acp, tptr, a.T); ::gbc::note_launch();
         GBC_CUDA_TRY(cudaGetLastError());
     }
     int32_t *brow = nullptr;
     GBC_TRY(ws.alloc_n(&brow, B.nnz + 1));
     if (B.nzc > 0) {
-        k_prep_b<<<grid_for(ctx, (B.nzc + 7) / 8, 8), 256, 0, s>>>(B.nzc, B.nnz, B.cp, B.ir, A.ncol, brow, err);
+        k_prep_b<<<grid_for(ctx, (B.nzc + 7) / 8, 8), 256, 0, s>>>(B.nzc, B.nnz, B.cp, B.ir, A.ncol, brow, err); ::gbc::note_launch();
         GBC_CUDA_TRY(cudaGetLastError());
     }
     int32_t herr[4];
@@ -505,8 +572,10 @@ static int spgemm_exact(Context *ctx, const DevMatrix &A, const DevMatrix &B, co
     GBC_TRY(ws.alloc_n(&work, 8));
     GBC_CUDA_TRY(cudaMemsetAsync(work, 0, 8 * sizeof(unsigned long long), s));
     a.flop = flop;
+    a.col_begin = 0;
+    a.col_end = nb;
     if (nb > 0) {
-        k_flop<<<grid_for(ctx, (nb + 7) / 8, 8), 256, 0, s>>>(nb, B.cp, a.brow, acp, flop);
+        k_flop<<<grid_for(ctx, (nb + 7) / 8, 8), 256, 0, s>>>(nb, B.cp, a.brow, acp, flop); ::gbc::note_launch();
         GBC_CUDA_TRY(cudaGetLastError());
     }
     // symbolic
@@ -518,7 +587,7 @@ static int spgemm_exact(Context *ctx, const DevMatrix &A, const DevMatrix &B, co
         GBC_CUDA_TRY(cudaFuncSetAttribute(k_symbolic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sym_smem));
         int per_sm = std::max(1, (int)(ctx->smem_optin / (sym_smem + 8192)));
         k_symbolic<<<grid_for(ctx, nb, std::min(per_sm, 8)), kThreads, sym_smem, s>>>(a, cnt, tmask, sup_rows,
-                                                                                          work);
+                                                                                          work); ::gbc::note_launch();
         GBC_CUDA_TRY(cudaGetLastError());
     }
     GBC_TRY(device_alloc(ctx, (void **)&ccp, (nb + 1) * sizeof(int64_t)));
@@ -553,7 +622,7 @@ static int spgemm_exact(Context *ctx, const DevMatrix &A, const DevMatrix &B, co
         GBC_CUDA_TRY(cudaFuncSetAttribute(k_numeric<SR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)num_smem));
         int per_sm = std::max(1, (int)(ctx->smem_optin / (num_smem + 12288)));
         k_numeric<SR><<<grid_for(ctx, nb, std::min(per_sm, 8)), kThreads, num_smem, s>>>(
-            a, A.num, B.num, tmask, ccp, C->ir, C->num, work + 2);
+            a, A.num, B.num, tmask, ccp, C->ir, C->num, work + 2); ::gbc::note_launch();
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) {
             gbc_result_free(C);
@@ -569,11 +638,11 @@ static int spgemm_exact(Context *ctx, const DevMatrix &A, const DevMatrix &B, co
             gbc_result_free(C);
             return rc;
         }
-        if (nb > 0) k_iota_jc<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(nb, B.jc, C->jc);
+        if (nb > 0) k_iota_jc<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(nb, B.jc, C->jc); ::gbc::note_launch();
     } else {
         int64_t *flags = nullptr;
         GBC_TRY(ws.alloc_n(&flags, nb + 1));
-        k_nonempty_flags<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(nb, cnt, flags);
+        k_nonempty_flags<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(nb, cnt, flags); ::gbc::note_launch();
         GBC_TRY(exclusive_scan_i64(ws, flags, flags, nb, s));
         int64_t nzc = 0;
         GBC_TRY(read_i64(ctx, flags + nb, &nzc));
@@ -586,7 +655,7 @@ static int spgemm_exact(Context *ctx, const DevMatrix &A, const DevMatrix &B, co
             return rc;
         }
         GBC_CUDA_TRY(cudaMemsetAsync(cp2, 0, sizeof(int64_t), s));
-        k_compact_cols<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(nb, cnt, flags, ccp, B.jc, cp2, jc2);
+        k_compact_cols<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(nb, cnt, flags, ccp, B.jc, cp2, jc2); ::gbc::note_launch();
         device_free(ctx, C->cp);
         C->cp = cp2;
         C->jc = jc2;
@@ -626,6 +695,176 @@ static int spgemm_exact(Context *ctx, const DevMatrix &A, const DevMatrix &B, co
         st->ms_numeric = t23;
     }
     *Cout = C;
+    return GBC_OK;
+}
+
+
+// ------------------------------------------------------- column phases
+// Deterministic checksums of one phase's output: block partial sums over
+// contiguous ranges (fixed grid), combined in block order on the host.
+template <typename V>
+__global__ void k_phase_checksum(const int64_t *ir, const V *num, int64_t nnz, int64_t *rsum, double *vsum)
+{
+    __shared__ double sv[kWarps];
+    __shared__ long long sr[kWarps];
+    const int64_t per = (nnz + gridDim.x - 1) / gridDim.x;
+    const int64_t b0 = min(nnz, per * blockIdx.x), b1 = min(nnz, b0 + per);
+    double v = 0;
+    long long r = 0;
+    for (int64_t p = b0 + threadIdx.x; p < b1; p += blockDim.x) {
+        v += (double)num[p];
+        r += ir[p];
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+        r += __shfl_xor_sync(0xffffffffu, r, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        sv[threadIdx.x >> 5] = v;
+        sr[threadIdx.x >> 5] = r;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tv = 0;
+        long long tr = 0;
+        for (int w = 0; w < kWarps; ++w) {
+            tv += sv[w];
+            tr += sr[w];
+        }
+        vsum[blockIdx.x] = tv;
+        rsum[blockIdx.x] = tr;
+    }
+}
+
+// C = A*B computed in phases of B's stored columns so that each phase's
+// output holds at most max_phase_nnz entries -- the reference's column
+// phases of MemEfficientSpGEMM (ParFriends.h:553-556, ColSplit).  Each
+// phase's C is written to HBM and reduced to checksums; nothing is kept.
+template <class SR>
+static int spgemm_phased(Context *ctx, const DevMatrix &A, const DevMatrix &B, int64_t max_phase_nnz,
+                         gbc_phased_stats *st)
+{
+    typedef typename SR::V V;
+    cudaStream_t s = ctx->stream;
+    Workspace ws(ctx);
+    cudaEventRecord(ctx->ev[0], s);
+    SpgemmArgs a{};
+    int64_t *acp = nullptr;
+    GBC_TRY(prepare_operands(ws, A, B, a, &acp));
+    const int64_t nb = B.nzc;
+    int64_t *flop = nullptr, *cnt = nullptr, *fsum = nullptr;
+    uint64_t *tmask = nullptr;
+    unsigned long long *work = nullptr;
+    GBC_TRY(ws.alloc_n(&flop, nb + 1));
+    GBC_TRY(ws.alloc_n(&fsum, nb + 1));
+    GBC_TRY(ws.alloc_n(&cnt, nb + 1));
+    GBC_TRY(ws.alloc_n(&tmask, (size_t)nb * a.mask_words + 1));
+    GBC_TRY(ws.alloc_n(&work, 8));
+    GBC_CUDA_TRY(cudaMemsetAsync(work, 0, 8 * sizeof(unsigned long long), s));
+    a.flop = flop;
+    if (nb > 0) {
+        k_flop<<<grid_for(ctx, (nb + 7) / 8, 8), 256, 0, s>>>(nb, B.cp, a.brow, acp, flop); ::gbc::note_launch();
+        GBC_CUDA_TRY(cudaGetLastError());
+    }
+    int sup_rows = (int)std::min<int64_t>((int64_t)kSymRows, (int64_t)a.T * a.R);
+    sup_rows = (sup_rows / a.R) * a.R;
+    size_t sym_smem = (size_t)sup_rows / 8;
+    cudaEventRecord(ctx->ev[1], s);
+    if (nb > 0) {
+        GBC_CUDA_TRY(cudaFuncSetAttribute(k_symbolic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sym_smem));
+        int per_sm = std::max(1, (int)(ctx->smem_optin / (sym_smem + 8192)));
+        k_symbolic<<<grid_for(ctx, nb, std::min(per_sm, 8)), kThreads, sym_smem, s>>>(a, cnt, tmask, sup_rows,
+                                                                                          work); ::gbc::note_launch();
+        GBC_CUDA_TRY(cudaGetLastError());
+    }
+    cudaEventRecord(ctx->ev[2], s);
+    std::vector<int64_t> hcnt(nb > 0 ? nb : 1);
+    if (nb > 0) GBC_CUDA_TRY(cudaMemcpyAsync(hcnt.data(), cnt, nb * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    GBC_TRY(exclusive_scan_i64(ws, flop, fsum, nb, s));
+    int64_t flops = 0;
+    GBC_TRY(read_i64(ctx, fsum + nb, &flops));
+    // phase boundaries (greedy, a column bigger than the budget is alone)
+    std::vector<int64_t> bounds{0};
+    int64_t acc = 0, maxp = 0, total = 0;
+    for (int64_t j = 0; j < nb; ++j) {
+        if (acc > 0 && acc + hcnt[j] > max_phase_nnz) {
+            bounds.push_back(j);
+            maxp = std::max(maxp, acc);
+            acc = 0;
+        }
+        acc += hcnt[j];
+        total += hcnt[j];
+    }
+    maxp = std::max(maxp, acc);
+    if (bounds.back() != nb) bounds.push_back(nb);
+    int64_t maxcols = 0;
+    for (size_t p = 0; p + 1 < bounds.size(); ++p) maxcols = std::max(maxcols, bounds[p + 1] - bounds[p]);
+    int64_t *ir = nullptr, *ccp = nullptr, *rsum = nullptr;
+    V *num = nullptr;
+    double *vsum = nullptr;
+    const int csb = ctx->num_sms * 2;
+    GBC_TRY(ws.alloc_n(&ir, maxp + 1));
+    GBC_TRY(ws.alloc_n(&num, maxp + 1));
+    GBC_TRY(ws.alloc_n(&ccp, maxcols + 1));
+    GBC_TRY(ws.alloc_n(&rsum, (size_t)csb * (bounds.size() + 1)));
+    GBC_TRY(ws.alloc_n(&vsum, (size_t)csb * (bounds.size() + 1)));
+    size_t num_smem = numeric_smem_bytes(a.R, sizeof(V));
+    GBC_CUDA_TRY(cudaFuncSetAttribute(k_numeric<SR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)num_smem));
+    int per_sm = std::max(1, (int)(ctx->smem_optin / (num_smem + 12288)));
+    double ms_num = 0;
+    const int np = (int)bounds.size() - 1;
+    for (int p = 0; p < np; ++p) {
+        const int64_t j0 = bounds[p], j1 = bounds[p + 1];
+        GBC_TRY(exclusive_scan_i64(ws, cnt + j0, ccp, j1 - j0, s));
+        GBC_CUDA_TRY(cudaMemsetAsync(work + 2, 0, sizeof(unsigned long long), s));
+        a.col_begin = j0;
+        a.col_end = j1;
+        cudaEventRecord(ctx->ev[5], s);
+        k_numeric<SR><<<grid_for(ctx, j1 - j0, std::min(per_sm, 8)), kThreads, num_smem, s>>>(
+            a, A.num, B.num, tmask, ccp, ir, num, work + 2); ::gbc::note_launch();
+        GBC_CUDA_TRY(cudaGetLastError());
+        cudaEventRecord(ctx->ev[6], s);
+        int64_t pn = 0;
+        for (int64_t j = j0; j < j1; ++j) pn += hcnt[j];
+        k_phase_checksum<V><<<csb, kThreads, 0, s>>>(ir, num, pn, rsum + (size_t)p * csb, vsum + (size_t)p * csb); ::gbc::note_launch();
+        GBC_CUDA_TRY(cudaGetLastError());
+        GBC_CUDA_TRY(cudaEventSynchronize(ctx->ev[6]));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev[5], ctx->ev[6]);
+        ms_num += ms;
+    }
+    cudaEventRecord(ctx->ev[4], s);
+    std::vector<int64_t> hr((size_t)csb * np + 1);
+    std::vector<double> hv((size_t)csb * np + 1);
+    if (np > 0) {
+        GBC_CUDA_TRY(cudaMemcpyAsync(hr.data(), rsum, (size_t)csb * np * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        GBC_CUDA_TRY(cudaMemcpyAsync(hv.data(), vsum, (size_t)csb * np * sizeof(double), cudaMemcpyDeviceToHost, s));
+    }
+    int32_t herr = 0;
+    GBC_CUDA_TRY(cudaMemcpyAsync(&herr, a.err, sizeof(herr), cudaMemcpyDeviceToHost, s));
+    GBC_CUDA_TRY(cudaStreamSynchronize(s));
+    if (herr) return fail(GBC_ECUDA, "internal error: numeric and symbolic counts disagree");
+    if (st) {
+        float t04 = 0, t12 = 0;
+        cudaEventElapsedTime(&t04, ctx->ev[0], ctx->ev[4]);
+        cudaEventElapsedTime(&t12, ctx->ev[1], ctx->ev[2]);
+        st->flops = flops;
+        st->nnz = total;
+        st->phases = np;
+        st->ms_total = t04;
+        st->ms_symbolic = t12;
+        st->ms_numeric = ms_num;
+        int64_t rs = 0;
+        double vs = 0;
+        for (size_t k = 0; k < (size_t)csb * np; ++k) {
+            rs += hr[k];
+            vs += hv[k];
+        }
+        st->row_checksum = rs;
+        st->val_checksum = vs;
+        st->max_phase_nnz = maxp;
+    }
     return GBC_OK;
 }
 
@@ -680,12 +919,12 @@ int spgemm_colstats(gbc_context *ctx, const gbc_matrix *Am, const gbc_matrix *Bm
     GBC_CUDA_TRY(cudaMemsetAsync(work, 0, 4 * sizeof(unsigned long long), s));
     a.flop = flop;
     if (nb > 0) {
-        k_flop<<<grid_for(ctx, (nb + 7) / 8, 8), 256, 0, s>>>(nb, B.cp, a.brow, acp, flop);
+        k_flop<<<grid_for(ctx, (nb + 7) / 8, 8), 256, 0, s>>>(nb, B.cp, a.brow, acp, flop); ::gbc::note_launch();
         int sup_rows = (int)std::min<int64_t>((int64_t)kSymRows, (int64_t)a.T * a.R);
         sup_rows = (sup_rows / a.R) * a.R;
         size_t sym_smem = (size_t)sup_rows / 8;
         GBC_CUDA_TRY(cudaFuncSetAttribute(k_symbolic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sym_smem));
-        k_symbolic<<<grid_for(ctx, nb, 2), kThreads, sym_smem, s>>>(a, cnt, tmask, sup_rows, work);
+        k_symbolic<<<grid_for(ctx, nb, 2), kThreads, sym_smem, s>>>(a, cnt, tmask, sup_rows, work); ::gbc::note_launch();
         GBC_CUDA_TRY(cudaGetLastError());
     }
     cudaMemcpyKind k = where == GBC_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
@@ -739,6 +978,24 @@ GBC_SPGEMM_INST(gbc_spgemm_minplus_f64_i64, GBC_SR_MINPLUS, GBC_F64)
 GBC_SPGEMM_INST(gbc_spgemm_minplus_i64_i64, GBC_SR_MINPLUS, GBC_I64)
 GBC_SPGEMM_INST(gbc_spgemm_select2ndmin_i64_i64, GBC_SR_SELECT2NDMIN, GBC_I64)
 GBC_SPGEMM_INST(gbc_spgemm_bool_i64, GBC_SR_BOOL, GBC_BOOL)
+
+int gbc_spgemm_phased(gbc_context *ctx, int sr, int vt, const gbc_matrix *Am, const gbc_matrix *Bm,
+                      int64_t max_phase_nnz, gbc_phased_stats *st)
+{
+    if (!ctx) return fail(GBC_EINVAL, "null context");
+    if (!Am || !Bm || Am->ncol != Bm->nrow) return fail(GBC_EINVAL, "inner dimensions do not match");
+    if (max_phase_nnz <= 0) return fail(GBC_EINVAL, "phase budget must be positive");
+    GBC_CUDA_TRY(cudaSetDevice(ctx->device));
+    Workspace ws(ctx);
+    DevMatrix A, B;
+    GBC_TRY(upload(ws, Am, vt, &A));
+    GBC_TRY(upload(ws, Bm, vt, &B));
+    if (sr == GBC_SR_PLUSTIMES && vt == GBC_F64) return spgemm_phased<PlusTimes<double>>(ctx, A, B, max_phase_nnz, st);
+    if (sr == GBC_SR_PLUSTIMES && vt == GBC_F32) return spgemm_phased<PlusTimes<float>>(ctx, A, B, max_phase_nnz, st);
+    if (sr == GBC_SR_SELECT2NDMIN && vt == GBC_I64)
+        return spgemm_phased<Select2ndMin<int64_t>>(ctx, A, B, max_phase_nnz, st);
+    return fail(GBC_EUNSUPPORTED, "phased SpGEMM is instantiated for PlusTimes f64/f32 and Select2ndMin i64");
+}
 
 int gbc_spgemm_colstats(gbc_context *ctx, const gbc_matrix *A, const gbc_matrix *B, int64_t *flop, int64_t *nnz,
                         int where)

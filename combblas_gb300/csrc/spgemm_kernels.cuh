@@ -31,6 +31,7 @@ struct SpgemmArgs {
     const int32_t *brow;
     const int64_t *flop;
     int32_t *err;
+    int64_t col_begin, col_end;  // numeric pass: stored columns [col_begin, col_end) of B
 };
 
 // Block-wide exclusive sum (kThreads threads); *total gets the block total.
@@ -115,12 +116,11 @@ __device__ __forceinline__ int chunk_find(const ChunkSmem &ch, int j)
 
 inline size_t numeric_smem_bytes(int R, size_t vsize)
 {
-    size_t b = (size_t)R * vsize;          // accumulator
-    b += (size_t)(R / 32) * 4;             // touched bitmap
-    b = (b + 15) & ~size_t(15);
-    b += (size_t)kStage * vsize;           // staged values
-    b += (size_t)kStage * 2;               // staged row offsets
-    return b;
+    // acc[R] + sval[4096] (values) + bitmap[R/32] + srow[4096] (u16) + seg[4096] (u8)
+    size_t b = (size_t)R * vsize + (size_t)4096 * vsize;
+    b += (size_t)(R / 32) * 4;
+    b += (size_t)4096 * 2 + 4096;
+    return (b + 15) & ~size_t(15);
 }
 
 int prepare_operands(Workspace &ws, const DevMatrix &A, const DevMatrix &B, SpgemmArgs &a, int64_t **acp_out);

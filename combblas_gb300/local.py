@@ -267,6 +267,21 @@ def spgemm(A, B, sr: str = "plustimes", sizing: str = "exact", sorted: bool = Tr
     return SpResult(out, st)
 
 
+def spgemm_phased(A, B, sr: str = "plustimes", max_phase_nnz: int = 1 << 31, ctx: Context | None = None,
+                  dtype=None) -> L.gbc_phased_stats:
+    """C = A * B in column phases of at most ``max_phase_nnz`` output entries;
+    returns the statistics and checksums (the product is not kept)."""
+    ctx = ctx or default_context()
+    dt = np.dtype(dtype) if dtype is not None else _value_dtype(A, B, sr)
+    keep: list = []
+    ga = as_gbc_matrix(A, keep, dt)
+    gb = as_gbc_matrix(B, keep, dt)
+    st = L.gbc_phased_stats()
+    L.check(L.lib().gbc_spgemm_phased(ctx.h, SR_CODES[sr], VT_OF_DTYPE[dt], C.byref(ga), C.byref(gb),
+                                      int(max_phase_nnz), C.byref(st)))
+    return st
+
+
 def LocalHybridSpGEMM(A, B, clearA: bool = False, clearB: bool = False, sr: str = "plustimes", **kw) -> SpResult:
     return spgemm(A, B, sr=sr, **kw)
 

@@ -98,6 +98,8 @@ int gbc_context_set_stream(gbc_context *ctx, void *stream);
 int gbc_context_synchronize(gbc_context *ctx);
 const char *gbc_last_error(void);
 int gbc_version(void);
+/* Number of CUDA kernels this library has launched in this process. */
+int64_t gbc_launch_count(void);
 
 /* ------------------------------------------------------------------ result */
 /* A result is a device matrix owned by the library until gbc_result_free. */
@@ -136,11 +138,65 @@ int gbc_spgemm_select2ndmin_i64_i64(gbc_context *ctx, const gbc_matrix *A, const
 int gbc_spgemm_bool_i64(gbc_context *ctx, const gbc_matrix *A, const gbc_matrix *B, const gbc_spgemm_opts *opts,
                         gbc_result **C, gbc_spgemm_stats *stats);
 
+/* Column-phased product for outputs larger than device memory: B's stored
+ * columns are split into phases whose output holds at most max_phase_nnz
+ * entries, as the phases of MemEfficientSpGEMM (ParFriends.h:553-556,
+ * SpDCCols::ColSplit).  Each phase's C is produced in HBM and reduced to
+ * deterministic checksums (sum of row ids, sum of values as double); the
+ * product itself is not returned. */
+typedef struct {
+    int64_t flops;
+    int64_t nnz;
+    int64_t phases;
+    int64_t max_phase_nnz;
+    int64_t row_checksum;
+    double val_checksum;
+    double ms_total;
+    double ms_symbolic;
+    double ms_numeric; /* sum over phases of the numeric kernel */
+} gbc_phased_stats;
+
+int gbc_spgemm_phased(gbc_context *ctx, int sr, int vt, const gbc_matrix *A, const gbc_matrix *B,
+                      int64_t max_phase_nnz, gbc_phased_stats *st);
+
 /* Symbolic helpers: per stored column of B, flop = estimateFLOP
  * (mtSpGEMM.h:1057-1134) and nnz = estimateNNZ_Hash (mtSpGEMM.h:806-933).
  * Output arrays have B->nzc entries and live where `where` says. */
 int gbc_spgemm_colstats(gbc_context *ctx, const gbc_matrix *A, const gbc_matrix *B, int64_t *flop, int64_t *nnz,
                         int where);
+
+/* ------------------------------------------------------------ SpMSpV / BFS */
+/* A square pattern matrix prepared once for repeated sparse-vector
+ * multiplies and BFS (CSC, jc == NULL; values ignored). */
+typedef struct gbc_graph gbc_graph;
+
+typedef struct {
+    int64_t iterations; /* level-loop iterations, as the reference's BFS loop counts them */
+    int64_t reached;    /* vertices with a parent, plus the source */
+    int64_t edges;      /* undirected edges of the reached vertices: sum(deg)/2 */
+    double ms;          /* device time of the BFS */
+} gbc_bfs_stats;
+
+int gbc_graph_create(gbc_context *ctx, const gbc_matrix *A, gbc_graph **g);
+int gbc_graph_destroy(gbc_graph *g);
+
+/* y = A x over SelectMinSR / Select2ndMinSR (add = min, multiply returns the
+ * vector value): replaces SpMXSpV_Bucket<SR>(const Csc&, int32 mA, const
+ * int32* indx, const IVT* numx, int32 veclen, vector<int32>& indy,
+ * vector<OVT>& numy, PreAllocatedSPA&) (SpImpl.cpp:389-392, SpImpl.h:115-124).
+ * indy/numy receive nnzy entries sorted by row; they must hold up to nrow
+ * entries.  All four arrays live where `where` says. */
+int gbc_spmspv_select2ndmin_i64(gbc_context *ctx, gbc_graph *g, const int32_t *indx, const int64_t *numx,
+                                int32_t veclen, int32_t *indy, int64_t *numy, int32_t *nnzy, int where);
+
+/* BFS from `source` by repeated SpMSpV with the per-level glue fused, as the
+ * BFS_CSC loop of Applications/SpMSpV-IPDPS2017/SpMSpVBench.cpp:128-156:
+ * parents[v] = smallest frontier neighbour that first reached v (-1 if
+ * unreached; the source gets a parent only when a later level reaches it).
+ * levels[v] = loop iteration (1-based) in which v first entered the fringe,
+ * 0 for the source, -1 unreached.  Either output may be NULL. */
+int gbc_bfs(gbc_context *ctx, gbc_graph *g, int64_t source, int64_t *parents, int64_t *levels, gbc_bfs_stats *st,
+            int where);
 
 #ifdef __cplusplus
 }

@@ -9,7 +9,7 @@ from conftest import ROOT
 
 def declared_symbols():
     src = open(os.path.join(ROOT, "include", "gbcomb.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char \*)\s*(gbc_[a-z0-9_]+)\s*\(", src, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t|const char \*)\s*(gbc_[a-z0-9_]+)\s*\(", src, re.M)))
 
 
 def test_header_declares_entry_points():

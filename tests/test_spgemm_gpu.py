@@ -175,3 +175,19 @@ def test_colstats_vs_reference(gpu_ctx, golden):
         nnz = local.estimateNNZ_Hash(D, D)
         assert np.array_equal(flop, golden[f"colstats/{name}/flop"]), name
         assert np.array_equal(nnz, golden[f"colstats/{name}/nnz"]), name
+
+
+def test_phased_matches_single_pass(gpu_ctx, oracle_lib):
+    """Column phases (small budget -> many phases) give the same nnz and
+    checksums as the single-pass product and the oracle."""
+    O = oracle_lib
+    A = G.rmat(13, 8, seed=6)
+    cp, rows, vals = gpu_csc(A, A, 0)
+    pcp, prow, pval = O.port_spgemm(A, A, O.SR_PLUSTIMES_F64)
+    ref_rows = int(prow.sum())
+    for budget in (len(rows), 200_000, 50_000):
+        st = local.spgemm_phased(A, A, max_phase_nnz=budget)
+        assert st.nnz == len(prow) and st.row_checksum == ref_rows
+        assert abs(st.val_checksum - pval.sum()) <= 1e-9 * abs(pval.sum())
+        assert st.phases >= (len(prow) + budget - 1) // budget
+        assert st.flops == int(O.port_spgemm(A, A, O.SR_PLUSTIMES_F64, want_counts=True)[1][0].sum())
