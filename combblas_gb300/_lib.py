@@ -102,6 +102,9 @@ _SIGS.update({
     "gbc_graph_destroy": (C.c_int, [C.c_void_p]),
     "gbc_spmspv_select2ndmin_i64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
                                               C.c_void_p, C.POINTER(C.c_int32), C.c_int]),
+    "gbc_spmspv_select2ndmin_noalloc": (C.c_int, [C.c_int64, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
+                                                  C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
+                                                  C.POINTER(C.c_int32), C.c_void_p]),
     "gbc_bfs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.POINTER(gbc_bfs_stats),
                           C.c_int]),
 })

@@ -198,6 +198,26 @@ int gbc_spmspv_select2ndmin_i64(gbc_context *ctx, gbc_graph *g, const int32_t *i
 int gbc_bfs(gbc_context *ctx, gbc_graph *g, int64_t source, int64_t *parents, int64_t *levels, gbc_bfs_stats *st,
             int where);
 
+/* Allocation-free form of gbc_spmspv_select2ndmin_i64, for callers that
+ * cannot call cudaMalloc where they need the product: code running while
+ * another component has reserved the device's free memory, latency-critical
+ * paths that cannot take cudaMalloc's implicit device synchronisation, or
+ * environments that forbid driver allocations after start-up.  It has no
+ * counterpart in the reference.  Every array is caller-provided device
+ * memory on the current device (A as CSC: cp[ncol+1], ir[nnz]; x: indx,
+ * numx[veclen]; y: indy, numy with room for nrow entries); *nnzy (host) gets
+ * the output count after the call synchronises `stream` (a cudaStream_t,
+ * NULL for the default stream).  Working storage is one fixed __device__
+ * array of about 8.4 MB that every GPU loading the library holds until the
+ * process exits; nrow above 1048576 is rejected with GBC_EOVERFLOW.  All
+ * calls share that array: calls that overlap on the GPU race and must be
+ * serialised by the caller.  The first call on a device looks up the
+ * array's address (cudaGetSymbolAddress) -- make it before any stream
+ * capture. */
+int gbc_spmspv_select2ndmin_noalloc(int64_t nrow, int64_t ncol, int64_t nnz, const int64_t *cp, const int64_t *ir,
+                                    const int32_t *indx, const int64_t *numx, int32_t veclen, int32_t *indy,
+                                    int64_t *numy, int32_t *nnzy, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
