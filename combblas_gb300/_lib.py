@@ -98,6 +98,21 @@ for _n in ("plustimes_f64", "plustimes_f32", "plustimes_i64", "minplus_f64", "mi
                                                C.POINTER(gbc_spgemm_stats)])
 _SIGS["gbc_spgemm_bool_i64"] = _SIGS["gbc_spgemm_plustimes_f64_i64"]
 _SIGS.update({
+    "gbc_mlp_create": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "gbc_mlp_destroy": (C.c_int, [C.c_void_p]),
+    "gbc_mlp_num_params": (C.c_int, []),
+    "gbc_mlp_get": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_float)]),
+    "gbc_mlp_set": (C.c_int, [C.c_void_p, C.c_void_p, C.c_float]),
+    "gbc_mlp_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_float,
+                                C.POINTER(C.c_float), C.c_int]),
+    "gbc_mlp_gradient": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int]),
+    "gbc_mlp_predict": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int]),
+    "gbc_context_set_mlp": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gbc_spgemm_features": (C.c_int, [C.c_void_p, C.POINTER(gbc_matrix), C.POINTER(gbc_matrix), C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_int]),
+    "gbc_mcl_expand_f32": (C.c_int, [C.c_void_p, C.POINTER(gbc_matrix), C.c_float, C.c_int64, C.c_int,
+                                     C.POINTER(C.c_void_p), C.POINTER(gbc_spgemm_stats)]),
+    "gbc_mcl_prune_select_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_float, C.c_int64, C.POINTER(C.c_void_p)]),
     "gbc_graph_create": (C.c_int, [C.c_void_p, C.POINTER(gbc_matrix), C.POINTER(C.c_void_p)]),
     "gbc_graph_destroy": (C.c_int, [C.c_void_p]),
     "gbc_spmspv_select2ndmin_i64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,

@@ -43,6 +43,7 @@ struct Context {
     bool own_stream = false;
     cudaEvent_t ev[8] = {};
     int32_t *d_flag = nullptr;  // device error/overflow flags (8 ints)
+    void *mlp = nullptr;        // sizing model used by GBC_SIZING_LEARNED (gbc_mlp*)
     void *pinned = nullptr;     // small pinned staging for scalar reads
 };
 

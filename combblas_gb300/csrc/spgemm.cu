@@ -26,6 +26,8 @@
 #include "gbc_internal.cuh"
 #include "semiring.cuh"
 #include "spgemm_kernels.cuh"
+#include "spgemm_small.cuh"
+#include "mlp.cuh"
 
 namespace gbc {
 
@@ -130,47 +132,105 @@ __global__ void k_prep_b(int64_t nzc, int64_t nnz, const int64_t *cp, const int6
     }
 }
 
-// flop[i] = sum over B(:,i) entries k of nnz(A(:,k)).
-__global__ void k_flop(int64_t nb, const int64_t *bcp, const int32_t *brow, const int64_t *acp, int64_t *flop)
+// Row-tile mask of every column of A: bit t set when A(tile t, k) is nonempty.
+__global__ void k_amask(int64_t ncol, const uint32_t *tptr, int T, int mask_words, uint64_t *amask)
 {
-    int lane = threadIdx.x & 31;
-    int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
+    const int64_t c = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c >= ncol) return;
+    const uint32_t *tp = tptr + c * (int64_t)(T + 1);
+    for (int w = 0; w < mask_words; ++w) {
+        uint64_t m = 0;
+        for (int b = 0; b < 64 && w * 64 + b < T; ++b) {
+            const int t = w * 64 + b;
+            if (tp[t + 1] > tp[t]) m |= 1ull << b;
+        }
+        amask[c * mask_words + w] = m;
+    }
+}
+
+// flop[i] = sum over B(:,i) entries k of nnz(A(:,k)) (estimateFLOP), and the
+// column's tile mask = OR of the masks of those A columns (exactly the row
+// tiles the output column touches).
+__global__ void k_flop_mask(int64_t nb, const int64_t *bcp, const int32_t *brow, const int64_t *acp,
+                            const uint64_t *amask, int mask_words, int64_t *flop, uint64_t *tmask)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
     for (int64_t i = warp; i < nb; i += nwarps) {
         int64_t f = 0;
         for (int64_t p = bcp[i] + lane; p < bcp[i + 1]; p += 32) {
-            int k = brow[p];
+            const int k = brow[p];
             f += acp[k + 1] - acp[k];
         }
 #pragma unroll
         for (int o = 16; o; o >>= 1) f += __shfl_xor_sync(0xffffffffu, f, o);
         if (lane == 0) flop[i] = f;
+        for (int w = 0; w < mask_words; ++w) {
+            uint64_t m = 0;
+            for (int64_t p = bcp[i] + lane; p < bcp[i + 1]; p += 32) m |= amask[(int64_t)brow[p] * mask_words + w];
+#pragma unroll
+            for (int o = 16; o; o >>= 1) m |= __shfl_xor_sync(0xffffffffu, m, o);
+            if (lane == 0) tmask[i * mask_words + w] = m;
+        }
+    }
+}
+
+// Split stored columns j0..j1-1 of B by their flop count: empty (count 0),
+// small (<= kSmall1, <= kSmall2 multiplications, warp kernels) and big (block
+// kernels).  Lists are appended in any order; every column is written to its
+// own output range, so the order does not affect the result.
+constexpr int kSmall1 = 256;
+constexpr int kSmall2 = 4096;
+
+__global__ void k_classify(const int64_t *flop, int64_t j0, int64_t j1, int32_t *l1, int32_t *l2, int32_t *lb,
+                           unsigned long long *counts, int64_t *cnt_zero)
+{
+    const int64_t i = j0 + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    int cls = -1;
+    if (i < j1) {
+        const int64_t f = flop[i];
+        if (f == 0) {
+            if (cnt_zero) cnt_zero[i] = 0;
+        } else {
+            cls = f <= kSmall1 ? 0 : (f <= kSmall2 ? 1 : 2);
+        }
+    }
+    int32_t *lists[3] = {l1, l2, lb};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const unsigned m = __ballot_sync(0xffffffffu, cls == c);
+        if (!m) continue;
+        const int leader = __ffs(m) - 1;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(&counts[c], (unsigned long long)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (cls == c) lists[c][base + __popc(m & ((1u << lane) - 1))] = (int32_t)i;
     }
 }
 
 // ---------------------------------------------------------------- symbolic
-// One block per column (dynamic work counter).  Bitmap over a super-tile of
-// SR rows (a whole number of R-row tiles); products set bits; the column's
-// count is the popcount and each R-tile with a set bit is marked in the
-// column's tile mask (mask words of 64 tiles).
-__global__ void __launch_bounds__(kThreads) k_symbolic(SpgemmArgs a, int64_t *cnt, uint64_t *tmask,
-                                                       int sup_rows, unsigned long long *work)
+// One block per listed column (dynamic work counter).  Bitmap over a
+// super-tile of sup_rows rows (a whole number of R-row tiles); products set
+// bits; the column's count is the popcount.
+__global__ void __launch_bounds__(kThreads) k_symbolic(SpgemmArgs a, const int32_t *cols, int64_t ncols,
+                                                       int64_t *cnt, int sup_rows, unsigned long long *work)
 {
     extern __shared__ uint32_t bm[];
     __shared__ ChunkSmem ch;
     __shared__ int64_t s_col;
-    __shared__ uint32_t s_tmask[kMaxMaskWords * 2];
     __shared__ int64_t s_red[kThreads / 32];
     const int tid = threadIdx.x;
     const int tiles_per_sup = sup_rows / a.R;
     for (;;) {
         if (tid == 0) s_col = (int64_t)atomicAdd(work, 1ull);
         __syncthreads();
-        int64_t i = s_col;
+        const int64_t ci = s_col;
         __syncthreads();
-        if (i >= a.nb) break;
+        if (ci >= ncols) break;
+        const int64_t i = cols[ci];
         int64_t bs = a.bcp[i], be = a.bcp[i + 1];
-        for (int w = tid; w < a.mask_words * 2; w += kThreads) s_tmask[w] = 0;
         int64_t total = 0;
         if (a.flop[i] > 0) {
             for (int t0 = 0; t0 < a.T; t0 += tiles_per_sup) {
@@ -190,17 +250,8 @@ __global__ void __launch_bounds__(kThreads) k_symbolic(SpgemmArgs a, int64_t *cn
                     }
                     __syncthreads();
                 }
-                // count and per-tile occupancy
                 int64_t c = 0;
-                int wpt = a.R >> 5;  // words per tile
-                for (int w = tid; w < words; w += kThreads) {
-                    uint32_t x = bm[w];
-                    if (x) {
-                        c += __popc(x);
-                        int t = t0 + w / wpt;
-                        atomicOr(&s_tmask[t >> 5], 1u << (t & 31));
-                    }
-                }
+                for (int w = tid; w < words; w += kThreads) c += __popc(bm[w]);
                 total += c;
                 __syncthreads();
             }
@@ -216,8 +267,6 @@ __global__ void __launch_bounds__(kThreads) k_symbolic(SpgemmArgs a, int64_t *cn
             for (int w = 0; w < kThreads / 32; ++w) s += s_red[w];
             cnt[i] = s;
         }
-        for (int w = tid; w < a.mask_words; w += kThreads)
-            tmask[i * a.mask_words + w] = (uint64_t)s_tmask[2 * w] | ((uint64_t)s_tmask[2 * w + 1] << 32);
         __syncthreads();
     }
 }
@@ -277,7 +326,9 @@ __device__ __forceinline__ void seg_max_scan(uint8_t *seg, int seed)
 
 template <class SR>
 __global__ void __launch_bounds__(kThreads, 1) k_numeric(SpgemmArgs a, const void *aval_v, const void *bval_v,
-                                                         const uint64_t *tmask, const int64_t *ccp, int64_t *cir,
+                                                         const uint64_t *tmask, const int32_t *cols, int64_t ncols,
+                                                         const int64_t *ccp, int64_t ccp_base, const int64_t *cap,
+                                                         int64_t *out_cnt, int32_t *overflow, int64_t *cir,
                                                          void *cval_v, unsigned long long *work)
 {
     typedef typename SR::V V;
@@ -300,15 +351,18 @@ __global__ void __launch_bounds__(kThreads, 1) k_numeric(SpgemmArgs a, const voi
     constexpr int NC = kWarps * kSubPerThread * kWarps;
 
     for (;;) {
-        if (tid == 0) s_col = a.col_begin + (int64_t)atomicAdd(work, 1ull);
+        if (tid == 0) s_col = (int64_t)atomicAdd(work, 1ull);
         __syncthreads();
-        const int64_t i = s_col;
+        const int64_t ci = s_col;
         __syncthreads();
-        if (i >= a.col_end) break;
+        if (ci >= ncols) break;
+        const int64_t i = cols[ci];
         const int64_t bs = a.bcp[i], be = a.bcp[i + 1];
-        // ccp is indexed relative to the first column of this pass
-        int64_t out = ccp[i - a.col_begin];
-        const int64_t lim = ccp[i - a.col_begin + 1];
+        // ccp is indexed relative to ccp_base (the first column of a phase)
+        const int64_t out0 = ccp[i - ccp_base];
+        int64_t out = out0;
+        const int64_t lim = cap ? out0 + cap[i] : ccp[i - ccp_base + 1];
+        bool over = false;
         for (int mw = 0; mw < a.mask_words; ++mw) {
             uint64_t msk = tmask[i * a.mask_words + mw];
             while (msk) {
@@ -441,7 +495,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_numeric(SpgemmArgs a, const voi
                                 cir[pos] = (int64_t)row0 + o;
                                 cval[pos] = acc[o];
                             } else {
-                                atomicOr(a.err, 128);  // count mismatch: never write past the column
+                                over = true;  // never write past the column's range
                             }
                             ++pos;
                         }
@@ -449,6 +503,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_numeric(SpgemmArgs a, const voi
                     out += tot;
                 }
                 __syncthreads();
+            }
+        }
+        over = __syncthreads_or(over);
+        if (tid == 0) {
+            if (out_cnt) out_cnt[i] = out - out0;
+            if (over) {
+                if (overflow)
+                    overflow[i] = 1;
+                else
+                    atomicOr(a.err, 128);  // exact sizing: counts disagree
             }
         }
     }
@@ -493,7 +557,7 @@ int prepare_operands(Workspace &ws, const DevMatrix &A, const DevMatrix &B, Spge
     a.kdim = A.ncol;
     a.n = B.ncol;
     a.nb = B.nzc;
-    a.R = std::min<int64_t>(kTileRows, ((A.nrow + kThreads - 1) / kThreads) * kThreads);
+    a.R = (int)std::min<int64_t>(kTileRows, ((A.nrow + kThreads - 1) / kThreads) * kThreads);
     if (a.R < kThreads) a.R = kThreads;
     a.T = (int)((A.nrow + a.R - 1) / a.R);
     if (a.T < 1) a.T = 1;
@@ -510,24 +574,28 @@ int prepare_operands(Workspace &ws, const DevMatrix &A, const DevMatrix &B, Spge
     GBC_TRY(ws.alloc_n(&tptr, (size_t)A.ncol * (a.T + 1) + 1));
     if (A.jc) {
         GBC_TRY(ws.alloc_n(&acp, A.ncol + 1));
-        k_dense_colptr<<<(unsigned)((A.nzc + 1 + 255) / 256), 256, 0, s>>>(A.ncol, A.nzc, A.cp, A.jc, acp); ::gbc::note_launch();
+        k_dense_colptr<<<(unsigned)((A.nzc + 1 + 255) / 256), 256, 0, s>>>(A.ncol, A.nzc, A.cp, A.jc, acp);
+        note_launch();
         GBC_CUDA_TRY(cudaGetLastError());
     } else {
         acp = const_cast<int64_t *>(A.cp);
     }
     if (A.nzc > 0) {
         k_prep_a<<<grid_for(ctx, (A.nzc + 7) / 8, 8), 256, 0, s>>>(A.ncol, A.nrow, A.cp, A.jc, A.nzc, A.nnz,
-                                                                     A.ir, arow, tptr, a.T, a.R, err); ::gbc::note_launch();
+                                                                     A.ir, arow, tptr, a.T, a.R, err);
+        note_launch();
         GBC_CUDA_TRY(cudaGetLastError());
     }
     if (A.ncol > 0) {
-        k_fill_empty_tptr<<<(unsigned)((A.ncol + 255) / 256), 256, 0, s>>>(A.ncol, acp, tptr, a.T); ::gbc::note_launch();
+        k_fill_empty_tptr<<<(unsigned)((A.ncol + 255) / 256), 256, 0, s>>>(A.ncol, acp, tptr, a.T);
+        note_launch();
         GBC_CUDA_TRY(cudaGetLastError());
     }
     int32_t *brow = nullptr;
     GBC_TRY(ws.alloc_n(&brow, B.nnz + 1));
     if (B.nzc > 0) {
-        k_prep_b<<<grid_for(ctx, (B.nzc + 7) / 8, 8), 256, 0, s>>>(B.nzc, B.nnz, B.cp, B.ir, A.ncol, brow, err); ::gbc::note_launch();
+        k_prep_b<<<grid_for(ctx, (B.nzc + 7) / 8, 8), 256, 0, s>>>(B.nzc, B.nnz, B.cp, B.ir, A.ncol, brow, err);
+        note_launch();
         GBC_CUDA_TRY(cudaGetLastError());
     }
     int32_t herr[4];
@@ -536,7 +604,7 @@ int prepare_operands(Workspace &ws, const DevMatrix &A, const DevMatrix &B, Spge
     if (herr[0]) {
         char buf[160];
         snprintf(buf, sizeof buf, "malformed input matrix (code 0x%x): %s%s%s", herr[0],
-                 (herr[0] & 0x15) ? "bad column pointers or ids; " : "",
+                 (herr[0] & 0x13) ? "bad column pointers or ids; " : "",
                  (herr[0] & 0x24) ? "row id out of range; " : "",
                  (herr[0] & 0x48) ? "rows not strictly ascending within a column" : "");
         return fail(GBC_EINVAL, buf);
@@ -547,8 +615,241 @@ int prepare_operands(Workspace &ws, const DevMatrix &A, const DevMatrix &B, Spge
     a.tptr = tptr;
     a.bcp = B.cp;
     a.brow = brow;
+    a.col_begin = 0;
+    a.col_end = B.nzc;
     *acp_out = acp;
     return GBC_OK;
+}
+
+// Everything the numeric passes need, built once per product.
+struct Plan {
+    SpgemmArgs a{};
+    int64_t nb = 0;
+    int64_t *flop = nullptr;
+    uint64_t *tmask = nullptr;
+    int key_bits = 0;
+    unsigned long long *work = nullptr;  // kernel work counters
+    int32_t *lbuf = nullptr;             // column lists (3 x nb)
+    unsigned long long *lcnt = nullptr;  // list lengths
+};
+
+struct Lists {
+    const int32_t *l[3] = {nullptr, nullptr, nullptr};  // small1, small2, big
+    int64_t n[3] = {0, 0, 0};
+};
+
+static int plan_build(Workspace &ws, const DevMatrix &A, const DevMatrix &B, Plan &P)
+{
+    Context *ctx = ws.ctx;
+    cudaStream_t s = ctx->stream;
+    int64_t *acp = nullptr;
+    GBC_TRY(prepare_operands(ws, A, B, P.a, &acp));
+    SpgemmArgs &a = P.a;
+    P.nb = B.nzc;
+    int64_t m1 = A.nrow > 1 ? A.nrow - 1 : 0;
+    P.key_bits = 0;
+    while (m1 > 0) {
+        ++P.key_bits;
+        m1 >>= 1;
+    }
+    uint64_t *amask = nullptr;
+    GBC_TRY(ws.alloc_n(&amask, (size_t)A.ncol * a.mask_words + 1));
+    GBC_TRY(ws.alloc_n(&P.flop, P.nb + 1));
+    GBC_TRY(ws.alloc_n(&P.tmask, (size_t)P.nb * a.mask_words + 1));
+    GBC_TRY(ws.alloc_n(&P.work, 16));
+    GBC_TRY(ws.alloc_n(&P.lbuf, 3 * (size_t)P.nb + 3));
+    GBC_TRY(ws.alloc_n(&P.lcnt, 4));
+    if (A.ncol > 0) {
+        k_amask<<<(unsigned)((A.ncol + 255) / 256), 256, 0, s>>>(A.ncol, a.tptr, a.T, a.mask_words, amask);
+        note_launch();
+    }
+    if (P.nb > 0) {
+        k_flop_mask<<<grid_for(ctx, (P.nb + 7) / 8, 8), 256, 0, s>>>(P.nb, B.cp, a.brow, acp, amask, a.mask_words,
+                                                                       P.flop, P.tmask);
+        note_launch();
+    }
+    a.flop = P.flop;
+    GBC_CUDA_TRY(cudaGetLastError());
+    return GBC_OK;
+}
+
+// Column lists of stored columns [j0, j1); empty columns get cnt 0.
+static int plan_classify(Plan &P, cudaStream_t s, int64_t j0, int64_t j1, Lists &L, int64_t *cnt_zero)
+{
+    GBC_CUDA_TRY(cudaMemsetAsync(P.lcnt, 0, 4 * sizeof(unsigned long long), s));
+    int32_t *l0 = P.lbuf, *l1 = P.lbuf + P.nb + 1, *l2 = P.lbuf + 2 * (P.nb + 1);
+    if (j1 > j0) {
+        k_classify<<<(unsigned)((j1 - j0 + 255) / 256), 256, 0, s>>>(P.flop, j0, j1, l0, l1, l2, P.lcnt, cnt_zero);
+        note_launch();
+        GBC_CUDA_TRY(cudaGetLastError());
+    }
+    unsigned long long h[4];
+    GBC_CUDA_TRY(cudaMemcpyAsync(h, P.lcnt, sizeof(h), cudaMemcpyDeviceToHost, s));
+    GBC_CUDA_TRY(cudaStreamSynchronize(s));
+    L.l[0] = l0;
+    L.l[1] = l1;
+    L.l[2] = l2;
+    for (int c = 0; c < 3; ++c) L.n[c] = (int64_t)h[c];
+    return GBC_OK;
+}
+
+template <class K>
+static int set_smem(K kernel, size_t bytes)
+{
+    GBC_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    return GBC_OK;
+}
+
+// Exact nnz per listed column (estimateNNZ_Hash's result).
+static int run_symbolic(Context *ctx, Plan &P, const Lists &L, int64_t *cnt)
+{
+    cudaStream_t s = ctx->stream;
+    SpgemmArgs &a = P.a;
+    if (L.n[0] > 0) {
+        constexpr int WPB = 8, TS = 2 * kSmall1;
+        const size_t sm = (size_t)WPB * TS * 4;
+        GBC_TRY(set_smem(k_small_count<TS, WPB>, sm));
+        k_small_count<TS, WPB><<<grid_for(ctx, (L.n[0] + WPB - 1) / WPB, 8), WPB * 32, sm, s>>>(a, L.l[0], L.n[0],
+                                                                                                 cnt);
+        note_launch();
+    }
+    if (L.n[1] > 0) {
+        constexpr int WPB = 4, TS = 2 * kSmall2;
+        const size_t sm = (size_t)WPB * TS * 4;
+        GBC_TRY(set_smem(k_small_count<TS, WPB>, sm));
+        int per_sm = std::max(1, (int)(ctx->smem_optin / (sm + 1024)));
+        k_small_count<TS, WPB><<<grid_for(ctx, (L.n[1] + WPB - 1) / WPB, per_sm), WPB * 32, sm, s>>>(
+            a, L.l[1], L.n[1], cnt);
+        note_launch();
+    }
+    if (L.n[2] > 0) {
+        int sup_rows = (int)std::min<int64_t>((int64_t)kSymRows, (int64_t)a.T * a.R);
+        sup_rows = (sup_rows / a.R) * a.R;
+        size_t sym_smem = (size_t)sup_rows / 8;
+        GBC_TRY(set_smem(k_symbolic, sym_smem));
+        int per_sm = std::max(1, (int)(ctx->smem_optin / (sym_smem + 8192)));
+        GBC_CUDA_TRY(cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), s));
+        k_symbolic<<<grid_for(ctx, L.n[2], std::min(per_sm, 8)), kThreads, sym_smem, s>>>(a, L.l[2], L.n[2], cnt,
+                                                                                             sup_rows, P.work);
+        note_launch();
+    }
+    GBC_CUDA_TRY(cudaGetLastError());
+    return GBC_OK;
+}
+
+template <class SR, int FS, int WPB, bool PACK>
+static int launch_small(Context *ctx, Plan &P, const int32_t *cols, int64_t n, const void *aval, const void *bval,
+                        const int64_t *ccp, int64_t ccp_base, const int64_t *cap, int64_t *out_cnt, int32_t *overflow,
+                        int64_t *cir, void *cval)
+{
+    typedef typename SR::V V;
+    const size_t sm = WPB * small_warp_smem<FS, V, PACK>();
+    GBC_TRY(set_smem(k_small_numeric<SR, FS, WPB, PACK>, sm));
+    int per_sm = std::max(1, (int)(ctx->smem_optin / (sm + 1024)));
+    k_small_numeric<SR, FS, WPB, PACK><<<grid_for(ctx, (n + WPB - 1) / WPB, std::min(per_sm, 8)), WPB * 32, sm,
+                                         ctx->stream>>>(P.a, aval, bval, cols, n, ccp, ccp_base, cap, out_cnt,
+                                                        overflow, cir, cval, P.key_bits);
+    note_launch();
+    return GBC_OK;
+}
+
+// Numeric pass over the listed columns.  Exact sizing: cap == nullptr and
+// ccp holds the exact offsets.  Learned sizing: cap gives each column's room
+// at ccp[i - ccp_base]; out_cnt/overflow receive actual counts and flags.
+template <class SR>
+static int run_numeric(Context *ctx, Plan &P, const Lists &L, const void *aval, const void *bval, const int64_t *ccp,
+                       int64_t ccp_base, const int64_t *cap, int64_t *out_cnt, int32_t *overflow, int64_t *cir,
+                       void *cval)
+{
+    typedef typename SR::V V;
+    cudaStream_t s = ctx->stream;
+    SpgemmArgs &a = P.a;
+    const bool pack = P.key_bits <= 20;
+    if (L.n[0] > 0) {
+        if (pack)
+            GBC_TRY((launch_small<SR, kSmall1, 8, true>(ctx, P, L.l[0], L.n[0], aval, bval, ccp, ccp_base, cap,
+                                                         out_cnt, overflow, cir, cval)));
+        else
+            GBC_TRY((launch_small<SR, kSmall1, 8, false>(ctx, P, L.l[0], L.n[0], aval, bval, ccp, ccp_base, cap,
+                                                          out_cnt, overflow, cir, cval)));
+    }
+    if (L.n[1] > 0) {
+        if (pack)
+            GBC_TRY((launch_small<SR, kSmall2, 2, true>(ctx, P, L.l[1], L.n[1], aval, bval, ccp, ccp_base, cap,
+                                                         out_cnt, overflow, cir, cval)));
+        else
+            GBC_TRY((launch_small<SR, kSmall2, 2, false>(ctx, P, L.l[1], L.n[1], aval, bval, ccp, ccp_base, cap,
+                                                          out_cnt, overflow, cir, cval)));
+    }
+    if (L.n[2] > 0) {
+        const size_t num_smem = numeric_smem_bytes(a.R, sizeof(V));
+        GBC_TRY(set_smem(k_numeric<SR>, num_smem));
+        int per_sm = std::max(1, (int)(ctx->smem_optin / (num_smem + 12288)));
+        GBC_CUDA_TRY(cudaMemsetAsync(P.work + 1, 0, sizeof(unsigned long long), s));
+        k_numeric<SR><<<grid_for(ctx, L.n[2], std::min(per_sm, 8)), kThreads, num_smem, s>>>(
+            a, aval, bval, P.tmask, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir, cval, P.work + 1);
+        note_launch();
+    }
+    GBC_CUDA_TRY(cudaGetLastError());
+    return GBC_OK;
+}
+
+static int check_err(Context *ctx, const SpgemmArgs &a)
+{
+    int32_t herr = 0;
+    GBC_CUDA_TRY(cudaMemcpyAsync(&herr, a.err, sizeof(herr), cudaMemcpyDeviceToHost, ctx->stream));
+    GBC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    if (herr) return fail(GBC_ECUDA, "internal error: numeric and symbolic counts disagree");
+    return GBC_OK;
+}
+
+// Turn per-column exact counts into the result's column structure (keeping
+// or dropping empty output columns) -- shared by every sizing mode.
+static int finish_columns(Context *ctx, Workspace &ws, const DevMatrix &B, const gbc_spgemm_opts &opt, int64_t nb,
+                          const int64_t *cnt, gbc_result *C)
+{
+    cudaStream_t s = ctx->stream;
+    if (opt.keep_empty || nb == 0) {
+        C->nzc = nb;
+        GBC_TRY(device_alloc(ctx, (void **)&C->jc, (nb + 1) * sizeof(int64_t)));
+        if (nb > 0) {
+            k_iota_jc<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(nb, B.jc, C->jc);
+            note_launch();
+        }
+        return GBC_OK;
+    }
+    int64_t *flags = nullptr;
+    GBC_TRY(ws.alloc_n(&flags, nb + 1));
+    k_nonempty_flags<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(nb, cnt, flags);
+    note_launch();
+    GBC_TRY(exclusive_scan_i64(ws, flags, flags, nb, s));
+    int64_t nzc = 0;
+    GBC_TRY(read_i64(ctx, flags + nb, &nzc));
+    int64_t *cp2 = nullptr, *jc2 = nullptr;
+    GBC_TRY(device_alloc(ctx, (void **)&cp2, (nzc + 1) * sizeof(int64_t)));
+    int rc = device_alloc(ctx, (void **)&jc2, (nzc + 1) * sizeof(int64_t));
+    if (rc != GBC_OK) {
+        device_free(ctx, cp2);
+        return rc;
+    }
+    GBC_CUDA_TRY(cudaMemsetAsync(cp2, 0, sizeof(int64_t), s));
+    k_compact_cols<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(nb, cnt, flags, C->cp, B.jc, cp2, jc2);
+    note_launch();
+    device_free(ctx, C->cp);
+    C->cp = cp2;
+    C->jc = jc2;
+    C->nzc = nzc;
+    return GBC_OK;
+}
+
+static int64_t sum_i64(Workspace &ws, Context *ctx, const int64_t *v, int64_t n)
+{
+    int64_t *tmp = nullptr;
+    if (ws.alloc_n(&tmp, n + 1) != GBC_OK) return -1;
+    if (exclusive_scan_i64(ws, v, tmp, n, ctx->stream) != GBC_OK) return -1;
+    int64_t t = 0;
+    if (read_i64(ctx, tmp + n, &t) != GBC_OK) return -1;
+    return t;
 }
 
 template <class SR>
@@ -559,145 +860,55 @@ static int spgemm_exact(Context *ctx, const DevMatrix &A, const DevMatrix &B, co
     cudaStream_t s = ctx->stream;
     Workspace ws(ctx);
     cudaEventRecord(ctx->ev[0], s);
-    SpgemmArgs a{};
-    int64_t *acp = nullptr;
-    GBC_TRY(prepare_operands(ws, A, B, a, &acp));
-    const int64_t nb = B.nzc;
-    int64_t *flop = nullptr, *cnt = nullptr, *ccp = nullptr;
-    uint64_t *tmask = nullptr;
-    unsigned long long *work = nullptr;
-    GBC_TRY(ws.alloc_n(&flop, nb + 1));
+    Plan P;
+    GBC_TRY(plan_build(ws, A, B, P));
+    const int64_t nb = P.nb;
+    int64_t *cnt = nullptr, *ccp = nullptr;
     GBC_TRY(ws.alloc_n(&cnt, nb + 1));
-    GBC_TRY(ws.alloc_n(&tmask, (size_t)nb * a.mask_words + 1));
-    GBC_TRY(ws.alloc_n(&work, 8));
-    GBC_CUDA_TRY(cudaMemsetAsync(work, 0, 8 * sizeof(unsigned long long), s));
-    a.flop = flop;
-    a.col_begin = 0;
-    a.col_end = nb;
-    if (nb > 0) {
-        k_flop<<<grid_for(ctx, (nb + 7) / 8, 8), 256, 0, s>>>(nb, B.cp, a.brow, acp, flop); ::gbc::note_launch();
-        GBC_CUDA_TRY(cudaGetLastError());
-    }
-    // symbolic
-    int sup_rows = (int)std::min<int64_t>((int64_t)kSymRows, (int64_t)a.T * a.R);
-    sup_rows = (sup_rows / a.R) * a.R;
-    size_t sym_smem = (size_t)sup_rows / 8;
+    Lists L;
+    GBC_TRY(plan_classify(P, s, 0, nb, L, cnt));
     cudaEventRecord(ctx->ev[1], s);
-    if (nb > 0) {
-        GBC_CUDA_TRY(cudaFuncSetAttribute(k_symbolic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sym_smem));
-        int per_sm = std::max(1, (int)(ctx->smem_optin / (sym_smem + 8192)));
-        k_symbolic<<<grid_for(ctx, nb, std::min(per_sm, 8)), kThreads, sym_smem, s>>>(a, cnt, tmask, sup_rows,
-                                                                                          work); ::gbc::note_launch();
-        GBC_CUDA_TRY(cudaGetLastError());
-    }
+    GBC_TRY(run_symbolic(ctx, P, L, cnt));
     GBC_TRY(device_alloc(ctx, (void **)&ccp, (nb + 1) * sizeof(int64_t)));
-    int rc = exclusive_scan_i64(ws, cnt, ccp, nb, s);
-    if (rc != GBC_OK) {
-        device_free(ctx, ccp);
-        return rc;
-    }
-    int64_t nnzc = 0;
-    rc = read_i64(ctx, ccp + nb, &nnzc);
-    if (rc != GBC_OK) {
-        device_free(ctx, ccp);
-        return rc;
-    }
-    cudaEventRecord(ctx->ev[2], s);
-    // numeric
     gbc_result *C = new gbc_result();
     C->ctx = ctx;
     C->nrow = A.nrow;
     C->ncol = B.ncol;
     C->valtype = vt;
-    C->nnz = nnzc;
     C->cp = ccp;
-    rc = device_alloc(ctx, (void **)&C->ir, (nnzc + 1) * sizeof(int64_t));
+    int rc = exclusive_scan_i64(ws, cnt, ccp, nb, s);
+    int64_t nnzc = 0;
+    if (rc == GBC_OK) rc = read_i64(ctx, ccp + nb, &nnzc);
+    cudaEventRecord(ctx->ev[2], s);
+    C->nnz = nnzc;
+    if (rc == GBC_OK) rc = device_alloc(ctx, (void **)&C->ir, (nnzc + 1) * sizeof(int64_t));
     if (rc == GBC_OK) rc = device_alloc(ctx, &C->num, (nnzc + 1) * sizeof(V));
+    if (rc == GBC_OK && nnzc > 0)
+        rc = run_numeric<SR>(ctx, P, L, A.num, B.num, ccp, 0, nullptr, nullptr, nullptr, C->ir, C->num);
+    cudaEventRecord(ctx->ev[3], s);
+    if (rc == GBC_OK) rc = finish_columns(ctx, ws, B, opt, nb, cnt, C);
+    cudaEventRecord(ctx->ev[4], s);
+    if (rc == GBC_OK) rc = check_err(ctx, P.a);
     if (rc != GBC_OK) {
         gbc_result_free(C);
         return rc;
     }
-    if (nb > 0 && nnzc > 0) {
-        size_t num_smem = numeric_smem_bytes(a.R, sizeof(V));
-        GBC_CUDA_TRY(cudaFuncSetAttribute(k_numeric<SR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)num_smem));
-        int per_sm = std::max(1, (int)(ctx->smem_optin / (num_smem + 12288)));
-        k_numeric<SR><<<grid_for(ctx, nb, std::min(per_sm, 8)), kThreads, num_smem, s>>>(
-            a, A.num, B.num, tmask, ccp, C->ir, C->num, work + 2); ::gbc::note_launch();
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) {
-            gbc_result_free(C);
-            return fail(GBC_ECUDA, std::string("k_numeric launch: ") + cudaGetErrorString(e));
-        }
-    }
-    cudaEventRecord(ctx->ev[3], s);
-    // column ids / empty-column compaction
-    if (opt.keep_empty || nb == 0) {
-        C->nzc = nb;
-        rc = device_alloc(ctx, (void **)&C->jc, (nb + 1) * sizeof(int64_t));
-        if (rc != GBC_OK) {
-            gbc_result_free(C);
-            return rc;
-        }
-        if (nb > 0) k_iota_jc<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(nb, B.jc, C->jc); ::gbc::note_launch();
-    } else {
-        int64_t *flags = nullptr;
-        GBC_TRY(ws.alloc_n(&flags, nb + 1));
-        k_nonempty_flags<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(nb, cnt, flags); ::gbc::note_launch();
-        GBC_TRY(exclusive_scan_i64(ws, flags, flags, nb, s));
-        int64_t nzc = 0;
-        GBC_TRY(read_i64(ctx, flags + nb, &nzc));
-        int64_t *cp2 = nullptr, *jc2 = nullptr;
-        rc = device_alloc(ctx, (void **)&cp2, (nzc + 1) * sizeof(int64_t));
-        if (rc == GBC_OK) rc = device_alloc(ctx, (void **)&jc2, (nzc + 1) * sizeof(int64_t));
-        if (rc != GBC_OK) {
-            device_free(ctx, cp2);
-            gbc_result_free(C);
-            return rc;
-        }
-        GBC_CUDA_TRY(cudaMemsetAsync(cp2, 0, sizeof(int64_t), s));
-        k_compact_cols<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(nb, cnt, flags, ccp, B.jc, cp2, jc2); ::gbc::note_launch();
-        device_free(ctx, C->cp);
-        C->cp = cp2;
-        C->jc = jc2;
-        C->nzc = nzc;
-    }
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) {
-        gbc_result_free(C);
-        return fail(GBC_ECUDA, std::string("spgemm: ") + cudaGetErrorString(e));
-    }
-    cudaEventRecord(ctx->ev[4], s);
-    {
-        int32_t herr = 0;
-        GBC_CUDA_TRY(cudaMemcpyAsync(&herr, a.err, sizeof(herr), cudaMemcpyDeviceToHost, s));
-        GBC_CUDA_TRY(cudaStreamSynchronize(s));
-        if (herr) {
-            gbc_result_free(C);
-            return fail(GBC_ECUDA, "internal error: numeric and symbolic counts disagree");
-        }
-    }
     if (st) {
-        // flop total
-        int64_t *fsum = nullptr;
-        GBC_TRY(ws.alloc_n(&fsum, nb + 1));
-        GBC_TRY(exclusive_scan_i64(ws, flop, fsum, nb, s));
-        GBC_TRY(read_i64(ctx, fsum + nb, &st->flops));
+        st->flops = sum_i64(ws, ctx, P.flop, nb);
         st->nnz = nnzc;
         st->overflow_cols = 0;
         st->alloc_entries = nnzc;
-        float t01 = 0, t13 = 0, t04 = 0, t23 = 0;
+        float t04 = 0, t12 = 0, t23 = 0;
         cudaEventElapsedTime(&t04, ctx->ev[0], ctx->ev[4]);
-        cudaEventElapsedTime(&t01, ctx->ev[1], ctx->ev[2]);
+        cudaEventElapsedTime(&t12, ctx->ev[1], ctx->ev[2]);
         cudaEventElapsedTime(&t23, ctx->ev[2], ctx->ev[3]);
-        (void)t13;
         st->ms_total = t04;
-        st->ms_symbolic = t01;
+        st->ms_symbolic = t12;
         st->ms_numeric = t23;
     }
     *Cout = C;
     return GBC_OK;
 }
-
 
 // ------------------------------------------------------- column phases
 // Deterministic checksums of one phase's output: block partial sums over
@@ -749,42 +960,20 @@ static int spgemm_phased(Context *ctx, const DevMatrix &A, const DevMatrix &B, i
     cudaStream_t s = ctx->stream;
     Workspace ws(ctx);
     cudaEventRecord(ctx->ev[0], s);
-    SpgemmArgs a{};
-    int64_t *acp = nullptr;
-    GBC_TRY(prepare_operands(ws, A, B, a, &acp));
-    const int64_t nb = B.nzc;
-    int64_t *flop = nullptr, *cnt = nullptr, *fsum = nullptr;
-    uint64_t *tmask = nullptr;
-    unsigned long long *work = nullptr;
-    GBC_TRY(ws.alloc_n(&flop, nb + 1));
-    GBC_TRY(ws.alloc_n(&fsum, nb + 1));
+    Plan P;
+    GBC_TRY(plan_build(ws, A, B, P));
+    const int64_t nb = P.nb;
+    int64_t *cnt = nullptr;
     GBC_TRY(ws.alloc_n(&cnt, nb + 1));
-    GBC_TRY(ws.alloc_n(&tmask, (size_t)nb * a.mask_words + 1));
-    GBC_TRY(ws.alloc_n(&work, 8));
-    GBC_CUDA_TRY(cudaMemsetAsync(work, 0, 8 * sizeof(unsigned long long), s));
-    a.flop = flop;
-    if (nb > 0) {
-        k_flop<<<grid_for(ctx, (nb + 7) / 8, 8), 256, 0, s>>>(nb, B.cp, a.brow, acp, flop); ::gbc::note_launch();
-        GBC_CUDA_TRY(cudaGetLastError());
-    }
-    int sup_rows = (int)std::min<int64_t>((int64_t)kSymRows, (int64_t)a.T * a.R);
-    sup_rows = (sup_rows / a.R) * a.R;
-    size_t sym_smem = (size_t)sup_rows / 8;
+    Lists L;
+    GBC_TRY(plan_classify(P, s, 0, nb, L, cnt));
     cudaEventRecord(ctx->ev[1], s);
-    if (nb > 0) {
-        GBC_CUDA_TRY(cudaFuncSetAttribute(k_symbolic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sym_smem));
-        int per_sm = std::max(1, (int)(ctx->smem_optin / (sym_smem + 8192)));
-        k_symbolic<<<grid_for(ctx, nb, std::min(per_sm, 8)), kThreads, sym_smem, s>>>(a, cnt, tmask, sup_rows,
-                                                                                          work); ::gbc::note_launch();
-        GBC_CUDA_TRY(cudaGetLastError());
-    }
+    GBC_TRY(run_symbolic(ctx, P, L, cnt));
     cudaEventRecord(ctx->ev[2], s);
     std::vector<int64_t> hcnt(nb > 0 ? nb : 1);
     if (nb > 0) GBC_CUDA_TRY(cudaMemcpyAsync(hcnt.data(), cnt, nb * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    GBC_TRY(exclusive_scan_i64(ws, flop, fsum, nb, s));
-    int64_t flops = 0;
-    GBC_TRY(read_i64(ctx, fsum + nb, &flops));
-    // phase boundaries (greedy, a column bigger than the budget is alone)
+    const int64_t flops = sum_i64(ws, ctx, P.flop, nb);
+    // phase boundaries (greedy; a column bigger than the budget is alone)
     std::vector<int64_t> bounds{0};
     int64_t acc = 0, maxp = 0, total = 0;
     for (int64_t j = 0; j < nb; ++j) {
@@ -804,30 +993,25 @@ static int spgemm_phased(Context *ctx, const DevMatrix &A, const DevMatrix &B, i
     V *num = nullptr;
     double *vsum = nullptr;
     const int csb = ctx->num_sms * 2;
+    const int np = (int)bounds.size() - 1;
     GBC_TRY(ws.alloc_n(&ir, maxp + 1));
     GBC_TRY(ws.alloc_n(&num, maxp + 1));
     GBC_TRY(ws.alloc_n(&ccp, maxcols + 1));
-    GBC_TRY(ws.alloc_n(&rsum, (size_t)csb * (bounds.size() + 1)));
-    GBC_TRY(ws.alloc_n(&vsum, (size_t)csb * (bounds.size() + 1)));
-    size_t num_smem = numeric_smem_bytes(a.R, sizeof(V));
-    GBC_CUDA_TRY(cudaFuncSetAttribute(k_numeric<SR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)num_smem));
-    int per_sm = std::max(1, (int)(ctx->smem_optin / (num_smem + 12288)));
+    GBC_TRY(ws.alloc_n(&rsum, (size_t)csb * (np + 1)));
+    GBC_TRY(ws.alloc_n(&vsum, (size_t)csb * (np + 1)));
     double ms_num = 0;
-    const int np = (int)bounds.size() - 1;
     for (int p = 0; p < np; ++p) {
         const int64_t j0 = bounds[p], j1 = bounds[p + 1];
+        Lists Lp;
+        GBC_TRY(plan_classify(P, s, j0, j1, Lp, nullptr));
         GBC_TRY(exclusive_scan_i64(ws, cnt + j0, ccp, j1 - j0, s));
-        GBC_CUDA_TRY(cudaMemsetAsync(work + 2, 0, sizeof(unsigned long long), s));
-        a.col_begin = j0;
-        a.col_end = j1;
         cudaEventRecord(ctx->ev[5], s);
-        k_numeric<SR><<<grid_for(ctx, j1 - j0, std::min(per_sm, 8)), kThreads, num_smem, s>>>(
-            a, A.num, B.num, tmask, ccp, ir, num, work + 2); ::gbc::note_launch();
-        GBC_CUDA_TRY(cudaGetLastError());
+        GBC_TRY(run_numeric<SR>(ctx, P, Lp, A.num, B.num, ccp, j0, nullptr, nullptr, nullptr, ir, num));
         cudaEventRecord(ctx->ev[6], s);
         int64_t pn = 0;
         for (int64_t j = j0; j < j1; ++j) pn += hcnt[j];
-        k_phase_checksum<V><<<csb, kThreads, 0, s>>>(ir, num, pn, rsum + (size_t)p * csb, vsum + (size_t)p * csb); ::gbc::note_launch();
+        k_phase_checksum<V><<<csb, kThreads, 0, s>>>(ir, num, pn, rsum + (size_t)p * csb, vsum + (size_t)p * csb);
+        note_launch();
         GBC_CUDA_TRY(cudaGetLastError());
         GBC_CUDA_TRY(cudaEventSynchronize(ctx->ev[6]));
         float ms = 0;
@@ -841,10 +1025,7 @@ static int spgemm_phased(Context *ctx, const DevMatrix &A, const DevMatrix &B, i
         GBC_CUDA_TRY(cudaMemcpyAsync(hr.data(), rsum, (size_t)csb * np * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
         GBC_CUDA_TRY(cudaMemcpyAsync(hv.data(), vsum, (size_t)csb * np * sizeof(double), cudaMemcpyDeviceToHost, s));
     }
-    int32_t herr = 0;
-    GBC_CUDA_TRY(cudaMemcpyAsync(&herr, a.err, sizeof(herr), cudaMemcpyDeviceToHost, s));
-    GBC_CUDA_TRY(cudaStreamSynchronize(s));
-    if (herr) return fail(GBC_ECUDA, "internal error: numeric and symbolic counts disagree");
+    GBC_TRY(check_err(ctx, P.a));
     if (st) {
         float t04 = 0, t12 = 0;
         cudaEventElapsedTime(&t04, ctx->ev[0], ctx->ev[4]);
@@ -868,11 +1049,384 @@ static int spgemm_phased(Context *ctx, const DevMatrix &A, const DevMatrix &B, i
     return GBC_OK;
 }
 
-template <class SR>
-int spgemm_learned(Context *, const DevMatrix &, const DevMatrix &, const gbc_spgemm_opts &, int, gbc_result **,
-                   gbc_spgemm_stats *)
+// ------------------------------------------------------- learned sizing
+// Per-column features of the sizing MLP: log2(1+x) of nnz(B(:,j)), flop,
+// the largest and the spread (standard deviation) of the referenced A
+// column lengths, the number of row tiles touched, and the row count.
+__global__ void k_features(SpgemmArgs a, int64_t nb, const uint64_t *tmask, float *feat)
 {
-    return fail(GBC_EUNSUPPORTED, "learned sizing is not built yet");
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t i = warp; i < nb; i += nwarps) {
+        const int64_t bs = a.bcp[i], be = a.bcp[i + 1];
+        double sum = 0, sq = 0, mx = 0;
+        for (int64_t p = bs + lane; p < be; p += 32) {
+            const int k = a.brow[p];
+            const double len = (double)(a.acp[k + 1] - a.acp[k]);
+            sum += len;
+            sq += len * len;
+            mx = fmax(mx, len);
+        }
+        int tiles = 0;
+        for (int w = lane; w < a.mask_words; w += 32) tiles += __popcll(tmask[i * a.mask_words + w]);
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            sum += __shfl_xor_sync(0xffffffffu, sum, o);
+            sq += __shfl_xor_sync(0xffffffffu, sq, o);
+            mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            tiles += __shfl_xor_sync(0xffffffffu, tiles, o);
+        }
+        if (lane == 0) {
+            const double nbj = (double)(be - bs);
+            const double mean = nbj > 0 ? sum / nbj : 0.0;
+            const double var = nbj > 0 ? fmax(sq / nbj - mean * mean, 0.0) : 0.0;
+            float *f = feat + i * kNF;
+            f[0] = log2f(1.f + (float)nbj);
+            f[1] = log2f(1.f + (float)sum);
+            f[2] = log2f(1.f + (float)mx);
+            f[3] = log2f(1.f + sqrtf((float)var));
+            f[4] = log2f(1.f + (float)tiles);
+            f[5] = log2f(1.f + (float)a.m);
+        }
+    }
+}
+
+// capacity = 2^(prediction + margin) - 1, at least 1 and at most min(flop, m)
+__global__ void k_capacity(int64_t nb, const int64_t *flop, const float *pred, float margin, int64_t m, int64_t *cap)
+{
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= nb) return;
+    const int64_t f = flop[i];
+    if (f == 0) {
+        cap[i] = 0;
+        return;
+    }
+    const float e = fminf(pred[i] + margin, 62.f);
+    int64_t c = (int64_t)ceilf(exp2f(e)) - 1;
+    if (c < 1) c = 1;
+    const int64_t hi = f < m ? f : m;
+    cap[i] = c > hi ? hi : c;
+}
+
+// Stored columns flagged in `flag`, split by flop class like k_classify.
+__global__ void k_classify_flagged(const int64_t *flop, int64_t nb, const int32_t *flag, int32_t *l1, int32_t *l2,
+                                   int32_t *lb, unsigned long long *counts)
+{
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    int cls = -1;
+    if (i < nb && flag[i]) {
+        const int64_t f = flop[i];
+        cls = f <= kSmall1 ? 0 : (f <= kSmall2 ? 1 : 2);
+    }
+    int32_t *lists[3] = {l1, l2, lb};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const unsigned m = __ballot_sync(0xffffffffu, cls == c);
+        if (!m) continue;
+        const int leader = __ffs(m) - 1;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(&counts[c], (unsigned long long)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (cls == c) lists[c][base + __popc(m & ((1u << lane) - 1))] = (int32_t)i;
+    }
+}
+
+__global__ void k_masked_counts(int64_t nb, const int32_t *flag, const int64_t *cnt, int64_t *out)
+{
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < nb) out[i] = flag[i] ? cnt[i] : 0;
+}
+
+__global__ void k_final_counts(int64_t nb, const int32_t *flag, const int64_t *exact, int64_t *cnt)
+{
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < nb && flag[i]) cnt[i] = exact[i];
+}
+
+// Gather every column from its region (slots, or the overflow region for
+// flagged columns) into the contiguous result.
+template <typename V>
+__global__ void k_compact(int64_t nb, const int64_t *cnt, const int64_t *dst, const int32_t *flag,
+                          const int64_t *beg0, const int64_t *ir0, const V *v0, const int64_t *beg1,
+                          const int64_t *ir1, const V *v1, int64_t *oir, V *ov)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t i = warp; i < nb; i += nwarps) {
+        const bool o = flag[i] != 0;
+        const int64_t b = o ? beg1[i] : beg0[i];
+        const int64_t *sir = o ? ir1 : ir0;
+        const V *sv = o ? v1 : v0;
+        const int64_t d = dst[i];
+        for (int64_t p = lane; p < cnt[i]; p += 32) {
+            oir[d + p] = sir[b + p];
+            ov[d + p] = sv[b + p];
+        }
+    }
+}
+
+// The learned product before compaction: column i holds cnt[i] entries at
+// beg0[i] of (ir0, v0), or -- when flag[i] (capacity overflow, recomputed
+// exactly) -- at beg1[i] of (ir1, v1).  Allocations live in `ws`.
+struct LearnedOut {
+    int64_t *beg0 = nullptr, *ir0 = nullptr, *beg1 = nullptr, *ir1 = nullptr, *cnt = nullptr;
+    void *v0 = nullptr, *v1 = nullptr;
+    int32_t *flag = nullptr;
+    int64_t nb = 0, alloc = 0, overflow_cols = 0, flops = 0;
+    double ms_predict = 0, ms_numeric = 0, ms_rerun = 0;
+};
+
+template <class SR>
+static int learned_into_slots(Context *ctx, Workspace &ws, const DevMatrix &A, const DevMatrix &B, Plan &P,
+                              LearnedOut &O)
+{
+    typedef typename SR::V V;
+    cudaStream_t s = ctx->stream;
+    Mlp *mlp = static_cast<Mlp *>(ctx->mlp);
+    if (!mlp || !mlp->trained)
+        return fail(GBC_EINVAL, "learned sizing needs a trained model (gbc_context_set_mlp)");
+    GBC_TRY(plan_build(ws, A, B, P));
+    const int64_t nb = P.nb;
+    O.nb = nb;
+    Lists L;
+    GBC_TRY(plan_classify(P, s, 0, nb, L, nullptr));
+    float *feat = nullptr, *pred = nullptr;
+    GBC_TRY(ws.alloc_n(&feat, (size_t)nb * kNF + 1));
+    GBC_TRY(ws.alloc_n(&pred, nb + 1));
+    GBC_TRY(ws.alloc_n(&O.cnt, nb + 1));
+    GBC_TRY(ws.alloc_n(&O.flag, nb + 1));
+    GBC_TRY(ws.alloc_n(&O.beg0, nb + 1));
+    int64_t *cap = nullptr;
+    GBC_TRY(ws.alloc_n(&cap, nb + 1));
+    GBC_CUDA_TRY(cudaMemsetAsync(O.flag, 0, (nb + 1) * sizeof(int32_t), s));
+    GBC_CUDA_TRY(cudaMemsetAsync(O.cnt, 0, (nb + 1) * sizeof(int64_t), s));
+    cudaEventRecord(ctx->ev[5], s);
+    if (nb > 0) {
+        k_features<<<grid_for(ctx, (nb + 7) / 8, 8), 256, 0, s>>>(P.a, nb, P.tmask, feat);
+        note_launch();
+        GBC_TRY(mlp_predict_device(mlp, feat, nb, pred, s));
+        k_capacity<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(nb, P.flop, pred, mlp->margin, A.nrow, cap);
+        note_launch();
+    }
+    GBC_TRY(exclusive_scan_i64(ws, cap, O.beg0, nb, s));
+    GBC_TRY(read_i64(ctx, O.beg0 + nb, &O.alloc));
+    cudaEventRecord(ctx->ev[6], s);
+    GBC_TRY(ws.alloc_n(&O.ir0, O.alloc + 1));
+    GBC_TRY(ws.alloc(&O.v0, (O.alloc + 1) * sizeof(V)));
+    GBC_TRY(run_numeric<SR>(ctx, P, L, A.num, B.num, O.beg0, 0, cap, O.cnt, O.flag, O.ir0, O.v0));
+    cudaEventRecord(ctx->ev[7], s);
+    // columns that overflowed their capacity: exact symbolic + numeric
+    Lists Lo;
+    GBC_CUDA_TRY(cudaMemsetAsync(P.lcnt, 0, 4 * sizeof(unsigned long long), s));
+    int32_t *l0 = P.lbuf, *l1 = P.lbuf + nb + 1, *l2 = P.lbuf + 2 * (nb + 1);
+    if (nb > 0) {
+        k_classify_flagged<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(P.flop, nb, O.flag, l0, l1, l2, P.lcnt);
+        note_launch();
+    }
+    unsigned long long h[4];
+    GBC_CUDA_TRY(cudaMemcpyAsync(h, P.lcnt, sizeof(h), cudaMemcpyDeviceToHost, s));
+    GBC_CUDA_TRY(cudaStreamSynchronize(s));
+    {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev[5], ctx->ev[6]);
+        O.ms_predict = ms;
+        cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]);
+        O.ms_numeric = ms;
+    }
+    Lo.l[0] = l0;
+    Lo.l[1] = l1;
+    Lo.l[2] = l2;
+    for (int c = 0; c < 3; ++c) Lo.n[c] = (int64_t)h[c];
+    O.overflow_cols = Lo.n[0] + Lo.n[1] + Lo.n[2];
+    GBC_TRY(ws.alloc_n(&O.beg1, nb + 1));
+    if (O.overflow_cols > 0) {
+        cudaEventRecord(ctx->ev[5], s);
+        int64_t *exact = nullptr, *masked = nullptr;
+        GBC_TRY(ws.alloc_n(&exact, nb + 1));
+        GBC_TRY(ws.alloc_n(&masked, nb + 1));
+        GBC_TRY(run_symbolic(ctx, P, Lo, exact));
+        k_masked_counts<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(nb, O.flag, exact, masked);
+        note_launch();
+        GBC_TRY(exclusive_scan_i64(ws, masked, O.beg1, nb, s));
+        int64_t tot = 0;
+        GBC_TRY(read_i64(ctx, O.beg1 + nb, &tot));
+        GBC_TRY(ws.alloc_n(&O.ir1, tot + 1));
+        GBC_TRY(ws.alloc(&O.v1, (tot + 1) * sizeof(V)));
+        GBC_TRY(run_numeric<SR>(ctx, P, Lo, A.num, B.num, O.beg1, 0, nullptr, nullptr, nullptr, O.ir1, O.v1));
+        k_final_counts<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(nb, O.flag, exact, O.cnt);
+        note_launch();
+        cudaEventRecord(ctx->ev[6], s);
+        GBC_CUDA_TRY(cudaEventSynchronize(ctx->ev[6]));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev[5], ctx->ev[6]);
+        O.ms_rerun = ms;
+    } else {
+        O.ir1 = O.ir0;
+        O.v1 = O.v0;
+        GBC_CUDA_TRY(cudaMemsetAsync(O.beg1, 0, (nb + 1) * sizeof(int64_t), s));
+    }
+    O.flops = sum_i64(ws, ctx, P.flop, nb);
+    return check_err(ctx, P.a);
+}
+
+template <class SR>
+int spgemm_learned(Context *ctx, const DevMatrix &A, const DevMatrix &B, const gbc_spgemm_opts &opt, int vt,
+                   gbc_result **Cout, gbc_spgemm_stats *st)
+{
+    typedef typename SR::V V;
+    cudaStream_t s = ctx->stream;
+    Workspace ws(ctx);
+    cudaEventRecord(ctx->ev[0], s);
+    Plan P;
+    LearnedOut O;
+    GBC_TRY(learned_into_slots<SR>(ctx, ws, A, B, P, O));
+    const int64_t nb = O.nb;
+    int64_t *ccp = nullptr;
+    GBC_TRY(device_alloc(ctx, (void **)&ccp, (nb + 1) * sizeof(int64_t)));
+    gbc_result *C = new gbc_result();
+    C->ctx = ctx;
+    C->nrow = A.nrow;
+    C->ncol = B.ncol;
+    C->valtype = vt;
+    C->cp = ccp;
+    int rc = exclusive_scan_i64(ws, O.cnt, ccp, nb, s);
+    int64_t nnzc = 0;
+    if (rc == GBC_OK) rc = read_i64(ctx, ccp + nb, &nnzc);
+    C->nnz = nnzc;
+    if (rc == GBC_OK) rc = device_alloc(ctx, (void **)&C->ir, (nnzc + 1) * sizeof(int64_t));
+    if (rc == GBC_OK) rc = device_alloc(ctx, &C->num, (nnzc + 1) * sizeof(V));
+    if (rc == GBC_OK && nb > 0) {
+        k_compact<V><<<grid_for(ctx, (nb + 7) / 8, 8), 256, 0, s>>>(
+            nb, O.cnt, ccp, O.flag, O.beg0, O.ir0, static_cast<const V *>(O.v0), O.beg1, O.ir1,
+            static_cast<const V *>(O.v1), C->ir, static_cast<V *>(C->num));
+        note_launch();
+    }
+    if (rc == GBC_OK) rc = finish_columns(ctx, ws, B, opt, nb, O.cnt, C);
+    cudaEventRecord(ctx->ev[4], s);
+    if (rc == GBC_OK && cudaStreamSynchronize(s) != cudaSuccess) rc = fail(GBC_ECUDA, "learned spgemm failed");
+    if (rc != GBC_OK) {
+        gbc_result_free(C);
+        return rc;
+    }
+    if (st) {
+        float t04 = 0;
+        cudaEventElapsedTime(&t04, ctx->ev[0], ctx->ev[4]);
+        st->flops = O.flops;
+        st->nnz = nnzc;
+        st->overflow_cols = O.overflow_cols;
+        st->alloc_entries = O.alloc;
+        st->ms_total = t04;
+        st->ms_symbolic = O.ms_predict;
+        st->ms_numeric = O.ms_numeric + O.ms_rerun;
+    }
+    *Cout = C;
+    return GBC_OK;
+}
+
+// Features and (optionally) exact counts of every stored column of B, the
+// training data of the sizing model.
+int spgemm_features(gbc_context *ctx, const gbc_matrix *Am, const gbc_matrix *Bm, float *feat_out,
+                    int64_t *flop_out, int64_t *nnz_out, int where)
+{
+    if (!ctx || !Am || !Bm) return fail(GBC_EINVAL, "null argument");
+    if (Am->ncol != Bm->nrow) return fail(GBC_EINVAL, "inner dimensions do not match");
+    GBC_CUDA_TRY(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    Workspace ws(ctx);
+    DevMatrix A, B;
+    GBC_TRY(upload(ws, Am, GBC_F64, &A));
+    GBC_TRY(upload(ws, Bm, GBC_F64, &B));
+    Plan P;
+    GBC_TRY(plan_build(ws, A, B, P));
+    const int64_t nb = P.nb;
+    float *feat = nullptr;
+    GBC_TRY(ws.alloc_n(&feat, (size_t)nb * kNF + 1));
+    if (nb > 0) {
+        k_features<<<grid_for(ctx, (nb + 7) / 8, 8), 256, 0, s>>>(P.a, nb, P.tmask, feat);
+        note_launch();
+    }
+    int64_t *cnt = nullptr;
+    if (nnz_out) {
+        GBC_TRY(ws.alloc_n(&cnt, nb + 1));
+        Lists L;
+        GBC_TRY(plan_classify(P, s, 0, nb, L, cnt));
+        GBC_TRY(run_symbolic(ctx, P, L, cnt));
+    }
+    cudaMemcpyKind k = where == GBC_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (feat_out && nb) GBC_CUDA_TRY(cudaMemcpyAsync(feat_out, feat, (size_t)nb * kNF * sizeof(float), k, s));
+    if (flop_out && nb) GBC_CUDA_TRY(cudaMemcpyAsync(flop_out, P.flop, nb * sizeof(int64_t), k, s));
+    if (nnz_out && nb) GBC_CUDA_TRY(cudaMemcpyAsync(nnz_out, cnt, nb * sizeof(int64_t), k, s));
+    GBC_CUDA_TRY(cudaStreamSynchronize(s));
+    return GBC_OK;
+}
+
+// MCL expansion step: C = A*A (PlusTimes fp32) then prune/select, with exact
+// or learned sizing.  Learned sizing hands the select its slotted product
+// directly (no compaction pass).
+int mcl_select_device2(Context *ctx, int64_t nrow, int64_t n, const int64_t *cnt, const int32_t *flag,
+                       const int64_t *beg0, const int64_t *ir0, const float *v0, const int64_t *beg1,
+                       const int64_t *ir1, const float *v1, float thr, int64_t select, const int64_t *jc,
+                       gbc_result **out);
+
+int mcl_expand(gbc_context *ctx, const gbc_matrix *Am, float thr, int64_t select, int sizing, gbc_result **out,
+               gbc_spgemm_stats *st)
+{
+    if (!ctx || !Am || !out) return fail(GBC_EINVAL, "null argument");
+    if (Am->nrow != Am->ncol) return fail(GBC_EINVAL, "MCL needs a square matrix");
+    GBC_CUDA_TRY(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    Workspace ws(ctx);
+    DevMatrix A;
+    GBC_TRY(upload(ws, Am, GBC_F32, &A));
+    cudaEventRecord(ctx->ev[0], s);
+    if (sizing == GBC_SIZING_LEARNED) {
+        Plan P;
+        LearnedOut O;
+        GBC_TRY(learned_into_slots<PlusTimes<float>>(ctx, ws, A, A, P, O));
+        int64_t *jc = nullptr;
+        GBC_TRY(ws.alloc_n(&jc, O.nb + 1));
+        if (O.nb > 0) {
+            k_iota_jc<<<(unsigned)((O.nb + 255) / 256), 256, 0, s>>>(O.nb, A.jc, jc);
+            note_launch();
+        }
+        GBC_TRY(mcl_select_device2(ctx, A.nrow, O.nb, O.cnt, O.flag, O.beg0, O.ir0, static_cast<const float *>(O.v0),
+                                   O.beg1, O.ir1, static_cast<const float *>(O.v1), thr, select, jc, out));
+        cudaEventRecord(ctx->ev[4], s);
+        GBC_CUDA_TRY(cudaEventSynchronize(ctx->ev[4]));
+        if (st) {
+            float t = 0;
+            cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[4]);
+            st->flops = O.flops;
+            st->nnz = (*out)->nnz;
+            st->overflow_cols = O.overflow_cols;
+            st->alloc_entries = O.alloc;
+            st->ms_total = t;
+            st->ms_symbolic = O.ms_predict;
+            st->ms_numeric = O.ms_numeric + O.ms_rerun;
+        }
+        return GBC_OK;
+    }
+    gbc_result *C = nullptr;
+    gbc_spgemm_opts opt{GBC_SIZING_EXACT, GBC_SORTED, 1, 0};
+    gbc_spgemm_stats s1{};
+    GBC_TRY(spgemm_exact<PlusTimes<float>>(ctx, A, A, opt, GBC_F32, &C, &s1));
+    int rc = mcl_select_device2(ctx, C->nrow, C->nzc, nullptr, nullptr, C->cp, C->ir,
+                                static_cast<const float *>(C->num), nullptr, nullptr, nullptr, thr, select, C->jc, out);
+    gbc_result_free(C);
+    GBC_TRY(rc);
+    cudaEventRecord(ctx->ev[4], s);
+    GBC_CUDA_TRY(cudaEventSynchronize(ctx->ev[4]));
+    if (st) {
+        float t = 0;
+        cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[4]);
+        *st = s1;
+        st->nnz = (*out)->nnz;
+        st->ms_total = t;
+    }
+    return GBC_OK;
 }
 
 template <class SR>
@@ -905,30 +1459,16 @@ int spgemm_colstats(gbc_context *ctx, const gbc_matrix *Am, const gbc_matrix *Bm
     DevMatrix A, B;
     GBC_TRY(upload(ws, Am, GBC_F64, &A));
     GBC_TRY(upload(ws, Bm, GBC_F64, &B));
-    SpgemmArgs a{};
-    int64_t *acp = nullptr;
-    GBC_TRY(prepare_operands(ws, A, B, a, &acp));
-    int64_t nb = B.nzc;
-    int64_t *flop = nullptr, *cnt = nullptr;
-    uint64_t *tmask = nullptr;
-    unsigned long long *work = nullptr;
-    GBC_TRY(ws.alloc_n(&flop, nb + 1));
+    Plan P;
+    GBC_TRY(plan_build(ws, A, B, P));
+    int64_t nb = P.nb;
+    int64_t *cnt = nullptr;
     GBC_TRY(ws.alloc_n(&cnt, nb + 1));
-    GBC_TRY(ws.alloc_n(&tmask, (size_t)nb * a.mask_words + 1));
-    GBC_TRY(ws.alloc_n(&work, 4));
-    GBC_CUDA_TRY(cudaMemsetAsync(work, 0, 4 * sizeof(unsigned long long), s));
-    a.flop = flop;
-    if (nb > 0) {
-        k_flop<<<grid_for(ctx, (nb + 7) / 8, 8), 256, 0, s>>>(nb, B.cp, a.brow, acp, flop); ::gbc::note_launch();
-        int sup_rows = (int)std::min<int64_t>((int64_t)kSymRows, (int64_t)a.T * a.R);
-        sup_rows = (sup_rows / a.R) * a.R;
-        size_t sym_smem = (size_t)sup_rows / 8;
-        GBC_CUDA_TRY(cudaFuncSetAttribute(k_symbolic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sym_smem));
-        k_symbolic<<<grid_for(ctx, nb, 2), kThreads, sym_smem, s>>>(a, cnt, tmask, sup_rows, work); ::gbc::note_launch();
-        GBC_CUDA_TRY(cudaGetLastError());
-    }
+    Lists L;
+    GBC_TRY(plan_classify(P, s, 0, nb, L, cnt));
+    GBC_TRY(run_symbolic(ctx, P, L, cnt));
     cudaMemcpyKind k = where == GBC_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    if (flop_out && nb) GBC_CUDA_TRY(cudaMemcpyAsync(flop_out, flop, nb * sizeof(int64_t), k, s));
+    if (flop_out && nb) GBC_CUDA_TRY(cudaMemcpyAsync(flop_out, P.flop, nb * sizeof(int64_t), k, s));
     if (nnz_out && nb) GBC_CUDA_TRY(cudaMemcpyAsync(nnz_out, cnt, nb * sizeof(int64_t), k, s));
     GBC_CUDA_TRY(cudaStreamSynchronize(s));
     return GBC_OK;
@@ -995,6 +1535,25 @@ int gbc_spgemm_phased(gbc_context *ctx, int sr, int vt, const gbc_matrix *Am, co
     if (sr == GBC_SR_SELECT2NDMIN && vt == GBC_I64)
         return spgemm_phased<Select2ndMin<int64_t>>(ctx, A, B, max_phase_nnz, st);
     return fail(GBC_EUNSUPPORTED, "phased SpGEMM is instantiated for PlusTimes f64/f32 and Select2ndMin i64");
+}
+
+int gbc_spgemm_features(gbc_context *ctx, const gbc_matrix *A, const gbc_matrix *B, float *feat, int64_t *flop,
+                        int64_t *nnz, int where)
+{
+    return spgemm_features(ctx, A, B, feat, flop, nnz, where);
+}
+
+int gbc_context_set_mlp(gbc_context *ctx, gbc_mlp *m)
+{
+    if (!ctx) return fail(GBC_EINVAL, "null context");
+    ctx->mlp = m;
+    return GBC_OK;
+}
+
+int gbc_mcl_expand_f32(gbc_context *ctx, const gbc_matrix *A, float thr, int64_t select, int sizing, gbc_result **out,
+                       gbc_spgemm_stats *st)
+{
+    return mcl_expand(ctx, A, thr, select, sizing, out, st);
 }
 
 int gbc_spgemm_colstats(gbc_context *ctx, const gbc_matrix *A, const gbc_matrix *B, int64_t *flop, int64_t *nnz,

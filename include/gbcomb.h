@@ -165,6 +165,51 @@ int gbc_spgemm_phased(gbc_context *ctx, int sr, int vt, const gbc_matrix *A, con
 int gbc_spgemm_colstats(gbc_context *ctx, const gbc_matrix *A, const gbc_matrix *B, int64_t *flop, int64_t *nnz,
                         int where);
 
+/* -------------------------------------------------------- learned sizing */
+/* The sizing model: a 6-32-32-1 MLP that predicts log2(1 + nnz) of each
+ * output column from per-column features (no counterpart in the reference,
+ * which always runs the exact symbolic pass estimateNNZ_Hash).  Trained and
+ * evaluated by the library's own GPU kernels.  With GBC_SIZING_LEARNED the
+ * predicted capacity replaces the symbolic pass; columns that overflow it are
+ * recomputed exactly, so results are identical to GBC_SIZING_EXACT. */
+typedef struct gbc_mlp gbc_mlp;
+#define GBC_MLP_FEATURES 6
+int gbc_mlp_create(gbc_context *ctx, uint64_t seed, gbc_mlp **m);
+int gbc_mlp_destroy(gbc_mlp *m);
+/* number of floats in the parameter block of gbc_mlp_get / gbc_mlp_set */
+int gbc_mlp_num_params(void);
+int gbc_mlp_get(gbc_mlp *m, float *params, float *margin);
+int gbc_mlp_set(gbc_mlp *m, const float *params, float margin);
+/* Full-batch Adam on (features [n x 6], targets log2(1 + nnz) [n]). */
+int gbc_mlp_train(gbc_context *ctx, gbc_mlp *m, const float *feat, const float *target, int64_t n, int steps, float lr,
+                  float *loss, int where);
+/* grad[num params of the network + 1]: mean-squared-error gradient at the
+ * current parameters, then the loss (checks the backward kernels). */
+int gbc_mlp_gradient(gbc_context *ctx, gbc_mlp *m, const float *feat, const float *target, int64_t n, float *grad,
+                     int where);
+int gbc_mlp_predict(gbc_context *ctx, gbc_mlp *m, const float *feat, int64_t n, float *pred, int where);
+/* Model used by GBC_SIZING_LEARNED on this context (NULL clears it). */
+int gbc_context_set_mlp(gbc_context *ctx, gbc_mlp *m);
+/* Per stored column of B: features [nzc x 6], flop, and (when nnz != NULL)
+ * the exact nnz from the symbolic pass -- the model's training data. */
+int gbc_spgemm_features(gbc_context *ctx, const gbc_matrix *A, const gbc_matrix *B, float *feat, int64_t *flop,
+                        int64_t *nnz, int where);
+
+/* ------------------------------------------------------------------- MCL */
+/* Prune and select of one MCL expansion step on a device fp32 result:
+ * MCLPruneRecoverySelect with recoverNum == 0 (ParFriends.h:185-354) and
+ * Kselect1 (SpParMat.cpp:1191-1300).  A column whose count of entries
+ * > thr exceeds `select` keeps its entries >= the select-th largest value of
+ * the whole column (ties kept); every other column keeps entries >= thr.
+ * Entry order within a column is preserved.  *out is a new result. */
+int gbc_mcl_prune_select_f32(gbc_context *ctx, const gbc_result *C, float thr, int64_t select, gbc_result **out);
+/* One MCL expansion step as MemEfficientSpGEMM(A, A, phases=1, thr, select,
+ * recoverNum=0, ..., computationKernel=1) runs it (ParFriends.h:452): C =
+ * A*A over PlusTimes fp32, then the prune/select above.  sizing is
+ * GBC_SIZING_EXACT or GBC_SIZING_LEARNED; stats describe the SpGEMM. */
+int gbc_mcl_expand_f32(gbc_context *ctx, const gbc_matrix *A, float thr, int64_t select, int sizing, gbc_result **out,
+                       gbc_spgemm_stats *stats);
+
 /* ------------------------------------------------------------ SpMSpV / BFS */
 /* A square pattern matrix prepared once for repeated sparse-vector
  * multiplies and BFS (CSC, jc == NULL; values ignored). */
