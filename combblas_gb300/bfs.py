@@ -4,6 +4,7 @@ Applications/SpMSpV-IPDPS2017/SpMSpVBench.cpp:128-156.  GPU only."""
 from __future__ import annotations
 
 import ctypes as C
+import sys
 
 import numpy as np
 
@@ -30,6 +31,8 @@ class Graph:
             self.h = C.c_void_p()
 
     def __del__(self):
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:

@@ -21,6 +21,7 @@ Every call goes through libgbcomb.so on the GPU; there is no CPU path.
 from __future__ import annotations
 
 import ctypes as C
+import sys
 from dataclasses import dataclass
 
 import numpy as np
@@ -54,6 +55,10 @@ class Context:
             self.h = C.c_void_p()
 
     def __del__(self):
+        # at interpreter exit objects are finalised in no particular order;
+        # the process teardown releases the device memory
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
@@ -231,6 +236,8 @@ class SpResult:
             self.h = C.c_void_p()
 
     def __del__(self):
+        if sys.is_finalizing():
+            return
         try:
             self.free()
         except Exception:

@@ -12,6 +12,7 @@ the statistics class of the training matrices, so reruns reuse them.
 from __future__ import annotations
 
 import ctypes as C
+import sys
 import json
 import os
 
@@ -132,6 +133,8 @@ class SizingModel:
             self.h = C.c_void_p()
 
     def __del__(self):
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:

@@ -52,13 +52,14 @@ def test_training_reduces_loss_and_is_deterministic(gpu_ctx):
 
 @pytest.mark.parametrize("kind", ["rmat", "mcl"])
 def test_learned_identical_to_exact(gpu_ctx, kind):
+    # the model is trained on another matrix of the same statistics class
     if kind == "rmat":
         A = G.rmat(14, 8, seed=41)
-        Atrain = G.rmat(13, 8, seed=42)
+        Atrain = G.rmat(14, 8, seed=42)
         dt = np.float64
     else:
         A = G.mcl_planted(1 << 15, 512, 20, 5, seed=43)
-        Atrain = G.mcl_planted(1 << 14, 512, 20, 5, seed=44)
+        Atrain = G.mcl_planted(1 << 15, 512, 20, 5, seed=44)
         dt = np.float32
     m, info, _, _, _ = trained_model(Atrain)
     m.use()
@@ -67,7 +68,6 @@ def test_learned_identical_to_exact(gpu_ctx, kind):
     ce, cl = Re.to_csc(), Rl.to_csc()
     assert all(np.array_equal(x, y) for x, y in zip(ce, cl))
     st = Rl.stats
-    assert st.alloc_entries >= st.nnz - 0  # slots hold at least the kept entries of non-overflow columns
     assert st.overflow_cols <= 0.05 * A.ncol
     m.close()
 
@@ -89,20 +89,20 @@ def test_model_beats_flop_bound_sizing(gpu_ctx):
     """What the network gains over sizing without it: the capacity it
     allocates is far below the multiplication-count bound (the only size
     known without a symbolic pass), at a small overflow rate."""
-    A = G.mcl_planted(1 << 15, 512, 20, 5, seed=61)
-    m, info, feat, flop, nnz = trained_model(G.mcl_planted(1 << 15, 512, 20, 5, seed=62))
+    A = G.rmat(15, 8, seed=61)
+    m, info, feat, flop, nnz = trained_model(G.rmat(15, 8, seed=62))
     m.use()
-    Rl = local.spgemm(A, A, dtype=np.float32, sizing="learned")
+    Rl = local.spgemm(A, A, sizing="learned")
     st = Rl.stats
     bound = int(np.minimum(sizing.features(A, A, exact=False)[1], A.nrow).sum())
-    assert st.alloc_entries < 0.8 * bound
+    assert st.alloc_entries < 0.6 * bound
     assert st.overflow_cols < 0.02 * A.ncol
     m.close()
 
 
 def test_mcl_learned_identical(gpu_ctx):
     A = G.mcl_planted(1 << 15, 512, 24, 6, seed=71)
-    m, _, _, _, _ = trained_model(G.mcl_planted(1 << 14, 512, 24, 6, seed=72))
+    m, _, _, _, _ = trained_model(G.mcl_planted(1 << 15, 512, 24, 6, seed=72))
     m.use()
     Re, se = mcl.mcl_expand(A, 1e-4, 50, sizing="exact")
     Rl, sl = mcl.mcl_expand(A, 1e-4, 50, sizing="learned")
