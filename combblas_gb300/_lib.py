@@ -98,6 +98,13 @@ for _n in ("plustimes_f64", "plustimes_f32", "plustimes_i64", "minplus_f64", "mi
                                                C.POINTER(gbc_spgemm_stats)])
 _SIGS["gbc_spgemm_bool_i64"] = _SIGS["gbc_spgemm_plustimes_f64_i64"]
 _SIGS.update({
+    "gbc_batch_create": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(gbc_matrix),
+                                   C.POINTER(gbc_matrix), C.c_int64, C.c_int64, C.POINTER(C.c_void_p)]),
+    "gbc_batch_run": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "gbc_batch_info": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                 C.POINTER(C.c_int64)]),
+    "gbc_batch_result": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "gbc_batch_destroy": (C.c_int, [C.c_void_p]),
     "gbc_mlp_create": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
     "gbc_mlp_destroy": (C.c_int, [C.c_void_p]),
     "gbc_mlp_num_params": (C.c_int, []),

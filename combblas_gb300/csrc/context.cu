@@ -12,6 +12,8 @@ static thread_local std::string g_err;
 static std::atomic<long long> g_launches{0};
 
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void note_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(); }
 
 void set_error(const std::string &msg) { g_err = msg; }
 
@@ -205,6 +207,42 @@ int exclusive_scan_i64(Workspace &ws, const int64_t *in, int64_t *out, int64_t n
     GBC_CUDA_TRY(cudaGetLastError());
     GBC_TRY(exclusive_scan_i64(ws, sums, sums, tiles, s));
     k_tile_scan<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(in, out, n, sums); ::gbc::note_launch();
+    GBC_CUDA_TRY(cudaGetLastError());
+    return GBC_OK;
+}
+
+int64_t scan_tmp_elems(int64_t n)
+{
+    int64_t t = 0;
+    while (n > SCAN_TILE) {
+        const int64_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+        t += tiles + 1;
+        n = tiles;
+    }
+    return t + 1;
+}
+
+// Same scan with caller-provided temporary storage (scan_tmp_elems(n)
+// int64s): no allocation, so it can be captured into a CUDA graph.
+int exclusive_scan_i64_tmp(const int64_t *in, int64_t *out, int64_t n, int64_t *tmp, cudaStream_t s)
+{
+    if (n <= 0) {
+        GBC_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(int64_t), s));
+        return GBC_OK;
+    }
+    const int64_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (tiles == 1) {
+        k_tile_scan<<<1, SCAN_THREADS, 0, s>>>(in, out, n, nullptr);
+        note_launch();
+        GBC_CUDA_TRY(cudaGetLastError());
+        return GBC_OK;
+    }
+    int64_t *sums = tmp;
+    k_tile_sums<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(in, n, sums);
+    note_launch();
+    GBC_TRY(exclusive_scan_i64_tmp(sums, sums, tiles, tmp + tiles + 1, s));
+    k_tile_scan<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(in, out, n, sums);
+    note_launch();
     GBC_CUDA_TRY(cudaGetLastError());
     return GBC_OK;
 }

@@ -33,6 +33,10 @@ int fail(int code, const std::string &msg);
 // Count of kernel launches issued by this library (all contexts, this
 // process); reported by gbc_launch_count().
 void note_launch();
+// Adjust the count by n (graph captures record kernels without running them;
+// each replay then runs them).
+void note_launches(long long n);
+long long launch_count();
 
 // ---------------------------------------------------------------- context
 struct Context {
@@ -95,6 +99,9 @@ int upload(Workspace &ws, const gbc_matrix *M, int vt, DevMatrix *out);
 // --------------------------------------------------------------- scans
 // Exclusive scan of n int64 values (out may alias in); out[n] = total.
 int exclusive_scan_i64(Workspace &ws, const int64_t *in, int64_t *out, int64_t n, cudaStream_t s);
+// Allocation-free form (graph-capturable); tmp holds scan_tmp_elems(n) int64s.
+int64_t scan_tmp_elems(int64_t n);
+int exclusive_scan_i64_tmp(const int64_t *in, int64_t *out, int64_t n, int64_t *tmp, cudaStream_t s);
 
 }  // namespace gbc
 

@@ -22,6 +22,9 @@
 //                 (tile order, then bitmap order): no sort is needed.
 #include <algorithm>
 #include <cstdio>
+#include <functional>
+#include <map>
+#include <mutex>
 
 #include "gbc_internal.cuh"
 #include "semiring.cuh"
@@ -176,28 +179,30 @@ __global__ void k_flop_mask(int64_t nb, const int64_t *bcp, const int32_t *brow,
     }
 }
 
-// Split stored columns j0..j1-1 of B by their flop count: empty (count 0),
-// small (<= kSmall1, <= kSmall2 multiplications, warp kernels) and big (block
-// kernels).  Lists are appended in any order; every column is written to its
-// own output range, so the order does not affect the result.
+// Split stored columns j0..j1-1 of one product by their flop count: empty
+// (count 0), small (<= s1 and <= s2 multiplications: warp kernels) and big
+// (block kernels).  The thresholds are tuning parameters (s1 <= kSmall1,
+// s2 <= kSmall2).  Lists are appended in any order; every column is written
+// to its own output range, so the order does not affect the result.
 constexpr int kSmall1 = 256;
 constexpr int kSmall2 = 4096;
 
-__global__ void k_classify(const int64_t *flop, int64_t j0, int64_t j1, int32_t *l1, int32_t *l2, int32_t *lb,
-                           unsigned long long *counts, int64_t *cnt_zero)
+__global__ void k_classify(const int64_t *flop, int pid, int64_t col_base, int64_t j0, int64_t j1, int64_t s1,
+                           int64_t s2, int64_t *l1, int64_t *l2, int64_t *lb, unsigned long long *counts,
+                           int64_t *cnt_zero, const int32_t *only_flagged)
 {
     const int64_t i = j0 + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     int cls = -1;
-    if (i < j1) {
+    if (i < j1 && (!only_flagged || only_flagged[col_base + i])) {
         const int64_t f = flop[i];
         if (f == 0) {
-            if (cnt_zero) cnt_zero[i] = 0;
+            if (cnt_zero) cnt_zero[col_base + i] = 0;
         } else {
-            cls = f <= kSmall1 ? 0 : (f <= kSmall2 ? 1 : 2);
+            cls = f <= s1 ? 0 : (f <= s2 ? 1 : 2);
         }
     }
-    int32_t *lists[3] = {l1, l2, lb};
+    int64_t *lists[3] = {l1, l2, lb};
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const unsigned m = __ballot_sync(0xffffffffu, cls == c);
@@ -206,7 +211,7 @@ __global__ void k_classify(const int64_t *flop, int64_t j0, int64_t j1, int32_t 
         unsigned long long base = 0;
         if (lane == leader) base = atomicAdd(&counts[c], (unsigned long long)__popc(m));
         base = __shfl_sync(0xffffffffu, base, leader);
-        if (cls == c) lists[c][base + __popc(m & ((1u << lane) - 1))] = (int32_t)i;
+        if (cls == c) lists[c][base + __popc(m & ((1u << lane) - 1))] = make_item(pid, i);
     }
 }
 
@@ -214,22 +219,28 @@ __global__ void k_classify(const int64_t *flop, int64_t j0, int64_t j1, int32_t 
 // One block per listed column (dynamic work counter).  Bitmap over a
 // super-tile of sup_rows rows (a whole number of R-row tiles); products set
 // bits; the column's count is the popcount.
-__global__ void __launch_bounds__(kThreads) k_symbolic(SpgemmArgs a, const int32_t *cols, int64_t ncols,
-                                                       int64_t *cnt, int sup_rows, unsigned long long *work)
+__global__ void __launch_bounds__(kThreads) k_symbolic(const SpgemmArgs *args, const int64_t *items,
+                                                       int64_t nitems, int64_t *cnt, unsigned long long *work)
 {
     extern __shared__ uint32_t bm[];
     __shared__ ChunkSmem ch;
     __shared__ int64_t s_col;
     __shared__ int64_t s_red[kThreads / 32];
+    __shared__ SpgemmArgs sa;
     const int tid = threadIdx.x;
-    const int tiles_per_sup = sup_rows / a.R;
     for (;;) {
-        if (tid == 0) s_col = (int64_t)atomicAdd(work, 1ull);
+        if (tid == 0) {
+            s_col = (int64_t)atomicAdd(work, 1ull);
+            if (s_col < nitems) sa = args[item_pid(items[s_col])];
+        }
         __syncthreads();
         const int64_t ci = s_col;
         __syncthreads();
-        if (ci >= ncols) break;
-        const int64_t i = cols[ci];
+        if (ci >= nitems) break;
+        const SpgemmArgs &a = sa;
+        const int64_t i = item_col(items[ci]);
+        const int sup_rows = (int)((min((int64_t)kSymRows, (int64_t)a.T * a.R) / a.R) * a.R);
+        const int tiles_per_sup = sup_rows / a.R;
         int64_t bs = a.bcp[i], be = a.bcp[i + 1];
         int64_t total = 0;
         if (a.flop[i] > 0) {
@@ -265,7 +276,7 @@ __global__ void __launch_bounds__(kThreads) k_symbolic(SpgemmArgs a, const int32
         if (tid == 0) {
             int64_t s = 0;
             for (int w = 0; w < kThreads / 32; ++w) s += s_red[w];
-            cnt[i] = s;
+            cnt[a.col_base + i] = s;
         }
         __syncthreads();
     }
@@ -325,46 +336,51 @@ __device__ __forceinline__ void seg_max_scan(uint8_t *seg, int seed)
 }
 
 template <class SR>
-__global__ void __launch_bounds__(kThreads, 1) k_numeric(SpgemmArgs a, const void *aval_v, const void *bval_v,
-                                                         const uint64_t *tmask, const int32_t *cols, int64_t ncols,
+__global__ void __launch_bounds__(kThreads, 1) k_numeric(const SpgemmArgs *args, const int64_t *items, int64_t nitems,
                                                          const int64_t *ccp, int64_t ccp_base, const int64_t *cap,
                                                          int64_t *out_cnt, int32_t *overflow, int64_t *cir,
                                                          void *cval_v, unsigned long long *work)
 {
     typedef typename SR::V V;
     extern __shared__ __align__(16) unsigned char smem[];
-    V *acc = reinterpret_cast<V *>(smem);                            // [R]
-    V *sval = acc + a.R;                                             // [kSub]
-    uint32_t *bm = reinterpret_cast<uint32_t *>(sval + kSub);        // [R/32]
-    uint16_t *srow = reinterpret_cast<uint16_t *>(bm + (a.R >> 5));  // [kSub]
-    uint8_t *seg = reinterpret_cast<uint8_t *>(srow + kSub);         // [kSub]
     __shared__ ChunkSmem ch;
     __shared__ V ch_bv[kThreads];
     __shared__ int32_t s_cnt[kWarps * kSubPerThread * kWarps + 1];  // [owner][round][warp]
     __shared__ int64_t s_col;
-    const V *aval = static_cast<const V *>(aval_v);
-    const V *bval = static_cast<const V *>(bval_v);
+    __shared__ SpgemmArgs sa;
     V *cval = static_cast<V *>(cval_v);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned lt = (1u << lane) - 1;
-    const int words = a.R >> 5;
     constexpr int NC = kWarps * kSubPerThread * kWarps;
 
     for (;;) {
-        if (tid == 0) s_col = (int64_t)atomicAdd(work, 1ull);
+        if (tid == 0) {
+            s_col = (int64_t)atomicAdd(work, 1ull);
+            if (s_col < nitems) sa = args[item_pid(items[s_col])];
+        }
         __syncthreads();
         const int64_t ci = s_col;
         __syncthreads();
-        if (ci >= ncols) break;
-        const int64_t i = cols[ci];
+        if (ci >= nitems) break;
+        const SpgemmArgs &a = sa;
+        const int64_t i = item_col(items[ci]);
+        const int64_t g = a.col_base + i;
+        V *acc = reinterpret_cast<V *>(smem);                            // [R]
+        V *sval = acc + a.R;                                             // [kSub]
+        uint32_t *bm = reinterpret_cast<uint32_t *>(sval + kSub);        // [R/32]
+        uint16_t *srow = reinterpret_cast<uint16_t *>(bm + (a.R >> 5));  // [kSub]
+        uint8_t *seg = reinterpret_cast<uint8_t *>(srow + kSub);         // [kSub]
+        const V *aval = static_cast<const V *>(a.aval);
+        const V *bval = static_cast<const V *>(a.bval);
+        const int words = a.R >> 5;
         const int64_t bs = a.bcp[i], be = a.bcp[i + 1];
-        // ccp is indexed relative to ccp_base (the first column of a phase)
-        const int64_t out0 = ccp[i - ccp_base];
+        // ccp is indexed by batch-wide column relative to ccp_base
+        const int64_t out0 = ccp[g - ccp_base];
         int64_t out = out0;
-        const int64_t lim = cap ? out0 + cap[i] : ccp[i - ccp_base + 1];
+        const int64_t lim = cap ? out0 + cap[g] : ccp[g - ccp_base + 1];
         bool over = false;
         for (int mw = 0; mw < a.mask_words; ++mw) {
-            uint64_t msk = tmask[i * a.mask_words + mw];
+            uint64_t msk = a.tmask[i * a.mask_words + mw];
             while (msk) {
                 const int t = mw * 64 + __ffsll((long long)msk) - 1;
                 msk &= msk - 1;
@@ -507,10 +523,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_numeric(SpgemmArgs a, const voi
         }
         over = __syncthreads_or(over);
         if (tid == 0) {
-            if (out_cnt) out_cnt[i] = out - out0;
+            if (out_cnt) out_cnt[g] = out - out0;
             if (over) {
                 if (overflow)
-                    overflow[i] = 1;
+                    overflow[g] = 1;
                 else
                     atomicOr(a.err, 128);  // exact sizing: counts disagree
             }
@@ -621,68 +637,108 @@ int prepare_operands(Workspace &ws, const DevMatrix &A, const DevMatrix &B, Spge
     return GBC_OK;
 }
 
-// Everything the numeric passes need, built once per product.
+// Everything the passes need, built once: one descriptor per product of a
+// batch (a single product is a batch of one).
 struct Plan {
-    SpgemmArgs a{};
-    int64_t nb = 0;
-    int64_t *flop = nullptr;
-    uint64_t *tmask = nullptr;
-    int key_bits = 0;
+    std::vector<SpgemmArgs> h;        // host copies of the descriptors
+    SpgemmArgs *d = nullptr;          // device array
+    int64_t total_cols = 0;           // stored columns of all B's
+    int max_R = 0, max_key_bits = 0;
+    size_t max_sym_smem = 0;
+    int64_t s1 = kSmall1, s2 = kSmall2;  // flop thresholds of the column classes
     unsigned long long *work = nullptr;  // kernel work counters
-    int32_t *lbuf = nullptr;             // column lists (3 x nb)
+    int64_t *lbuf = nullptr;             // column lists (3 x (total_cols + 1))
     unsigned long long *lcnt = nullptr;  // list lengths
+    SpgemmArgs &a() { return h[0]; }
 };
 
 struct Lists {
-    const int32_t *l[3] = {nullptr, nullptr, nullptr};  // small1, small2, big
+    const int64_t *l[3] = {nullptr, nullptr, nullptr};  // small1, small2, big
     int64_t n[3] = {0, 0, 0};
 };
 
-static int plan_build(Workspace &ws, const DevMatrix &A, const DevMatrix &B, Plan &P)
+// Prepare one product (A*B) and append it to the plan.
+static int plan_add(Workspace &ws, Plan &P, const DevMatrix &A, const DevMatrix &B)
 {
     Context *ctx = ws.ctx;
     cudaStream_t s = ctx->stream;
+    SpgemmArgs a{};
     int64_t *acp = nullptr;
-    GBC_TRY(prepare_operands(ws, A, B, P.a, &acp));
-    SpgemmArgs &a = P.a;
-    P.nb = B.nzc;
+    GBC_TRY(prepare_operands(ws, A, B, a, &acp));
+    const int64_t nb = B.nzc;
     int64_t m1 = A.nrow > 1 ? A.nrow - 1 : 0;
-    P.key_bits = 0;
+    a.key_bits = 0;
     while (m1 > 0) {
-        ++P.key_bits;
+        ++a.key_bits;
         m1 >>= 1;
     }
-    uint64_t *amask = nullptr;
+    uint64_t *amask = nullptr, *tmask = nullptr;
+    int64_t *flop = nullptr;
     GBC_TRY(ws.alloc_n(&amask, (size_t)A.ncol * a.mask_words + 1));
-    GBC_TRY(ws.alloc_n(&P.flop, P.nb + 1));
-    GBC_TRY(ws.alloc_n(&P.tmask, (size_t)P.nb * a.mask_words + 1));
-    GBC_TRY(ws.alloc_n(&P.work, 16));
-    GBC_TRY(ws.alloc_n(&P.lbuf, 3 * (size_t)P.nb + 3));
-    GBC_TRY(ws.alloc_n(&P.lcnt, 4));
+    GBC_TRY(ws.alloc_n(&flop, nb + 1));
+    GBC_TRY(ws.alloc_n(&tmask, (size_t)nb * a.mask_words + 1));
     if (A.ncol > 0) {
         k_amask<<<(unsigned)((A.ncol + 255) / 256), 256, 0, s>>>(A.ncol, a.tptr, a.T, a.mask_words, amask);
         note_launch();
     }
-    if (P.nb > 0) {
-        k_flop_mask<<<grid_for(ctx, (P.nb + 7) / 8, 8), 256, 0, s>>>(P.nb, B.cp, a.brow, acp, amask, a.mask_words,
-                                                                       P.flop, P.tmask);
+    if (nb > 0) {
+        k_flop_mask<<<grid_for(ctx, (nb + 7) / 8, 8), 256, 0, s>>>(nb, B.cp, a.brow, acp, amask, a.mask_words, flop,
+                                                                     tmask);
         note_launch();
     }
-    a.flop = P.flop;
     GBC_CUDA_TRY(cudaGetLastError());
+    a.flop = flop;
+    a.tmask = tmask;
+    a.aval = A.num;
+    a.bval = B.num;
+    a.col_base = P.total_cols;
+    P.total_cols += nb;
+    P.max_R = std::max(P.max_R, a.R);
+    P.max_key_bits = std::max(P.max_key_bits, a.key_bits);
+    int sup_rows = (int)std::min<int64_t>((int64_t)kSymRows, (int64_t)a.T * a.R);
+    sup_rows = (sup_rows / a.R) * a.R;
+    P.max_sym_smem = std::max(P.max_sym_smem, (size_t)sup_rows / 8);
+    P.h.push_back(a);
     return GBC_OK;
 }
 
-// Column lists of stored columns [j0, j1); empty columns get cnt 0.
-static int plan_classify(Plan &P, cudaStream_t s, int64_t j0, int64_t j1, Lists &L, int64_t *cnt_zero)
+static int plan_finalize(Workspace &ws, Plan &P)
+{
+    GBC_TRY(ws.alloc_n(&P.d, P.h.size() + 1));
+    GBC_TRY(ws.alloc_n(&P.work, 16));
+    GBC_TRY(ws.alloc_n(&P.lbuf, 3 * ((size_t)P.total_cols + 1)));
+    GBC_TRY(ws.alloc_n(&P.lcnt, 4));
+    GBC_CUDA_TRY(cudaMemcpyAsync(P.d, P.h.data(), P.h.size() * sizeof(SpgemmArgs), cudaMemcpyHostToDevice,
+                                 ws.ctx->stream));
+    return GBC_OK;
+}
+
+static int plan_build(Workspace &ws, const DevMatrix &A, const DevMatrix &B, Plan &P)
+{
+    GBC_TRY(plan_add(ws, P, A, B));
+    return plan_finalize(ws, P);
+}
+
+// Column lists: for every product (or only `pid` >= 0) its stored columns
+// [j0, j1) (j1 < 0: all), optionally only the flagged ones; empty columns
+// get cnt 0 in cnt_zero.
+static int plan_classify(Plan &P, cudaStream_t s, int pid, int64_t j0, int64_t j1, Lists &L, int64_t *cnt_zero,
+                         const int32_t *flagged = nullptr)
 {
     GBC_CUDA_TRY(cudaMemsetAsync(P.lcnt, 0, 4 * sizeof(unsigned long long), s));
-    int32_t *l0 = P.lbuf, *l1 = P.lbuf + P.nb + 1, *l2 = P.lbuf + 2 * (P.nb + 1);
-    if (j1 > j0) {
-        k_classify<<<(unsigned)((j1 - j0 + 255) / 256), 256, 0, s>>>(P.flop, j0, j1, l0, l1, l2, P.lcnt, cnt_zero);
-        note_launch();
-        GBC_CUDA_TRY(cudaGetLastError());
+    const int64_t stride = P.total_cols + 1;
+    int64_t *l0 = P.lbuf, *l1 = P.lbuf + stride, *l2 = P.lbuf + 2 * stride;
+    for (int q = 0; q < (int)P.h.size(); ++q) {
+        if (pid >= 0 && q != pid) continue;
+        const SpgemmArgs &a = P.h[q];
+        const int64_t lo = pid >= 0 ? j0 : 0, hi = (pid >= 0 && j1 >= 0) ? j1 : a.nb;
+        if (hi > lo) {
+            k_classify<<<(unsigned)((hi - lo + 255) / 256), 256, 0, s>>>(a.flop, q, a.col_base, lo, hi, P.s1, P.s2,
+                                                                         l0, l1, l2, P.lcnt, cnt_zero, flagged);
+            note_launch();
+        }
     }
+    GBC_CUDA_TRY(cudaGetLastError());
     unsigned long long h[4];
     GBC_CUDA_TRY(cudaMemcpyAsync(h, P.lcnt, sizeof(h), cudaMemcpyDeviceToHost, s));
     GBC_CUDA_TRY(cudaStreamSynchronize(s));
@@ -693,23 +749,33 @@ static int plan_classify(Plan &P, cudaStream_t s, int64_t j0, int64_t j1, Lists 
     return GBC_OK;
 }
 
+// Raise a kernel's dynamic shared-memory limit once (per device and kernel,
+// only upwards), so replays and graph captures make no attribute calls.
 template <class K>
 static int set_smem(K kernel, size_t bytes)
 {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, size_t> done;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    size_t &cur = done[{dev, (const void *)kernel}];
+    if (cur >= bytes) return GBC_OK;
     GBC_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    cur = bytes;
     return GBC_OK;
 }
 
-// Exact nnz per listed column (estimateNNZ_Hash's result).
+// Exact nnz per listed column (estimateNNZ_Hash's result), into the
+// batch-wide array cnt.
 static int run_symbolic(Context *ctx, Plan &P, const Lists &L, int64_t *cnt)
 {
     cudaStream_t s = ctx->stream;
-    SpgemmArgs &a = P.a;
     if (L.n[0] > 0) {
         constexpr int WPB = 8, TS = 2 * kSmall1;
         const size_t sm = (size_t)WPB * TS * 4;
         GBC_TRY(set_smem(k_small_count<TS, WPB>, sm));
-        k_small_count<TS, WPB><<<grid_for(ctx, (L.n[0] + WPB - 1) / WPB, 8), WPB * 32, sm, s>>>(a, L.l[0], L.n[0],
+        k_small_count<TS, WPB><<<grid_for(ctx, (L.n[0] + WPB - 1) / WPB, 8), WPB * 32, sm, s>>>(P.d, L.l[0], L.n[0],
                                                                                                  cnt);
         note_launch();
     }
@@ -719,18 +785,16 @@ static int run_symbolic(Context *ctx, Plan &P, const Lists &L, int64_t *cnt)
         GBC_TRY(set_smem(k_small_count<TS, WPB>, sm));
         int per_sm = std::max(1, (int)(ctx->smem_optin / (sm + 1024)));
         k_small_count<TS, WPB><<<grid_for(ctx, (L.n[1] + WPB - 1) / WPB, per_sm), WPB * 32, sm, s>>>(
-            a, L.l[1], L.n[1], cnt);
+            P.d, L.l[1], L.n[1], cnt);
         note_launch();
     }
     if (L.n[2] > 0) {
-        int sup_rows = (int)std::min<int64_t>((int64_t)kSymRows, (int64_t)a.T * a.R);
-        sup_rows = (sup_rows / a.R) * a.R;
-        size_t sym_smem = (size_t)sup_rows / 8;
+        const size_t sym_smem = P.max_sym_smem;
         GBC_TRY(set_smem(k_symbolic, sym_smem));
         int per_sm = std::max(1, (int)(ctx->smem_optin / (sym_smem + 8192)));
         GBC_CUDA_TRY(cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), s));
-        k_symbolic<<<grid_for(ctx, L.n[2], std::min(per_sm, 8)), kThreads, sym_smem, s>>>(a, L.l[2], L.n[2], cnt,
-                                                                                             sup_rows, P.work);
+        k_symbolic<<<grid_for(ctx, L.n[2], std::min(per_sm, 8)), kThreads, sym_smem, s>>>(P.d, L.l[2], L.n[2], cnt,
+                                                                                             P.work);
         note_launch();
     }
     GBC_CUDA_TRY(cudaGetLastError());
@@ -738,68 +802,68 @@ static int run_symbolic(Context *ctx, Plan &P, const Lists &L, int64_t *cnt)
 }
 
 template <class SR, int FS, int WPB, bool PACK>
-static int launch_small(Context *ctx, Plan &P, const int32_t *cols, int64_t n, const void *aval, const void *bval,
-                        const int64_t *ccp, int64_t ccp_base, const int64_t *cap, int64_t *out_cnt, int32_t *overflow,
-                        int64_t *cir, void *cval)
+static int launch_small(Context *ctx, Plan &P, const int64_t *items, int64_t n, const int64_t *ccp, int64_t ccp_base,
+                        const int64_t *cap, int64_t *out_cnt, int32_t *overflow, int64_t *cir, void *cval)
 {
     typedef typename SR::V V;
     const size_t sm = WPB * small_warp_smem<FS, V, PACK>();
     GBC_TRY(set_smem(k_small_numeric<SR, FS, WPB, PACK>, sm));
     int per_sm = std::max(1, (int)(ctx->smem_optin / (sm + 1024)));
     k_small_numeric<SR, FS, WPB, PACK><<<grid_for(ctx, (n + WPB - 1) / WPB, std::min(per_sm, 8)), WPB * 32, sm,
-                                         ctx->stream>>>(P.a, aval, bval, cols, n, ccp, ccp_base, cap, out_cnt,
-                                                        overflow, cir, cval, P.key_bits);
+                                         ctx->stream>>>(P.d, items, n, ccp, ccp_base, cap, out_cnt, overflow, cir,
+                                                        cval);
     note_launch();
     return GBC_OK;
 }
 
 // Numeric pass over the listed columns.  Exact sizing: cap == nullptr and
 // ccp holds the exact offsets.  Learned sizing: cap gives each column's room
-// at ccp[i - ccp_base]; out_cnt/overflow receive actual counts and flags.
+// at ccp[g - ccp_base]; out_cnt/overflow receive actual counts and flags.
+// All per-column arrays are indexed by batch-wide column g.
 template <class SR>
-static int run_numeric(Context *ctx, Plan &P, const Lists &L, const void *aval, const void *bval, const int64_t *ccp,
-                       int64_t ccp_base, const int64_t *cap, int64_t *out_cnt, int32_t *overflow, int64_t *cir,
-                       void *cval)
+static int run_numeric(Context *ctx, Plan &P, const Lists &L, const int64_t *ccp, int64_t ccp_base, const int64_t *cap,
+                       int64_t *out_cnt, int32_t *overflow, int64_t *cir, void *cval)
 {
     typedef typename SR::V V;
     cudaStream_t s = ctx->stream;
-    SpgemmArgs &a = P.a;
-    const bool pack = P.key_bits <= 20;
+    const bool pack = P.max_key_bits <= 20;
     if (L.n[0] > 0) {
         if (pack)
-            GBC_TRY((launch_small<SR, kSmall1, 8, true>(ctx, P, L.l[0], L.n[0], aval, bval, ccp, ccp_base, cap,
-                                                         out_cnt, overflow, cir, cval)));
+            GBC_TRY((launch_small<SR, kSmall1, 8, true>(ctx, P, L.l[0], L.n[0], ccp, ccp_base, cap, out_cnt, overflow,
+                                                         cir, cval)));
         else
-            GBC_TRY((launch_small<SR, kSmall1, 8, false>(ctx, P, L.l[0], L.n[0], aval, bval, ccp, ccp_base, cap,
-                                                          out_cnt, overflow, cir, cval)));
+            GBC_TRY((launch_small<SR, kSmall1, 8, false>(ctx, P, L.l[0], L.n[0], ccp, ccp_base, cap, out_cnt,
+                                                          overflow, cir, cval)));
     }
     if (L.n[1] > 0) {
         if (pack)
-            GBC_TRY((launch_small<SR, kSmall2, 2, true>(ctx, P, L.l[1], L.n[1], aval, bval, ccp, ccp_base, cap,
-                                                         out_cnt, overflow, cir, cval)));
+            GBC_TRY((launch_small<SR, kSmall2, 2, true>(ctx, P, L.l[1], L.n[1], ccp, ccp_base, cap, out_cnt, overflow,
+                                                         cir, cval)));
         else
-            GBC_TRY((launch_small<SR, kSmall2, 2, false>(ctx, P, L.l[1], L.n[1], aval, bval, ccp, ccp_base, cap,
-                                                          out_cnt, overflow, cir, cval)));
+            GBC_TRY((launch_small<SR, kSmall2, 2, false>(ctx, P, L.l[1], L.n[1], ccp, ccp_base, cap, out_cnt,
+                                                          overflow, cir, cval)));
     }
     if (L.n[2] > 0) {
-        const size_t num_smem = numeric_smem_bytes(a.R, sizeof(V));
+        const size_t num_smem = numeric_smem_bytes(P.max_R, sizeof(V));
         GBC_TRY(set_smem(k_numeric<SR>, num_smem));
         int per_sm = std::max(1, (int)(ctx->smem_optin / (num_smem + 12288)));
         GBC_CUDA_TRY(cudaMemsetAsync(P.work + 1, 0, sizeof(unsigned long long), s));
         k_numeric<SR><<<grid_for(ctx, L.n[2], std::min(per_sm, 8)), kThreads, num_smem, s>>>(
-            a, aval, bval, P.tmask, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir, cval, P.work + 1);
+            P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir, cval, P.work + 1);
         note_launch();
     }
     GBC_CUDA_TRY(cudaGetLastError());
     return GBC_OK;
 }
 
-static int check_err(Context *ctx, const SpgemmArgs &a)
+static int check_err(Context *ctx, const Plan &P)
 {
-    int32_t herr = 0;
-    GBC_CUDA_TRY(cudaMemcpyAsync(&herr, a.err, sizeof(herr), cudaMemcpyDeviceToHost, ctx->stream));
-    GBC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-    if (herr) return fail(GBC_ECUDA, "internal error: numeric and symbolic counts disagree");
+    for (const SpgemmArgs &a : P.h) {
+        int32_t herr = 0;
+        GBC_CUDA_TRY(cudaMemcpyAsync(&herr, a.err, sizeof(herr), cudaMemcpyDeviceToHost, ctx->stream));
+        GBC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+        if (herr) return fail(GBC_ECUDA, "internal error: numeric and symbolic counts disagree");
+    }
     return GBC_OK;
 }
 
@@ -861,12 +925,13 @@ static int spgemm_exact(Context *ctx, const DevMatrix &A, const DevMatrix &B, co
     Workspace ws(ctx);
     cudaEventRecord(ctx->ev[0], s);
     Plan P;
+    if (opt.reserved > 0) P.s2 = std::min<int64_t>(kSmall2, opt.reserved);
     GBC_TRY(plan_build(ws, A, B, P));
-    const int64_t nb = P.nb;
+    const int64_t nb = B.nzc;
     int64_t *cnt = nullptr, *ccp = nullptr;
     GBC_TRY(ws.alloc_n(&cnt, nb + 1));
     Lists L;
-    GBC_TRY(plan_classify(P, s, 0, nb, L, cnt));
+    GBC_TRY(plan_classify(P, s, -1, 0, -1, L, cnt));
     cudaEventRecord(ctx->ev[1], s);
     GBC_TRY(run_symbolic(ctx, P, L, cnt));
     GBC_TRY(device_alloc(ctx, (void **)&ccp, (nb + 1) * sizeof(int64_t)));
@@ -883,18 +948,17 @@ static int spgemm_exact(Context *ctx, const DevMatrix &A, const DevMatrix &B, co
     C->nnz = nnzc;
     if (rc == GBC_OK) rc = device_alloc(ctx, (void **)&C->ir, (nnzc + 1) * sizeof(int64_t));
     if (rc == GBC_OK) rc = device_alloc(ctx, &C->num, (nnzc + 1) * sizeof(V));
-    if (rc == GBC_OK && nnzc > 0)
-        rc = run_numeric<SR>(ctx, P, L, A.num, B.num, ccp, 0, nullptr, nullptr, nullptr, C->ir, C->num);
+    if (rc == GBC_OK && nnzc > 0) rc = run_numeric<SR>(ctx, P, L, ccp, 0, nullptr, nullptr, nullptr, C->ir, C->num);
     cudaEventRecord(ctx->ev[3], s);
     if (rc == GBC_OK) rc = finish_columns(ctx, ws, B, opt, nb, cnt, C);
     cudaEventRecord(ctx->ev[4], s);
-    if (rc == GBC_OK) rc = check_err(ctx, P.a);
+    if (rc == GBC_OK) rc = check_err(ctx, P);
     if (rc != GBC_OK) {
         gbc_result_free(C);
         return rc;
     }
     if (st) {
-        st->flops = sum_i64(ws, ctx, P.flop, nb);
+        st->flops = sum_i64(ws, ctx, P.a().flop, nb);
         st->nnz = nnzc;
         st->overflow_cols = 0;
         st->alloc_entries = nnzc;
@@ -962,17 +1026,17 @@ static int spgemm_phased(Context *ctx, const DevMatrix &A, const DevMatrix &B, i
     cudaEventRecord(ctx->ev[0], s);
     Plan P;
     GBC_TRY(plan_build(ws, A, B, P));
-    const int64_t nb = P.nb;
+    const int64_t nb = B.nzc;
     int64_t *cnt = nullptr;
     GBC_TRY(ws.alloc_n(&cnt, nb + 1));
     Lists L;
-    GBC_TRY(plan_classify(P, s, 0, nb, L, cnt));
+    GBC_TRY(plan_classify(P, s, -1, 0, -1, L, cnt));
     cudaEventRecord(ctx->ev[1], s);
     GBC_TRY(run_symbolic(ctx, P, L, cnt));
     cudaEventRecord(ctx->ev[2], s);
     std::vector<int64_t> hcnt(nb > 0 ? nb : 1);
     if (nb > 0) GBC_CUDA_TRY(cudaMemcpyAsync(hcnt.data(), cnt, nb * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    const int64_t flops = sum_i64(ws, ctx, P.flop, nb);
+    const int64_t flops = sum_i64(ws, ctx, P.a().flop, nb);
     // phase boundaries (greedy; a column bigger than the budget is alone)
     std::vector<int64_t> bounds{0};
     int64_t acc = 0, maxp = 0, total = 0;
@@ -1003,10 +1067,10 @@ static int spgemm_phased(Context *ctx, const DevMatrix &A, const DevMatrix &B, i
     for (int p = 0; p < np; ++p) {
         const int64_t j0 = bounds[p], j1 = bounds[p + 1];
         Lists Lp;
-        GBC_TRY(plan_classify(P, s, j0, j1, Lp, nullptr));
+        GBC_TRY(plan_classify(P, s, 0, j0, j1, Lp, nullptr));
         GBC_TRY(exclusive_scan_i64(ws, cnt + j0, ccp, j1 - j0, s));
         cudaEventRecord(ctx->ev[5], s);
-        GBC_TRY(run_numeric<SR>(ctx, P, Lp, A.num, B.num, ccp, j0, nullptr, nullptr, nullptr, ir, num));
+        GBC_TRY(run_numeric<SR>(ctx, P, Lp, ccp, j0, nullptr, nullptr, nullptr, ir, num));
         cudaEventRecord(ctx->ev[6], s);
         int64_t pn = 0;
         for (int64_t j = j0; j < j1; ++j) pn += hcnt[j];
@@ -1025,7 +1089,7 @@ static int spgemm_phased(Context *ctx, const DevMatrix &A, const DevMatrix &B, i
         GBC_CUDA_TRY(cudaMemcpyAsync(hr.data(), rsum, (size_t)csb * np * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
         GBC_CUDA_TRY(cudaMemcpyAsync(hv.data(), vsum, (size_t)csb * np * sizeof(double), cudaMemcpyDeviceToHost, s));
     }
-    GBC_TRY(check_err(ctx, P.a));
+    GBC_TRY(check_err(ctx, P));
     if (st) {
         float t04 = 0, t12 = 0;
         cudaEventElapsedTime(&t04, ctx->ev[0], ctx->ev[4]);
@@ -1053,7 +1117,7 @@ static int spgemm_phased(Context *ctx, const DevMatrix &A, const DevMatrix &B, i
 // Per-column features of the sizing MLP: log2(1+x) of nnz(B(:,j)), flop,
 // the largest and the spread (standard deviation) of the referenced A
 // column lengths, the number of row tiles touched, and the row count.
-__global__ void k_features(SpgemmArgs a, int64_t nb, const uint64_t *tmask, float *feat)
+__global__ void k_features(SpgemmArgs a, int64_t nb, float *feat)
 {
     const int lane = threadIdx.x & 31;
     const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
@@ -1069,7 +1133,7 @@ __global__ void k_features(SpgemmArgs a, int64_t nb, const uint64_t *tmask, floa
             mx = fmax(mx, len);
         }
         int tiles = 0;
-        for (int w = lane; w < a.mask_words; w += 32) tiles += __popcll(tmask[i * a.mask_words + w]);
+        for (int w = lane; w < a.mask_words; w += 32) tiles += __popcll(a.tmask[i * a.mask_words + w]);
 #pragma unroll
         for (int o = 16; o; o >>= 1) {
             sum += __shfl_xor_sync(0xffffffffu, sum, o);
@@ -1107,30 +1171,6 @@ __global__ void k_capacity(int64_t nb, const int64_t *flop, const float *pred, f
     if (c < 1) c = 1;
     const int64_t hi = f < m ? f : m;
     cap[i] = c > hi ? hi : c;
-}
-
-// Stored columns flagged in `flag`, split by flop class like k_classify.
-__global__ void k_classify_flagged(const int64_t *flop, int64_t nb, const int32_t *flag, int32_t *l1, int32_t *l2,
-                                   int32_t *lb, unsigned long long *counts)
-{
-    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31;
-    int cls = -1;
-    if (i < nb && flag[i]) {
-        const int64_t f = flop[i];
-        cls = f <= kSmall1 ? 0 : (f <= kSmall2 ? 1 : 2);
-    }
-    int32_t *lists[3] = {l1, l2, lb};
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const unsigned m = __ballot_sync(0xffffffffu, cls == c);
-        if (!m) continue;
-        const int leader = __ffs(m) - 1;
-        unsigned long long base = 0;
-        if (lane == leader) base = atomicAdd(&counts[c], (unsigned long long)__popc(m));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if (cls == c) lists[c][base + __popc(m & ((1u << lane) - 1))] = (int32_t)i;
-    }
 }
 
 __global__ void k_masked_counts(int64_t nb, const int32_t *flag, const int64_t *cnt, int64_t *out)
@@ -1189,10 +1229,10 @@ static int learned_into_slots(Context *ctx, Workspace &ws, const DevMatrix &A, c
     if (!mlp || !mlp->trained)
         return fail(GBC_EINVAL, "learned sizing needs a trained model (gbc_context_set_mlp)");
     GBC_TRY(plan_build(ws, A, B, P));
-    const int64_t nb = P.nb;
+    const int64_t nb = B.nzc;
     O.nb = nb;
     Lists L;
-    GBC_TRY(plan_classify(P, s, 0, nb, L, nullptr));
+    GBC_TRY(plan_classify(P, s, -1, 0, -1, L, nullptr));
     float *feat = nullptr, *pred = nullptr;
     GBC_TRY(ws.alloc_n(&feat, (size_t)nb * kNF + 1));
     GBC_TRY(ws.alloc_n(&pred, nb + 1));
@@ -1205,10 +1245,10 @@ static int learned_into_slots(Context *ctx, Workspace &ws, const DevMatrix &A, c
     GBC_CUDA_TRY(cudaMemsetAsync(O.cnt, 0, (nb + 1) * sizeof(int64_t), s));
     cudaEventRecord(ctx->ev[5], s);
     if (nb > 0) {
-        k_features<<<grid_for(ctx, (nb + 7) / 8, 8), 256, 0, s>>>(P.a, nb, P.tmask, feat);
+        k_features<<<grid_for(ctx, (nb + 7) / 8, 8), 256, 0, s>>>(P.a(), nb, feat);
         note_launch();
         GBC_TRY(mlp_predict_device(mlp, feat, nb, pred, s));
-        k_capacity<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(nb, P.flop, pred, mlp->margin, A.nrow, cap);
+        k_capacity<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(nb, P.a().flop, pred, mlp->margin, A.nrow, cap);
         note_launch();
     }
     GBC_TRY(exclusive_scan_i64(ws, cap, O.beg0, nb, s));
@@ -1216,19 +1256,11 @@ static int learned_into_slots(Context *ctx, Workspace &ws, const DevMatrix &A, c
     cudaEventRecord(ctx->ev[6], s);
     GBC_TRY(ws.alloc_n(&O.ir0, O.alloc + 1));
     GBC_TRY(ws.alloc(&O.v0, (O.alloc + 1) * sizeof(V)));
-    GBC_TRY(run_numeric<SR>(ctx, P, L, A.num, B.num, O.beg0, 0, cap, O.cnt, O.flag, O.ir0, O.v0));
+    GBC_TRY(run_numeric<SR>(ctx, P, L, O.beg0, 0, cap, O.cnt, O.flag, O.ir0, O.v0));
     cudaEventRecord(ctx->ev[7], s);
     // columns that overflowed their capacity: exact symbolic + numeric
     Lists Lo;
-    GBC_CUDA_TRY(cudaMemsetAsync(P.lcnt, 0, 4 * sizeof(unsigned long long), s));
-    int32_t *l0 = P.lbuf, *l1 = P.lbuf + nb + 1, *l2 = P.lbuf + 2 * (nb + 1);
-    if (nb > 0) {
-        k_classify_flagged<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(P.flop, nb, O.flag, l0, l1, l2, P.lcnt);
-        note_launch();
-    }
-    unsigned long long h[4];
-    GBC_CUDA_TRY(cudaMemcpyAsync(h, P.lcnt, sizeof(h), cudaMemcpyDeviceToHost, s));
-    GBC_CUDA_TRY(cudaStreamSynchronize(s));
+    GBC_TRY(plan_classify(P, s, -1, 0, -1, Lo, nullptr, O.flag));
     {
         float ms = 0;
         cudaEventElapsedTime(&ms, ctx->ev[5], ctx->ev[6]);
@@ -1236,10 +1268,6 @@ static int learned_into_slots(Context *ctx, Workspace &ws, const DevMatrix &A, c
         cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]);
         O.ms_numeric = ms;
     }
-    Lo.l[0] = l0;
-    Lo.l[1] = l1;
-    Lo.l[2] = l2;
-    for (int c = 0; c < 3; ++c) Lo.n[c] = (int64_t)h[c];
     O.overflow_cols = Lo.n[0] + Lo.n[1] + Lo.n[2];
     GBC_TRY(ws.alloc_n(&O.beg1, nb + 1));
     if (O.overflow_cols > 0) {
@@ -1255,7 +1283,7 @@ static int learned_into_slots(Context *ctx, Workspace &ws, const DevMatrix &A, c
         GBC_TRY(read_i64(ctx, O.beg1 + nb, &tot));
         GBC_TRY(ws.alloc_n(&O.ir1, tot + 1));
         GBC_TRY(ws.alloc(&O.v1, (tot + 1) * sizeof(V)));
-        GBC_TRY(run_numeric<SR>(ctx, P, Lo, A.num, B.num, O.beg1, 0, nullptr, nullptr, nullptr, O.ir1, O.v1));
+        GBC_TRY(run_numeric<SR>(ctx, P, Lo, O.beg1, 0, nullptr, nullptr, nullptr, O.ir1, O.v1));
         k_final_counts<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(nb, O.flag, exact, O.cnt);
         note_launch();
         cudaEventRecord(ctx->ev[6], s);
@@ -1268,8 +1296,8 @@ static int learned_into_slots(Context *ctx, Workspace &ws, const DevMatrix &A, c
         O.v1 = O.v0;
         GBC_CUDA_TRY(cudaMemsetAsync(O.beg1, 0, (nb + 1) * sizeof(int64_t), s));
     }
-    O.flops = sum_i64(ws, ctx, P.flop, nb);
-    return check_err(ctx, P.a);
+    O.flops = sum_i64(ws, ctx, P.a().flop, nb);
+    return check_err(ctx, P);
 }
 
 template <class SR>
@@ -1341,23 +1369,23 @@ int spgemm_features(gbc_context *ctx, const gbc_matrix *Am, const gbc_matrix *Bm
     GBC_TRY(upload(ws, Bm, GBC_F64, &B));
     Plan P;
     GBC_TRY(plan_build(ws, A, B, P));
-    const int64_t nb = P.nb;
+    const int64_t nb = B.nzc;
     float *feat = nullptr;
     GBC_TRY(ws.alloc_n(&feat, (size_t)nb * kNF + 1));
     if (nb > 0) {
-        k_features<<<grid_for(ctx, (nb + 7) / 8, 8), 256, 0, s>>>(P.a, nb, P.tmask, feat);
+        k_features<<<grid_for(ctx, (nb + 7) / 8, 8), 256, 0, s>>>(P.a(), nb, feat);
         note_launch();
     }
     int64_t *cnt = nullptr;
     if (nnz_out) {
         GBC_TRY(ws.alloc_n(&cnt, nb + 1));
         Lists L;
-        GBC_TRY(plan_classify(P, s, 0, nb, L, cnt));
+        GBC_TRY(plan_classify(P, s, -1, 0, -1, L, cnt));
         GBC_TRY(run_symbolic(ctx, P, L, cnt));
     }
     cudaMemcpyKind k = where == GBC_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     if (feat_out && nb) GBC_CUDA_TRY(cudaMemcpyAsync(feat_out, feat, (size_t)nb * kNF * sizeof(float), k, s));
-    if (flop_out && nb) GBC_CUDA_TRY(cudaMemcpyAsync(flop_out, P.flop, nb * sizeof(int64_t), k, s));
+    if (flop_out && nb) GBC_CUDA_TRY(cudaMemcpyAsync(flop_out, P.a().flop, nb * sizeof(int64_t), k, s));
     if (nnz_out && nb) GBC_CUDA_TRY(cudaMemcpyAsync(nnz_out, cnt, nb * sizeof(int64_t), k, s));
     GBC_CUDA_TRY(cudaStreamSynchronize(s));
     return GBC_OK;
@@ -1429,6 +1457,79 @@ int mcl_expand(gbc_context *ctx, const gbc_matrix *Am, float thr, int64_t select
     return GBC_OK;
 }
 
+// ---------------------------------------------------------------- batches
+// Many independent products in one plan: every pass is one launch per
+// column class over all products' columns (work items name the product),
+// and the symbolic + scan + numeric sequence is captured once into a CUDA
+// graph that later runs replay.
+struct Batch {
+    Context *ctx = nullptr;
+    Workspace *ws = nullptr;
+    int sr = 0, vt = 0, np = 0;
+    size_t vsize = 8;
+    Plan P;
+    Lists L;
+    int64_t *cnt = nullptr, *ccp = nullptr, *ir = nullptr, *scan_tmp = nullptr;
+    void *num = nullptr;
+    int64_t nnz = 0;
+    std::vector<int64_t> hccp;   // batch-wide column offsets (host copy)
+    std::vector<int64_t> flops;  // per product
+    std::function<int()> numeric;
+    cudaGraphExec_t exec = nullptr;
+    long long graph_kernels = 0;  // kernels one replay runs
+};
+
+static int batch_passes(Batch &b, bool with_symbolic)
+{
+    cudaStream_t s = b.ctx->stream;
+    if (with_symbolic) {
+        GBC_TRY(run_symbolic(b.ctx, b.P, b.L, b.cnt));
+        GBC_TRY(exclusive_scan_i64_tmp(b.cnt, b.ccp, b.P.total_cols, b.scan_tmp, s));
+    }
+    return b.numeric();
+}
+
+template <class SR>
+static int batch_build(Batch &b, const std::vector<DevMatrix> &A, const std::vector<DevMatrix> &B)
+{
+    Context *ctx = b.ctx;
+    cudaStream_t s = ctx->stream;
+    Workspace &ws = *b.ws;
+    for (int p = 0; p < b.np; ++p) GBC_TRY(plan_add(ws, b.P, A[p], B[p]));
+    GBC_TRY(plan_finalize(ws, b.P));
+    const int64_t tc = b.P.total_cols;
+    GBC_TRY(ws.alloc_n(&b.cnt, tc + 1));
+    GBC_TRY(ws.alloc_n(&b.ccp, tc + 1));
+    GBC_TRY(ws.alloc_n(&b.scan_tmp, scan_tmp_elems(tc) + 1));
+    GBC_TRY(plan_classify(b.P, s, -1, 0, -1, b.L, b.cnt));
+    GBC_TRY(run_symbolic(ctx, b.P, b.L, b.cnt));
+    GBC_TRY(exclusive_scan_i64_tmp(b.cnt, b.ccp, tc, b.scan_tmp, s));
+    GBC_TRY(read_i64(ctx, b.ccp + tc, &b.nnz));
+    GBC_TRY(ws.alloc_n(&b.ir, b.nnz + 1));
+    GBC_TRY(ws.alloc(&b.num, (b.nnz + 1) * sizeof(typename SR::V)));
+    b.numeric = [&b]() { return run_numeric<SR>(b.ctx, b.P, b.L, b.ccp, 0, nullptr, nullptr, nullptr, b.ir, b.num); };
+    GBC_TRY(b.numeric());
+    GBC_TRY(check_err(ctx, b.P));
+    b.hccp.resize(tc + 1);
+    GBC_CUDA_TRY(cudaMemcpyAsync(b.hccp.data(), b.ccp, (tc + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    for (int p = 0; p < b.np; ++p) b.flops.push_back(sum_i64(ws, ctx, b.P.h[p].flop, b.P.h[p].nb));
+    GBC_CUDA_TRY(cudaStreamSynchronize(s));
+    // capture symbolic + scan + numeric of the whole batch
+    cudaGraph_t graph;
+    const long long c0 = launch_count();
+    GBC_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const int rc = batch_passes(b, true);
+    cudaError_t e = cudaStreamEndCapture(s, &graph);
+    b.graph_kernels = launch_count() - c0;
+    note_launches(-b.graph_kernels);  // captured, not run
+    if (rc != GBC_OK) return rc;
+    if (e != cudaSuccess) return fail(GBC_ECUDA, std::string("batch capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&b.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(GBC_ECUDA, std::string("batch graph: ") + cudaGetErrorString(e));
+    return GBC_OK;
+}
+
 template <class SR>
 static int spgemm_entry(gbc_context *ctx, int vt, const gbc_matrix *Am, const gbc_matrix *Bm,
                         const gbc_spgemm_opts *opts, gbc_result **C, gbc_spgemm_stats *st)
@@ -1461,14 +1562,14 @@ int spgemm_colstats(gbc_context *ctx, const gbc_matrix *Am, const gbc_matrix *Bm
     GBC_TRY(upload(ws, Bm, GBC_F64, &B));
     Plan P;
     GBC_TRY(plan_build(ws, A, B, P));
-    int64_t nb = P.nb;
+    int64_t nb = B.nzc;
     int64_t *cnt = nullptr;
     GBC_TRY(ws.alloc_n(&cnt, nb + 1));
     Lists L;
-    GBC_TRY(plan_classify(P, s, 0, nb, L, cnt));
+    GBC_TRY(plan_classify(P, s, -1, 0, -1, L, cnt));
     GBC_TRY(run_symbolic(ctx, P, L, cnt));
     cudaMemcpyKind k = where == GBC_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    if (flop_out && nb) GBC_CUDA_TRY(cudaMemcpyAsync(flop_out, P.flop, nb * sizeof(int64_t), k, s));
+    if (flop_out && nb) GBC_CUDA_TRY(cudaMemcpyAsync(flop_out, P.a().flop, nb * sizeof(int64_t), k, s));
     if (nnz_out && nb) GBC_CUDA_TRY(cudaMemcpyAsync(nnz_out, cnt, nb * sizeof(int64_t), k, s));
     GBC_CUDA_TRY(cudaStreamSynchronize(s));
     return GBC_OK;
@@ -1535,6 +1636,125 @@ int gbc_spgemm_phased(gbc_context *ctx, int sr, int vt, const gbc_matrix *Am, co
     if (sr == GBC_SR_SELECT2NDMIN && vt == GBC_I64)
         return spgemm_phased<Select2ndMin<int64_t>>(ctx, A, B, max_phase_nnz, st);
     return fail(GBC_EUNSUPPORTED, "phased SpGEMM is instantiated for PlusTimes f64/f32 and Select2ndMin i64");
+}
+
+struct gbc_batch : gbc::Batch {};
+
+int gbc_batch_destroy(gbc_batch *b)
+{
+    if (!b) return GBC_OK;
+    cudaSetDevice(b->ctx->device);
+    cudaStreamSynchronize(b->ctx->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    delete b->ws;
+    cudaStreamSynchronize(b->ctx->stream);
+    delete b;
+    return GBC_OK;
+}
+
+int gbc_batch_create(gbc_context *ctx, int sr, int vt, int nprob, const gbc_matrix *A, const gbc_matrix *B,
+                     int64_t s1, int64_t s2, gbc_batch **out)
+{
+    if (!ctx || !A || !B || !out || nprob <= 0) return fail(GBC_EINVAL, "bad argument");
+    *out = nullptr;
+    GBC_CUDA_TRY(cudaSetDevice(ctx->device));
+    gbc_batch *b = new gbc_batch();
+    b->ctx = ctx;
+    b->ws = new Workspace(ctx);
+    b->sr = sr;
+    b->vt = vt;
+    b->np = nprob;
+    b->vsize = value_size(vt);
+    b->P.s1 = s1 >= 0 ? std::min<int64_t>(s1, kSmall1) : kSmall1;
+    b->P.s2 = s2 >= 0 ? std::min<int64_t>(std::max(s2, b->P.s1), kSmall2) : kSmall2;
+    std::vector<DevMatrix> dA(nprob), dB(nprob);
+    int rc = GBC_OK;
+    for (int p = 0; p < nprob && rc == GBC_OK; ++p) {
+        if (A[p].ncol != B[p].nrow) rc = fail(GBC_EINVAL, "inner dimensions do not match in a batch product");
+        if (rc == GBC_OK) rc = upload(*b->ws, &A[p], vt, &dA[p]);
+        if (rc == GBC_OK) rc = upload(*b->ws, &B[p], vt, &dB[p]);
+    }
+    if (rc == GBC_OK) {
+        if (sr == GBC_SR_PLUSTIMES && vt == GBC_F64)
+            rc = batch_build<PlusTimes<double>>(*b, dA, dB);
+        else if (sr == GBC_SR_PLUSTIMES && vt == GBC_F32)
+            rc = batch_build<PlusTimes<float>>(*b, dA, dB);
+        else if (sr == GBC_SR_SELECT2NDMIN && vt == GBC_I64)
+            rc = batch_build<Select2ndMin<int64_t>>(*b, dA, dB);
+        else if ((sr == GBC_SR_BOOL || sr == GBC_SR_PLUSTIMES) && vt == GBC_BOOL)
+            rc = batch_build<BoolOrAnd>(*b, dA, dB);
+        else
+            rc = fail(GBC_EUNSUPPORTED, "batched SpGEMM: semiring/type not instantiated");
+    }
+    if (rc != GBC_OK) {
+        std::string msg = gbc_last_error();
+        gbc_batch_destroy(b);
+        return fail(rc, msg);
+    }
+    *out = b;
+    return GBC_OK;
+}
+
+// Replay the whole batch (symbolic, scan, numeric of every product) as one
+// CUDA graph launch; *ms = device time.
+int gbc_batch_run(gbc_batch *b, double *ms)
+{
+    if (!b) return fail(GBC_EINVAL, "null batch");
+    GBC_CUDA_TRY(cudaSetDevice(b->ctx->device));
+    cudaStream_t s = b->ctx->stream;
+    cudaEventRecord(b->ctx->ev[0], s);
+    GBC_CUDA_TRY(cudaGraphLaunch(b->exec, s));
+    note_launches(b->graph_kernels);
+    cudaEventRecord(b->ctx->ev[1], s);
+    GBC_CUDA_TRY(cudaEventSynchronize(b->ctx->ev[1]));
+    GBC_TRY(check_err(b->ctx, b->P));
+    if (ms) {
+        float t = 0;
+        cudaEventElapsedTime(&t, b->ctx->ev[0], b->ctx->ev[1]);
+        *ms = t;
+    }
+    return GBC_OK;
+}
+
+int gbc_batch_info(const gbc_batch *b, int p, int64_t *nzc, int64_t *nnz, int64_t *flops)
+{
+    if (!b || p < 0 || p >= b->np) return fail(GBC_EINVAL, "bad batch index");
+    const SpgemmArgs &a = b->P.h[p];
+    if (nzc) *nzc = a.nb;
+    if (nnz) *nnz = b->hccp[a.col_base + a.nb] - b->hccp[a.col_base];
+    if (flops) *flops = b->flops[p];
+    return GBC_OK;
+}
+
+__global__ void k_rebase(int64_t n, const int64_t *src, int64_t base, int64_t *dst)
+{
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i <= n) dst[i] = src[i] - base;
+}
+
+// Product p of the batch: cp[nzc+1] (one column per stored column of its B),
+// ir[nnz], num[nnz], in host or device memory.
+int gbc_batch_result(const gbc_batch *b, int p, int64_t *cp, int64_t *ir, void *num, int where)
+{
+    if (!b || p < 0 || p >= b->np) return fail(GBC_EINVAL, "bad batch index");
+    GBC_CUDA_TRY(cudaSetDevice(b->ctx->device));
+    cudaStream_t s = b->ctx->stream;
+    const SpgemmArgs &a = b->P.h[p];
+    const int64_t base = b->hccp[a.col_base], n = b->hccp[a.col_base + a.nb] - base;
+    cudaMemcpyKind k = where == GBC_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (cp) {
+        if (where == GBC_DEVICE) {
+            k_rebase<<<(unsigned)((a.nb + 256) / 256), 256, 0, s>>>(a.nb, b->ccp + a.col_base, base, cp);
+            note_launch();
+        } else {
+            for (int64_t j = 0; j <= a.nb; ++j) cp[j] = b->hccp[a.col_base + j] - base;
+        }
+    }
+    if (ir && n) GBC_CUDA_TRY(cudaMemcpyAsync(ir, b->ir + base, n * sizeof(int64_t), k, s));
+    if (num && n)
+        GBC_CUDA_TRY(cudaMemcpyAsync(num, static_cast<const char *>(b->num) + base * b->vsize, n * b->vsize, k, s));
+    GBC_CUDA_TRY(cudaStreamSynchronize(s));
+    return GBC_OK;
 }
 
 int gbc_spgemm_features(gbc_context *ctx, const gbc_matrix *A, const gbc_matrix *B, float *feat, int64_t *flop,

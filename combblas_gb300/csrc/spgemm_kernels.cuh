@@ -31,8 +31,17 @@ struct SpgemmArgs {
     const int32_t *brow;
     const int64_t *flop;
     int32_t *err;
-    int64_t col_begin, col_end;  // numeric pass: stored columns [col_begin, col_end) of B
+    int64_t col_begin, col_end;  // stored columns [col_begin, col_end) of B
+    const void *aval, *bval;     // values of A and B (nullptr: all ones)
+    const uint64_t *tmask;       // [nb][mask_words] row tiles each output column touches
+    int64_t col_base;            // this product's first column in batch-wide per-column arrays
+    int key_bits;                // bits needed for a row id
 };
+
+// A work item names one output column of one product of a batch.
+__host__ __device__ __forceinline__ int64_t make_item(int pid, int64_t col) { return ((int64_t)pid << 32) | col; }
+__host__ __device__ __forceinline__ int item_pid(int64_t it) { return (int)(it >> 32); }
+__host__ __device__ __forceinline__ int64_t item_col(int64_t it) { return it & 0xffffffffll; }
 
 // Block-wide exclusive sum (kThreads threads); *total gets the block total.
 __device__ __forceinline__ int64_t block_exclusive_sum64(int64_t v, int64_t *total)

@@ -69,14 +69,15 @@ __device__ __forceinline__ void warp_products(const SpgemmArgs &a, int64_t bs, i
 
 // Warp hash count of distinct rows; table of TS slots per warp.
 template <int TS, int WPB>
-__global__ void __launch_bounds__(WPB * 32) k_small_count(SpgemmArgs a, const int32_t *cols, int64_t ncols,
+__global__ void __launch_bounds__(WPB * 32) k_small_count(const SpgemmArgs *args, const int64_t *items, int64_t ncols,
                                                           int64_t *cnt)
 {
     extern __shared__ int32_t tabs[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int32_t *t = tabs + (size_t)w * TS;
     for (int64_t ci = int64_t(blockIdx.x) * WPB + w; ci < ncols; ci += int64_t(gridDim.x) * WPB) {
-        const int32_t i = cols[ci];
+        const SpgemmArgs &a = args[item_pid(items[ci])];
+        const int64_t i = item_col(items[ci]);
         for (int s = lane; s < TS; s += 32) t[s] = -1;
         __syncwarp();
         int mine = 0;
@@ -96,7 +97,7 @@ __global__ void __launch_bounds__(WPB * 32) k_small_count(SpgemmArgs a, const in
         });
 #pragma unroll
         for (int o = 16; o; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
-        if (lane == 0) cnt[i] = mine;
+        if (lane == 0) cnt[a.col_base + i] = mine;
         __syncwarp();
     }
 }
@@ -181,11 +182,10 @@ __device__ __forceinline__ int warp_gather(const SpgemmArgs &a, const typename S
 // position in their low 12 bits and values stay in place; otherwise values
 // move with the keys.
 template <class SR, int FS, int WPB, bool PACK>
-__global__ void __launch_bounds__(WPB * 32) k_small_numeric(SpgemmArgs a, const void *aval_v, const void *bval_v,
-                                                            const int32_t *cols, int64_t ncols, const int64_t *ccp,
-                                                            int64_t ccp_base, const int64_t *cap, int64_t *out_cnt,
-                                                            int32_t *overflow, int64_t *cir, void *cval_v,
-                                                            int key_bits)
+__global__ void __launch_bounds__(WPB * 32) k_small_numeric(const SpgemmArgs *args, const int64_t *items,
+                                                            int64_t ncols, const int64_t *ccp, int64_t ccp_base,
+                                                            const int64_t *cap, int64_t *out_cnt, int32_t *overflow,
+                                                            int64_t *cir, void *cval_v)
 {
     typedef typename SR::V V;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -198,13 +198,16 @@ __global__ void __launch_bounds__(WPB * 32) k_small_numeric(SpgemmArgs a, const 
     uint32_t *keys0 = reinterpret_cast<uint32_t *>(vals0 + (PACK ? FS : 2 * FS));
     uint32_t *keys1 = keys0 + FS;
     int32_t *hist = reinterpret_cast<int32_t *>(keys1 + FS);
-    const V *aval = static_cast<const V *>(aval_v);
-    const V *bval = static_cast<const V *>(bval_v);
     V *cval = static_cast<V *>(cval_v);
     const int shift0 = PACK ? 12 : 0;
 
     for (int64_t ci = int64_t(blockIdx.x) * WPB + w; ci < ncols; ci += int64_t(gridDim.x) * WPB) {
-        const int32_t i = cols[ci];
+        const SpgemmArgs &a = args[item_pid(items[ci])];
+        const int64_t i = item_col(items[ci]);
+        const int64_t g = a.col_base + i;
+        const int key_bits = a.key_bits;
+        const V *aval = static_cast<const V *>(a.aval);
+        const V *bval = static_cast<const V *>(a.bval);
         // 1. gather products in k-major order
         const int n = warp_gather<SR, PACK>(a, aval, bval, a.bcp[i], a.bcp[i + 1], keys0, vals0, FS);
         if (n > FS) {  // the column was binned by its flop count, so this cannot happen
@@ -266,8 +269,8 @@ __global__ void __launch_bounds__(WPB * 32) k_small_numeric(SpgemmArgs a, const 
             }
         }
         // 3. fold runs of equal rows in order and write them
-        const int64_t out0 = ccp[i - ccp_base];
-        const int64_t room = cap ? cap[i] : (ccp[i - ccp_base + 1] - out0);
+        const int64_t out0 = ccp[g - ccp_base];
+        const int64_t room = cap ? cap[g] : (ccp[g - ccp_base + 1] - out0);
         int64_t heads = 0;  // output entries before this chunk
         bool over = false;
         for (int p0 = 0; p0 < n; p0 += 32) {
@@ -296,10 +299,10 @@ __global__ void __launch_bounds__(WPB * 32) k_small_numeric(SpgemmArgs a, const 
         }
         over = __any_sync(0xffffffffu, over);
         if (lane == 0) {
-            if (out_cnt) out_cnt[i] = heads;
+            if (out_cnt) out_cnt[g] = heads;
             if (over) {
                 if (overflow)
-                    overflow[i] = 1;
+                    overflow[g] = 1;
                 else
                     atomicOr(a.err, 128);
             }

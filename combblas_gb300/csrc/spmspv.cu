@@ -39,6 +39,7 @@ struct Graph {
     int64_t *ctl = nullptr;  // device control block (see CTL_*)
     int64_t *h_ctl = nullptr;  // pinned mirror
     cudaGraphExec_t level_exec = nullptr;
+    long long level_kernels = 0;  // kernels one replay of the level graph runs
     int64_t *g_parents = nullptr, *g_levels = nullptr;  // pointers baked into the graph
     bool bfs_ready = false;
 };
@@ -381,6 +382,7 @@ static int level_graph(Graph *g, int64_t *parents, int64_t *levels)
     cudaStream_t cs;
     GBC_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     cudaGraph_t graph;
+    const long long c0 = launch_count();
     cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) {
         cudaStreamDestroy(cs);
@@ -388,6 +390,8 @@ static int level_graph(Graph *g, int64_t *parents, int64_t *levels)
     }
     int rc = launch_level(g, parents, levels, cs);
     e = cudaStreamEndCapture(cs, &graph);
+    g->level_kernels = launch_count() - c0;
+    note_launches(-g->level_kernels);  // captured, not run
     cudaStreamDestroy(cs);
     if (rc != GBC_OK) return rc;
     if (e != cudaSuccess) return fail(GBC_ECUDA, std::string("capture end: ") + cudaGetErrorString(e));
@@ -422,6 +426,7 @@ static int bfs_device(Graph *g, int64_t source, int64_t *parents, int64_t *level
         for (int k = 0; k < batch; ++k) {
             if (use_graph) {
                 GBC_CUDA_TRY(cudaGraphLaunch(g->level_exec, s));
+                note_launches(g->level_kernels);
             } else {
                 GBC_TRY(launch_level(g, parents, levels, s));
             }

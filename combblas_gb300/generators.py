@@ -152,35 +152,35 @@ def mcl_planted(n: int = 1 << 20, cluster: int = 1024, intra_nnz: float = 24.0, 
 
 
 def poisson27(side: int, dtype=np.float64) -> CSC:
-    """27-point stencil on a side^3 grid: diagonal 26, each neighbour -1."""
+    """27-point stencil on a side^3 grid: diagonal 26, each neighbour -1.
+    Built directly in column order: neighbour offsets taken in (dz, dy, dx)
+    lexicographic order are ascending row ids."""
     n = side ** 3
     idx = np.arange(n, dtype=np.int64)
     x = idx % side
     y = (idx // side) % side
     z = idx // (side * side)
-    rows, cols, vals = [], [], []
+    rows = np.empty((n, 27), dtype=np.int64)
+    valid = np.empty((n, 27), dtype=bool)
+    vals = np.empty(27, dtype=np.float64)
+    k = 0
     for dz in (-1, 0, 1):
         for dy in (-1, 0, 1):
             for dx in (-1, 0, 1):
                 xx, yy, zz = x + dx, y + dy, z + dz
-                ok = (xx >= 0) & (xx < side) & (yy >= 0) & (yy < side) & (zz >= 0) & (zz < side)
-                nb = (zz * side + yy) * side + xx
-                rows.append(nb[ok])
-                cols.append(idx[ok])
-                vals.append(np.full(int(ok.sum()), 26.0 if (dx, dy, dz) == (0, 0, 0) else -1.0))
-    rows = np.concatenate(rows)
-    cols = np.concatenate(cols)
-    vals = np.concatenate(vals)
-    key = cols * n + rows
-    order = np.argsort(key, kind="stable")
-    M = csc_from_coo(n, n, rows[order], cols[order], vals[order])
-    M.values = M.values.astype(dtype)
-    return M
+                valid[:, k] = (xx >= 0) & (xx < side) & (yy >= 0) & (yy < side) & (zz >= 0) & (zz < side)
+                rows[:, k] = (zz * side + yy) * side + xx
+                vals[k] = 26.0 if (dx, dy, dz) == (0, 0, 0) else -1.0
+                k += 1
+    cnt = valid.sum(1)
+    colptr = np.zeros(n + 1, dtype=np.int64)
+    colptr[1:] = np.cumsum(cnt)
+    return CSC(n, n, colptr, rows[valid], np.broadcast_to(vals, (n, 27))[valid].astype(dtype))
 
 
 def aggregation(side: int, dtype=np.float64) -> CSC:
     """Restriction R (n/8 x n) that sums each 2x2x2 block of a side^3 grid
-    (side even); entries are ones."""
+    (side even); entries are ones.  Column c (a fine point) holds one row."""
     assert side % 2 == 0
     n = side ** 3
     h = side // 2
@@ -189,14 +189,34 @@ def aggregation(side: int, dtype=np.float64) -> CSC:
     y = (idx // side) % side
     z = idx // (side * side)
     agg = ((z // 2) * h + (y // 2)) * h + (x // 2)
-    M = csc_from_coo(h ** 3, n, agg, idx, np.ones(n))
-    M.values = M.values.astype(dtype)
-    return M
+    return CSC(h ** 3, n, np.arange(n + 1, dtype=np.int64), agg, np.ones(n, dtype=dtype))
 
 
 def transpose(M: CSC) -> CSC:
     cols = M.col_ids()
     return csc_from_coo(M.ncol, M.nrow, cols, M.rowidx, M.values, dedupe=False)
+
+
+def batch_c4(nprob: int = 256, seed: int = 4, rmat_scales=(10, 18), sides=(16, 64)):
+    """The uneven batch: half R-MAT products A*A (n log-uniform over
+    2^rmat_scales, edge factor uniform 4..16), half Galerkin triple products
+    R*A*R^T with A a 27-point Poisson stencil on a cube (side uniform over
+    the even values in `sides`) and R its 2x2x2 aggregation.  Returns
+    (rmat_list, galerkin_list) with rmat entries A and galerkin entries
+    (A, R, R^T)."""
+    rng = np.random.default_rng(seed)
+    rm, gk = [], []
+    for q in range(nprob // 2):
+        scale = int(rng.integers(rmat_scales[0], rmat_scales[1] + 1))
+        ef = int(rng.integers(4, 17))
+        rm.append(rmat(scale, ef, seed=seed * 1000 + q))
+    evens = np.arange(sides[0], sides[1] + 1, 2)
+    for q in range(nprob - nprob // 2):
+        side = int(rng.choice(evens))
+        A = poisson27(side)
+        R = aggregation(side)
+        gk.append((A, R, transpose(R)))
+    return rm, gk
 
 
 def random_sparse(m: int, n: int, density: float, seed: int, dtype=np.float64, empty_cols: float = 0.0) -> CSC:

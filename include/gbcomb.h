@@ -165,6 +165,23 @@ int gbc_spgemm_phased(gbc_context *ctx, int sr, int vt, const gbc_matrix *A, con
 int gbc_spgemm_colstats(gbc_context *ctx, const gbc_matrix *A, const gbc_matrix *B, int64_t *flop, int64_t *nnz,
                         int where);
 
+/* ----------------------------------------------------------------- batches */
+/* Many independent products C_p = A_p * B_p (uneven sizes) computed
+ * together: every pass is one launch over the columns of all products, and
+ * the symbolic + scan + numeric passes are captured once into a CUDA graph
+ * that gbc_batch_run replays.  s1/s2 (-1: defaults 256/4096) are the flop
+ * thresholds of the warp-kernel column classes, the knobs the autotuner
+ * picks.  The batch owns copies of host inputs; device inputs must outlive
+ * it.  No counterpart in the reference, which multiplies one pair at a time
+ * (PSpGEMM, SpParMat.h:464). */
+typedef struct gbc_batch gbc_batch;
+int gbc_batch_create(gbc_context *ctx, int sr, int vt, int nprob, const gbc_matrix *A, const gbc_matrix *B,
+                     int64_t s1, int64_t s2, gbc_batch **out);
+int gbc_batch_run(gbc_batch *b, double *ms);
+int gbc_batch_info(const gbc_batch *b, int p, int64_t *nzc, int64_t *nnz, int64_t *flops);
+int gbc_batch_result(const gbc_batch *b, int p, int64_t *cp, int64_t *ir, void *num, int where);
+int gbc_batch_destroy(gbc_batch *b);
+
 /* -------------------------------------------------------- learned sizing */
 /* The sizing model: a 6-32-32-1 MLP that predicts log2(1 + nnz) of each
  * output column from per-column features (no counterpart in the reference,
