@@ -122,6 +122,7 @@ _SIGS.update({
     "gbc_mcl_prune_select_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_float, C.c_int64, C.POINTER(C.c_void_p)]),
     "gbc_graph_create": (C.c_int, [C.c_void_p, C.POINTER(gbc_matrix), C.POINTER(C.c_void_p)]),
     "gbc_graph_destroy": (C.c_int, [C.c_void_p]),
+    "gbc_graph_set_policy": (C.c_int, [C.c_void_p, C.c_int]),
     "gbc_spmspv_select2ndmin_i64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
                                               C.c_void_p, C.POINTER(C.c_int32), C.c_int]),
     "gbc_spmspv_select2ndmin_noalloc": (C.c_int, [C.c_int64, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,

@@ -25,6 +25,10 @@ class Graph:
         self.n = int(A.ncol)
         self.colptr = A.colptr if not isinstance(A, DeviceMatrix) else None
 
+    def set_policy(self, policy: str):
+        """"auto" (per-level direction), "topdown" or "bottomup"."""
+        L.check(L.lib().gbc_graph_set_policy(self.h, {"auto": 0, "topdown": 1, "bottomup": 2}[policy]))
+
     def close(self):
         if self.h:
             L.lib().gbc_graph_destroy(self.h)

@@ -36,16 +36,37 @@ struct Graph {
     int32_t *cand = nullptr;     // [n] candidate parent, kNoCand when untouched
     uint32_t *visited = nullptr;  // [n/32] parents != -1
     int32_t *front[2] = {nullptr, nullptr};
+    uint32_t *fbits[2] = {nullptr, nullptr};  // frontier bitmaps (current / next)
+    int64_t *off = nullptr;                   // [n+1] prefix of frontier degrees
+    int64_t *tile = nullptr;                  // per-tile sums of that prefix
     int64_t *ctl = nullptr;  // device control block (see CTL_*)
     int64_t *h_ctl = nullptr;  // pinned mirror
     cudaGraphExec_t level_exec = nullptr;
     long long level_kernels = 0;  // kernels one replay of the level graph runs
     int64_t *g_parents = nullptr, *g_levels = nullptr;  // pointers baked into the graph
     bool bfs_ready = false;
+    int policy = 0;  // direction policy (see gbc_graph_set_policy)
 };
 
 // control block layout
-enum { CTL_NF = 0, CTL_NNEXT = 1, CTL_ITER = 2, CTL_WORK = 3, CTL_EDGES = 4, CTL_REACHED = 5, CTL_CUR = 6, CTL_N };
+enum {
+    CTL_NF = 0,       // current frontier size
+    CTL_NNEXT = 1,    // next frontier size
+    CTL_ITER = 2,     // level-loop iterations done
+    CTL_WORK = 3,     // work counter of the expand kernels
+    CTL_EDGES = 4,    // sum of degrees of reached vertices
+    CTL_REACHED = 5,  // reached vertices
+    CTL_CUR = 6,      // which frontier buffer is current
+    CTL_FE = 7,       // edges of the current frontier (sum of degrees)
+    CTL_FE_NEXT = 8,  // edges of the next frontier
+    CTL_UE = 9,       // edges of unreached vertices
+    CTL_DIR = 10,     // 0 top-down, 1 bottom-up
+    CTL_E = 11,       // top-down: total frontier edges of this level (scan result)
+    CTL_POLICY = 12,  // 0 choose per level, 1 always top-down, 2 always bottom-up
+    CTL_N
+};
+// frontier pointer table follows the control words
+constexpr int kCtlWords = 16;
 
 __global__ void k_graph_prep(int64_t n, int64_t nnz, const int64_t *cp, const int64_t *ir, uint32_t *cp32,
                              int32_t *row, int32_t *err)
@@ -94,19 +115,6 @@ __device__ __forceinline__ int front_find(const FrontChunk &ch, int j)
             hi = mid;
     }
     return lo;
-}
-
-// Warp-aggregated append of `r` (where `want`) to list[*count].
-__device__ __forceinline__ void warp_append(bool want, int32_t r, int32_t *list, int64_t *count)
-{
-    unsigned m = __ballot_sync(0xffffffffu, want);
-    if (!m) return;
-    int lane = threadIdx.x & 31;
-    int leader = __ffs(m) - 1;
-    unsigned long long base = 0;
-    if (lane == leader) base = atomicAdd((unsigned long long *)count, (unsigned long long)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (want) list[base + __popc(m & ((1u << lane) - 1))] = r;
 }
 
 // --------------------------------------------------------------- SpMSpV
@@ -183,73 +191,190 @@ __global__ void k_mark_emit(uint32_t *mark, int64_t words, const int64_t *pos, u
 }
 
 // ------------------------------------------------------------------- BFS
-// Expand one level: for every column c of the frontier (value c, as after
-// setNumToInd) and every row r of A(:,c) not yet visited, cand[r] = min(c);
-// a row touched for the first time joins the next frontier.  New frontier
-// rows are gathered in a block-local queue and flushed with one global
-// atomic per kQueue entries (a single global counter per warp would
-// serialise on hot levels).
+// Level loop of the reference's BFS over SelectMin (parent = smallest
+// frontier neighbour), run in either direction per level:
+//  * top-down: edge-balanced expansion of the frontier -- frontier degrees
+//    are prefix-summed and every block takes fixed chunks of kEdgeChunk edges,
+//    so hub vertices are shared by many blocks -- with cand[r] = atomicMin of
+//    the frontier ids (EWiseMult(..., exclude) is the visited-bitmap test);
+//  * bottom-up: every unreached vertex scans its neighbours in ascending
+//    order and takes the first one in the frontier bitmap.  Neighbours are
+//    sorted, so that first frontier neighbour IS the minimum, and the result
+//    equals the top-down one bit for bit.
+// The direction is chosen on the device per level (frontier edges against
+// unreached edges, as direction-optimizing BFS does), so one captured graph
+// serves every level.
 constexpr int kQueue = 4096;
+constexpr int kEdgeChunk = 1024;
+constexpr int kScanTile = 2048;
 
-__global__ void __launch_bounds__(kThreads) k_bfs_expand(const uint32_t *cp32, const int32_t *row,
-                                                         const uint32_t *visited, int32_t *cand, int64_t *ctl,
-                                                         int32_t *const *fronts)
+__device__ __forceinline__ void queue_flush(int32_t *q, int &s_qn, unsigned long long &s_gbase, int64_t *ctl,
+                                            int32_t *next)
 {
-    __shared__ FrontChunk ch;
-    __shared__ int64_t s_base;
+    const int tid = threadIdx.x;
+    const int qn = s_qn;
+    if (qn > 0) {
+        if (tid == 0) s_gbase = atomicAdd((unsigned long long *)&ctl[CTL_NNEXT], (unsigned long long)qn);
+        __syncthreads();
+        for (int k = tid; k < qn; k += blockDim.x) next[s_gbase + k] = q[k];
+        __syncthreads();
+        if (tid == 0) s_qn = 0;
+    }
+    __syncthreads();
+}
+
+// Per level: pick the direction (one thread).
+__global__ void k_bfs_direction(int64_t *ctl, int64_t n)
+{
+    const int64_t nf = ctl[CTL_NF];
+    if (nf == 0) return;
+    int64_t dir = ctl[CTL_DIR];
+    if (dir == 0 && ctl[CTL_FE] * 14 > ctl[CTL_UE]) dir = 1;
+    else if (dir == 1 && nf * 24 < n) dir = 0;
+    if (ctl[CTL_POLICY] == 1) dir = 0;
+    if (ctl[CTL_POLICY] == 2) dir = 1;
+    ctl[CTL_DIR] = dir;
+    ctl[CTL_E] = 0;
+}
+
+// Top-down prefix of frontier degrees, in three fixed-size launches so the
+// graph can be replayed for any frontier size: tile sums, tile scan (one
+// block), rescan.
+__global__ void k_bfs_deg_tiles(const uint32_t *cp32, const int64_t *ctl, int32_t *const *fronts, int64_t *tile)
+{
+    if (ctl[CTL_DIR] != 0) return;
+    const int64_t nf = ctl[CTL_NF];
+    const int32_t *front = fronts[ctl[CTL_CUR]];
+    const int64_t b0 = int64_t(blockIdx.x) * kScanTile;
+    if (b0 >= nf) return;
+    int64_t sum = 0;
+    for (int64_t f = b0 + threadIdx.x; f < min(nf, b0 + kScanTile); f += blockDim.x) {
+        const int32_t c = front[f];
+        sum += cp32[c + 1] - cp32[c];
+    }
+    int64_t tot;
+    block_exclusive_sum64(sum, &tot);
+    if (threadIdx.x == 0) tile[blockIdx.x] = tot;
+}
+
+__global__ void k_bfs_deg_scan(int64_t *ctl, int64_t *tile)
+{
+    if (ctl[CTL_DIR] != 0) return;
+    const int64_t nf = ctl[CTL_NF];
+    const int64_t nt = (nf + kScanTile - 1) / kScanTile;
+    int64_t carry = 0;
+    for (int64_t b = 0; b < nt; b += blockDim.x) {
+        const int64_t t = b + threadIdx.x;
+        const int64_t v = t < nt ? tile[t] : 0;
+        int64_t tot;
+        const int64_t ex = block_exclusive_sum64(v, &tot);
+        if (t < nt) tile[t] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) ctl[CTL_E] = carry;
+}
+
+__global__ void k_bfs_deg_rescan(const uint32_t *cp32, const int64_t *ctl, int32_t *const *fronts,
+                                 const int64_t *tile, int64_t *off)
+{
+    if (ctl[CTL_DIR] != 0) return;
+    const int64_t nf = ctl[CTL_NF];
+    const int32_t *front = fronts[ctl[CTL_CUR]];
+    const int64_t b0 = int64_t(blockIdx.x) * kScanTile;
+    if (b0 >= nf) return;
+    constexpr int PER = kScanTile / kThreads;
+    int64_t d[PER], sum = 0;
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+        const int64_t f = b0 + int64_t(threadIdx.x) * PER + u;
+        d[u] = 0;
+        if (f < nf) {
+            const int32_t c = front[f];
+            d[u] = cp32[c + 1] - cp32[c];
+        }
+        sum += d[u];
+    }
+    int64_t tot;
+    int64_t run = tile[blockIdx.x] + block_exclusive_sum64(sum, &tot);
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+        const int64_t f = b0 + int64_t(threadIdx.x) * PER + u;
+        if (f < nf) off[f] = run;
+        run += d[u];
+    }
+    if (b0 + kScanTile >= nf && threadIdx.x == kThreads - 1) off[nf] = run;
+}
+
+// Top-down expansion over fixed edge chunks.
+__global__ void __launch_bounds__(kThreads) k_bfs_td(const uint32_t *cp32, const int32_t *row,
+                                                     const uint32_t *visited, int32_t *cand, int64_t *ctl,
+                                                     int32_t *const *fronts, const int64_t *off)
+{
+    __shared__ int64_t s_off[kEdgeChunk + 2];
+    __shared__ uint32_t s_st[kEdgeChunk + 2];
+    __shared__ int32_t s_c[kEdgeChunk + 2];
+    __shared__ int64_t s_chunk, s_f0;
+    __shared__ int s_k;
     __shared__ int32_t q[kQueue];
     __shared__ int s_qn;
     __shared__ unsigned long long s_gbase;
+    if (ctl[CTL_DIR] != 0) return;
     const int tid = threadIdx.x, lane = tid & 31;
     const int cur = (int)ctl[CTL_CUR];
     const int32_t *front = fronts[cur];
     int32_t *next = fronts[cur ^ 1];
     const int64_t nf = ctl[CTL_NF];
+    const int64_t E = ctl[CTL_E];
     if (tid == 0) s_qn = 0;
     __syncthreads();
-    auto flush = [&]() {
-        // all threads: move the queue to the global frontier
-        const int qn = s_qn;
-        if (qn > 0) {
-            if (tid == 0) s_gbase = atomicAdd((unsigned long long *)&ctl[CTL_NNEXT], (unsigned long long)qn);
-            __syncthreads();
-            for (int k = tid; k < qn; k += kThreads) next[s_gbase + k] = q[k];
-            __syncthreads();
-            if (tid == 0) s_qn = 0;
-        }
-        __syncthreads();
-    };
     for (;;) {
-        if (tid == 0) s_base = (int64_t)atomicAdd((unsigned long long *)&ctl[CTL_WORK], (unsigned long long)kThreads);
-        __syncthreads();
-        const int64_t base = s_base;
-        __syncthreads();
-        if (base >= nf) break;
-        const int64_t f = base + tid;
-        int len = 0;
-        if (f < nf) {
-            const int32_t c = front[f];
-            const uint32_t s = cp32[c];
-            ch.s[tid] = s;
-            ch.val[tid] = c;
-            len = (int)(cp32[c + 1] - s);
+        if (tid == 0) {
+            s_chunk = (int64_t)atomicAdd((unsigned long long *)&ctl[CTL_WORK], 1ull);
+            const int64_t e0 = s_chunk * kEdgeChunk;
+            if (e0 < E) {
+                // first and last frontier entries holding edges of this chunk
+                int64_t lo = 0, hi = nf;  // off[lo] <= e0 < off[hi]
+                while (hi - lo > 1) {
+                    const int64_t mid = (lo + hi) >> 1;
+                    if (off[mid] <= e0) lo = mid; else hi = mid;
+                }
+                const int64_t e1 = min(E, e0 + kEdgeChunk) - 1;
+                int64_t lo2 = lo, hi2 = nf;
+                while (hi2 - lo2 > 1) {
+                    const int64_t mid = (lo2 + hi2) >> 1;
+                    if (off[mid] <= e1) lo2 = mid; else hi2 = mid;
+                }
+                s_f0 = lo;
+                s_k = (int)(lo2 - lo + 1);
+            }
         }
-        int64_t tot;
-        const int off = (int)block_exclusive_sum64(len, &tot);
-        ch.off[tid] = off;
-        if (tid == kThreads - 1) ch.off[kThreads] = off + len;
         __syncthreads();
-        const int iters = ((int)tot + kThreads - 1) / kThreads;
-        for (int it = 0; it < iters; ++it) {
-            const int j = it * kThreads + tid;
+        const int64_t e0 = s_chunk * kEdgeChunk;
+        if (e0 >= E) break;
+        const int K = s_k;
+        const int64_t f0 = s_f0;
+        for (int k = tid; k <= K; k += kThreads) {
+            s_off[k] = off[f0 + k];  // off has nf + 1 entries and f0 + K <= nf
+            if (k < K) {
+                const int32_t c = front[f0 + k];
+                s_c[k] = c;
+                s_st[k] = cp32[c];
+            }
+        }
+        __syncthreads();
+        const int64_t e1 = min(E, e0 + kEdgeChunk);
+        for (int64_t e = e0 + tid; e < e0 + kEdgeChunk; e += kThreads) {
             bool fresh = false;
             int32_t r = 0;
-            if (j < (int)tot) {
-                const int b = front_find(ch, j);
-                r = row[ch.s[b] + (j - ch.off[b])];
+            if (e < e1) {
+                int lo = 0, hi = K;
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (s_off[mid] <= e) lo = mid; else hi = mid;
+                }
+                r = row[s_st[lo] + (e - s_off[lo])];
                 if (!(visited[r >> 5] & (1u << (r & 31)))) {
-                    const int32_t c = (int32_t)ch.val[b];
-                    // skip the atomic when the stored candidate is already smaller
+                    const int32_t c = s_c[lo];
                     if (c < cand[r]) {
                         const int32_t old = atomicMin(&cand[r], c);
                         fresh = old == kNoCand;
@@ -263,31 +388,36 @@ __global__ void __launch_bounds__(kThreads) k_bfs_expand(const uint32_t *cp32, c
                 slot = __shfl_sync(0xffffffffu, slot, __ffs(m) - 1);
                 if (fresh) q[slot + __popc(m & ((1u << lane) - 1))] = r;
             }
-            __syncthreads();
-            if (s_qn > kQueue - kThreads) flush();
         }
         __syncthreads();
+        if (s_qn > kQueue - kEdgeChunk) queue_flush(q, s_qn, s_gbase, ctl, next);
     }
-    flush();
+    queue_flush(q, s_qn, s_gbase, ctl, next);
 }
 
-// parents.Set(fringe) for the new frontier; visited/levels/degree sums.
+// Top-down finalize: parents.Set(fringe) for the new frontier, plus visited,
+// levels, next-frontier bitmap and degree sums.
 __global__ void k_bfs_finalize(int32_t *cand, uint32_t *visited, int64_t *parents, int64_t *levels,
-                               const int64_t *cp, int64_t *ctl, int32_t *const *fronts)
+                               const int64_t *cp, int64_t *ctl, int32_t *const *fronts, uint32_t *const *fbits)
 {
+    if (ctl[CTL_NF] == 0 || ctl[CTL_DIR] != 0) return;
     const int cur = (int)ctl[CTL_CUR];
     const int32_t *next = fronts[cur ^ 1];
+    uint32_t *nbits = fbits[cur ^ 1];
     const int64_t nn = ctl[CTL_NNEXT];
     const int64_t iter = ctl[CTL_ITER] + 1;
-    int64_t deg = 0, reached = 0;
+    int64_t deg = 0, reached = 0, fdeg = 0;
     for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < nn; i += int64_t(gridDim.x) * blockDim.x) {
         const int32_t r = next[i];
         parents[r] = cand[r];
         cand[r] = kNoCand;
         atomicOr(&visited[r >> 5], 1u << (r & 31));
+        atomicOr(&nbits[r >> 5], 1u << (r & 31));
+        const int64_t d = cp[r + 1] - cp[r];
+        fdeg += d;
         if (levels[r] < 0) {
             levels[r] = iter;
-            deg += cp[r + 1] - cp[r];
+            deg += d;
             ++reached;
         }
     }
@@ -295,14 +425,96 @@ __global__ void k_bfs_finalize(int32_t *cand, uint32_t *visited, int64_t *parent
     for (int o = 16; o; o >>= 1) {
         deg += __shfl_xor_sync(0xffffffffu, deg, o);
         reached += __shfl_xor_sync(0xffffffffu, reached, o);
+        fdeg += __shfl_xor_sync(0xffffffffu, fdeg, o);
     }
-    if ((threadIdx.x & 31) == 0 && (deg || reached)) {
+    if ((threadIdx.x & 31) == 0 && (fdeg || reached)) {
         atomicAdd((unsigned long long *)&ctl[CTL_EDGES], (unsigned long long)deg);
         atomicAdd((unsigned long long *)&ctl[CTL_REACHED], (unsigned long long)reached);
+        atomicAdd((unsigned long long *)&ctl[CTL_FE_NEXT], (unsigned long long)fdeg);
     }
 }
 
-// Advance the level: next frontier becomes current.
+// Bottom-up level: every vertex without a parent takes its smallest
+// neighbour that is in the current frontier.
+__global__ void __launch_bounds__(kThreads) k_bfs_bu(const int64_t *cp, const int32_t *row, uint32_t *visited,
+                                                     int64_t *parents, int64_t *levels, int64_t n, int64_t *ctl,
+                                                     int32_t *const *fronts, uint32_t *const *fbits)
+{
+    __shared__ int32_t q[kQueue];
+    __shared__ int s_qn;
+    __shared__ unsigned long long s_gbase;
+    if (ctl[CTL_NF] == 0 || ctl[CTL_DIR] != 1) return;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int cur = (int)ctl[CTL_CUR];
+    int32_t *next = fronts[cur ^ 1];
+    const uint32_t *fb = fbits[cur];
+    uint32_t *nb = fbits[cur ^ 1];
+    const int64_t iter = ctl[CTL_ITER] + 1;
+    if (tid == 0) s_qn = 0;
+    __syncthreads();
+    int64_t deg = 0, reached = 0, fdeg = 0;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t b = int64_t(blockIdx.x) * blockDim.x; b < n; b += stride) {
+        const int64_t v = b + tid;
+        bool fresh = false;
+        if (v < n && !(visited[v >> 5] & (1u << (v & 31)))) {
+            const int64_t s = cp[v], e = cp[v + 1];
+            for (int64_t p = s; p < e; ++p) {
+                const int32_t u = row[p];
+                if (fb[u >> 5] & (1u << (u & 31))) {
+                    parents[v] = u;
+                    fresh = true;
+                    break;
+                }
+            }
+            if (fresh) {
+                atomicOr(&nb[v >> 5], 1u << (v & 31));
+                fdeg += e - s;
+                if (levels[v] < 0) {
+                    levels[v] = iter;
+                    deg += e - s;
+                    ++reached;
+                }
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, fresh);
+        if (m) {
+            int slot = 0;
+            if (lane == __ffs(m) - 1) slot = atomicAdd(&s_qn, __popc(m));
+            slot = __shfl_sync(0xffffffffu, slot, __ffs(m) - 1);
+            if (fresh) q[slot + __popc(m & ((1u << lane) - 1))] = (int32_t)v;
+        }
+        __syncthreads();
+        if (s_qn > kQueue - kThreads) queue_flush(q, s_qn, s_gbase, ctl, next);
+    }
+    queue_flush(q, s_qn, s_gbase, ctl, next);
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        deg += __shfl_xor_sync(0xffffffffu, deg, o);
+        reached += __shfl_xor_sync(0xffffffffu, reached, o);
+        fdeg += __shfl_xor_sync(0xffffffffu, fdeg, o);
+    }
+    if (lane == 0 && (fdeg || reached)) {
+        atomicAdd((unsigned long long *)&ctl[CTL_EDGES], (unsigned long long)deg);
+        atomicAdd((unsigned long long *)&ctl[CTL_REACHED], (unsigned long long)reached);
+        atomicAdd((unsigned long long *)&ctl[CTL_FE_NEXT], (unsigned long long)fdeg);
+    }
+}
+
+// Visited bits of the bottom-up level's new vertices are set after the
+// level, so a vertex found in this level is never taken as a parent in it
+// (only frontier bits are read there).
+__global__ void k_bfs_bu_mark(uint32_t *visited, const int64_t *ctl, int32_t *const *fronts)
+{
+    if (ctl[CTL_NF] == 0 || ctl[CTL_DIR] != 1) return;
+    const int32_t *next = fronts[ctl[CTL_CUR] ^ 1];
+    const int64_t nn = ctl[CTL_NNEXT];
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < nn; i += int64_t(gridDim.x) * blockDim.x)
+        atomicOr(&visited[next[i] >> 5], 1u << (next[i] & 31));
+}
+
+// Advance the level: the next frontier becomes current; the old current
+// frontier bitmap is cleared for reuse.
 __global__ void k_bfs_advance(int64_t *ctl)
 {
     if (ctl[CTL_NF] == 0) return;  // finished: later replays change nothing
@@ -311,62 +523,104 @@ __global__ void k_bfs_advance(int64_t *ctl)
     ctl[CTL_WORK] = 0;
     ctl[CTL_ITER] += 1;
     ctl[CTL_CUR] ^= 1;
+    ctl[CTL_UE] -= ctl[CTL_FE_NEXT];
+    ctl[CTL_FE] = ctl[CTL_FE_NEXT];
+    ctl[CTL_FE_NEXT] = 0;
 }
 
-__global__ void k_bfs_init(int64_t n, int32_t *cand, uint32_t *visited, int64_t *parents, int64_t *levels,
-                           int64_t source, const int64_t *cp, int64_t *ctl, int32_t *const *fronts)
+__global__ void k_bfs_clear_bits(const int64_t *ctl, uint32_t *const *fbits, int64_t words)
 {
-    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    // after advance: clear the bitmap that will collect the next frontier
+    uint32_t *nb = fbits[ctl[CTL_CUR] ^ 1];
+    for (int64_t w = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; w < words; w += int64_t(gridDim.x) * blockDim.x)
+        nb[w] = 0;
+}
+
+__global__ void k_bfs_init(int64_t n, int64_t nnz, int32_t *cand, uint32_t *visited, int64_t *parents,
+                           int64_t *levels, int64_t source, const int64_t *cp, int64_t *ctl, int32_t *const *fronts,
+                           uint32_t *const *fbits)
+{
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
     for (int64_t v = i; v < n; v += stride) {
         cand[v] = kNoCand;
         parents[v] = -1;
         levels[v] = -1;
     }
-    for (int64_t w = i; w < (n + 31) / 32; w += stride) visited[w] = 0;
-    if (i == 0) {
-        fronts[0][0] = (int32_t)source;
-        ctl[CTL_NF] = 1;
-        ctl[CTL_NNEXT] = 0;
-        ctl[CTL_ITER] = 0;
-        ctl[CTL_WORK] = 0;
-        ctl[CTL_EDGES] = cp[source + 1] - cp[source];
-        ctl[CTL_REACHED] = 1;
-        ctl[CTL_CUR] = 0;
+    for (int64_t w = i; w < (n + 31) / 32; w += stride) {
+        visited[w] = 0;
+        fbits[0][w] = 0;
+        fbits[1][w] = 0;
     }
 }
 
-__global__ void k_set_source_level(int64_t *levels, int64_t source) { levels[source] = 0; }
+__global__ void k_bfs_init2(int64_t n, int64_t nnz, int64_t *levels, int64_t source, const int64_t *cp,
+                            int64_t *ctl, int32_t *const *fronts, uint32_t *const *fbits, int policy)
+{
+    ctl[CTL_POLICY] = policy;
+    fronts[0][0] = (int32_t)source;
+    fbits[0][source >> 5] |= 1u << (source & 31);
+    levels[source] = 0;
+    const int64_t ds = cp[source + 1] - cp[source];
+    ctl[CTL_NF] = 1;
+    ctl[CTL_NNEXT] = 0;
+    ctl[CTL_ITER] = 0;
+    ctl[CTL_WORK] = 0;
+    ctl[CTL_EDGES] = ds;
+    ctl[CTL_REACHED] = 1;
+    ctl[CTL_CUR] = 0;
+    ctl[CTL_FE] = ds;
+    ctl[CTL_FE_NEXT] = 0;
+    ctl[CTL_UE] = nnz;  // the source is still unreached for the reference's loop
+    ctl[CTL_DIR] = 0;
+    ctl[CTL_E] = 0;
+}
 
 // -------------------------------------------------------------- host side
 static int graph_alloc_bfs(Graph *g)
 {
     Context *ctx = g->ctx;
     if (g->bfs_ready) return GBC_OK;
+    const int64_t words = (g->n + 31) / 32 + 1;
     GBC_TRY(device_alloc(ctx, (void **)&g->cand, g->n * sizeof(int32_t) + 16));
-    GBC_TRY(device_alloc(ctx, (void **)&g->visited, ((g->n + 31) / 32) * sizeof(uint32_t) + 16));
+    GBC_TRY(device_alloc(ctx, (void **)&g->visited, words * sizeof(uint32_t)));
     GBC_TRY(device_alloc(ctx, (void **)&g->front[0], g->n * sizeof(int32_t) + 16));
     GBC_TRY(device_alloc(ctx, (void **)&g->front[1], g->n * sizeof(int32_t) + 16));
-    GBC_TRY(device_alloc(ctx, (void **)&g->ctl, 16 * sizeof(int64_t)));
-    GBC_CUDA_TRY(cudaMallocHost(&g->h_ctl, 16 * sizeof(int64_t)));
+    GBC_TRY(device_alloc(ctx, (void **)&g->fbits[0], words * sizeof(uint32_t)));
+    GBC_TRY(device_alloc(ctx, (void **)&g->fbits[1], words * sizeof(uint32_t)));
+    GBC_TRY(device_alloc(ctx, (void **)&g->off, (g->n + 2) * sizeof(int64_t)));
+    GBC_TRY(device_alloc(ctx, (void **)&g->tile, ((g->n + kScanTile - 1) / kScanTile + 2) * sizeof(int64_t)));
+    GBC_TRY(device_alloc(ctx, (void **)&g->ctl, (kCtlWords + 8) * sizeof(int64_t)));
+    GBC_CUDA_TRY(cudaMallocHost(&g->h_ctl, (kCtlWords + 8) * sizeof(int64_t)));
+    // pointer tables after the control words: fronts[2], fbits[2]
+    void *tab[4] = {g->front[0], g->front[1], g->fbits[0], g->fbits[1]};
+    GBC_CUDA_TRY(cudaMemcpyAsync(g->ctl + kCtlWords, tab, sizeof(tab), cudaMemcpyHostToDevice, ctx->stream));
     g->bfs_ready = true;
     return GBC_OK;
 }
 
-static int32_t *const *fronts_dev(Graph *g)
-{
-    // the two frontier pointers, stored right after the control block
-    return reinterpret_cast<int32_t *const *>(g->ctl + 8);
-}
+static int32_t *const *fronts_dev(Graph *g) { return reinterpret_cast<int32_t *const *>(g->ctl + kCtlWords); }
+static uint32_t *const *fbits_dev(Graph *g) { return reinterpret_cast<uint32_t *const *>(g->ctl + kCtlWords + 2); }
 
 static int launch_level(Graph *g, int64_t *parents, int64_t *levels, cudaStream_t s)
 {
     Context *ctx = g->ctx;
-    int grid = ctx->num_sms * 4;
-    k_bfs_expand<<<grid, kThreads, 0, s>>>(g->cp32, g->row, g->visited, g->cand, g->ctl, fronts_dev(g)); ::gbc::note_launch();
-    k_bfs_finalize<<<ctx->num_sms * 4, 256, 0, s>>>(g->cand, g->visited, parents, levels, g->cp, g->ctl,
-                                                    fronts_dev(g)); ::gbc::note_launch();
-    k_bfs_advance<<<1, 1, 0, s>>>(g->ctl); ::gbc::note_launch();
+    const int grid = ctx->num_sms * 4;
+    const int64_t words = (g->n + 31) / 32;
+    const unsigned tiles = (unsigned)((g->n + kScanTile - 1) / kScanTile);
+    k_bfs_direction<<<1, 1, 0, s>>>(g->ctl, g->n);
+    k_bfs_deg_tiles<<<tiles, kThreads, 0, s>>>(g->cp32, g->ctl, fronts_dev(g), g->tile);
+    k_bfs_deg_scan<<<1, kThreads, 0, s>>>(g->ctl, g->tile);
+    k_bfs_deg_rescan<<<tiles, kThreads, 0, s>>>(g->cp32, g->ctl, fronts_dev(g), g->tile, g->off);
+    k_bfs_td<<<grid, kThreads, 0, s>>>(g->cp32, g->row, g->visited, g->cand, g->ctl, fronts_dev(g), g->off);
+    k_bfs_finalize<<<grid, 256, 0, s>>>(g->cand, g->visited, parents, levels, g->cp, g->ctl, fronts_dev(g),
+                                        fbits_dev(g));
+    k_bfs_bu<<<grid, kThreads, 0, s>>>(g->cp, g->row, g->visited, parents, levels, g->n, g->ctl, fronts_dev(g),
+                                       fbits_dev(g));
+    k_bfs_bu_mark<<<grid, 256, 0, s>>>(g->visited, g->ctl, fronts_dev(g));
+    k_bfs_advance<<<1, 1, 0, s>>>(g->ctl);
+    k_bfs_clear_bits<<<grid, 256, 0, s>>>(g->ctl, fbits_dev(g), words);
+    note_launches(10);
     GBC_CUDA_TRY(cudaGetLastError());
     return GBC_OK;
 }
@@ -410,13 +664,12 @@ static int bfs_device(Graph *g, int64_t source, int64_t *parents, int64_t *level
     Context *ctx = g->ctx;
     cudaStream_t s = ctx->stream;
     GBC_TRY(graph_alloc_bfs(g));
-    // frontier pointer table lives after the control words
-    int32_t *fp[2] = {g->front[0], g->front[1]};
-    GBC_CUDA_TRY(cudaMemcpyAsync(g->ctl + 8, fp, sizeof(fp), cudaMemcpyHostToDevice, s));
     cudaEventRecord(ctx->ev[5], s);
-    k_bfs_init<<<ctx->num_sms * 4, 256, 0, s>>>(g->n, g->cand, g->visited, parents, levels, source, g->cp, g->ctl,
-                                                fronts_dev(g)); ::gbc::note_launch();
-    k_set_source_level<<<1, 1, 0, s>>>(levels, source); ::gbc::note_launch();
+    k_bfs_init<<<ctx->num_sms * 4, 256, 0, s>>>(g->n, g->nnz, g->cand, g->visited, parents, levels, source, g->cp,
+                                                g->ctl, fronts_dev(g), fbits_dev(g));
+    k_bfs_init2<<<1, 1, 0, s>>>(g->n, g->nnz, levels, source, g->cp, g->ctl, fronts_dev(g), fbits_dev(g),
+                                g->policy);
+    note_launches(2);
     GBC_CUDA_TRY(cudaGetLastError());
     if (use_graph) GBC_TRY(level_graph(g, parents, levels));
     // Levels are replayed in batches; a finished BFS leaves nf == 0 and the
@@ -431,7 +684,7 @@ static int bfs_device(Graph *g, int64_t source, int64_t *parents, int64_t *level
                 GBC_TRY(launch_level(g, parents, levels, s));
             }
         }
-        GBC_CUDA_TRY(cudaMemcpyAsync(g->h_ctl, g->ctl, 8 * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        GBC_CUDA_TRY(cudaMemcpyAsync(g->h_ctl, g->ctl, kCtlWords * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
         GBC_CUDA_TRY(cudaStreamSynchronize(s));
         if (g->h_ctl[CTL_NF] == 0) break;
     }
@@ -440,8 +693,6 @@ static int bfs_device(Graph *g, int64_t source, int64_t *parents, int64_t *level
     if (st) {
         float ms = 0;
         cudaEventElapsedTime(&ms, ctx->ev[5], ctx->ev[6]);
-        // iterations of the reference loop: the last level that produced a
-        // nonempty fringe, plus the final (empty) one
         st->iterations = g->h_ctl[CTL_ITER];
         st->reached = g->h_ctl[CTL_REACHED];
         st->edges = g->h_ctl[CTL_EDGES] / 2;
@@ -513,10 +764,21 @@ int gbc_graph_destroy(gbc_graph *g)
     device_free(c, g->visited);
     device_free(c, g->front[0]);
     device_free(c, g->front[1]);
+    device_free(c, g->fbits[0]);
+    device_free(c, g->fbits[1]);
+    device_free(c, g->off);
+    device_free(c, g->tile);
     device_free(c, g->ctl);
     if (g->h_ctl) cudaFreeHost(g->h_ctl);
     cudaStreamSynchronize(c->stream);
     delete g;
+    return GBC_OK;
+}
+
+int gbc_graph_set_policy(gbc_graph *g, int policy)
+{
+    if (!g || policy < 0 || policy > 2) return fail(GBC_EINVAL, "bad graph or policy");
+    g->policy = policy;
     return GBC_OK;
 }
 

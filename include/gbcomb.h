@@ -241,6 +241,12 @@ typedef struct {
 
 int gbc_graph_create(gbc_context *ctx, const gbc_matrix *A, gbc_graph **g);
 int gbc_graph_destroy(gbc_graph *g);
+/* BFS direction policy: 0 (default) picks top-down or bottom-up per level
+ * from the frontier and unreached edge counts; 1 always top-down (the
+ * reference's SpMSpV formulation); 2 always bottom-up.  All three give the
+ * same parents: a bottom-up step takes each vertex's first neighbour (rows
+ * are ascending) in the frontier, which is the smallest one. */
+int gbc_graph_set_policy(gbc_graph *g, int policy);
 
 /* y = A x over SelectMinSR / Select2ndMinSR (add = min, multiply returns the
  * vector value): replaces SpMXSpV_Bucket<SR>(const Csc&, int32 mA, const

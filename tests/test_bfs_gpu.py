@@ -87,3 +87,26 @@ def test_spmspv_rejects_bad_index(gpu_ctx):
     g = B.Graph(A)
     with pytest.raises(GbcError):
         B.SpMXSpV(g, np.array([A.ncol + 5], np.int32), np.array([1], np.int64))
+
+
+@pytest.mark.parametrize("policy", ["topdown", "bottomup", "auto"])
+def test_bfs_directions_identical(gpu_ctx, oracle_lib, golden, policy):
+    """Top-down, bottom-up and per-level switching give the reference's
+    parents and levels (smallest frontier neighbour) bit for bit."""
+    O = oracle_lib
+    A = G.rmat(15, 16, seed=5, values=None)
+    g = B.Graph(A)
+    g.set_policy(policy)
+    deg = np.diff(A.colptr)
+    for s in np.random.default_rng(2).choice(np.nonzero(deg)[0], 5, replace=False):
+        par, lev, st = B.bfs(g, int(s))
+        epar, elev, eit = O.port_bfs(A, int(s))
+        assert np.array_equal(par, epar) and np.array_equal(lev, elev) and st.iterations == eit
+    for name in ("seven_sym", "torus", "rmat8"):
+        M = golden_matrix(golden, name).with_values(None)
+        gg = B.Graph(M)
+        gg.set_policy(policy)
+        for s in golden[f"bfs/{name}/sources"]:
+            par, lev, st = B.bfs(gg, int(s))
+            assert np.array_equal(par, golden[f"bfs/{name}/{s}/parents"]), (name, s, policy)
+            assert np.array_equal(lev, golden[f"bfs/{name}/{s}/levels"]), (name, s, policy)
