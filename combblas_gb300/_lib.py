@@ -44,7 +44,8 @@ class gbc_matrix(C.Structure):
 
 
 class gbc_spgemm_opts(C.Structure):
-    _fields_ = [("sizing", C.c_int), ("sorted", C.c_int), ("keep_empty", C.c_int), ("reserved", C.c_int)]
+    _fields_ = [("sizing", C.c_int), ("sorted", C.c_int), ("keep_empty", C.c_int), ("tile_rows", C.c_int),
+                ("tiny_limit", C.c_int64), ("small_limit", C.c_int64)]
 
 
 class gbc_spgemm_stats(C.Structure):

@@ -299,17 +299,19 @@ __global__ void __launch_bounds__(kThreads) k_symbolic(const SpgemmArgs *args, c
 //    window spanning segments groups equal rows with __match_any_sync and the
 //    lowest lane folds the group in lane order.  Each output entry is thus
 //    the left fold acc = add(mrhs, acc) over k ascending.
-constexpr int kSub = 4096;
-constexpr int kSubPerThread = kSub / kThreads;
-
 // Inclusive max-scan of seg[0..n) (uint8 segment-start markers, 0 where no
 // segment starts) seeded with `seed`: seg[j] = id of the segment holding j.
+template <int SUB>
 __device__ __forceinline__ void seg_max_scan(uint8_t *seg, int seed)
 {
+    constexpr int kSubPerThread = SUB / kThreads;
     __shared__ int ws[kWarps];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     uint8_t loc[kSubPerThread];
-    *reinterpret_cast<uint4 *>(loc) = *reinterpret_cast<const uint4 *>(seg + tid * kSubPerThread);
+    if constexpr (kSubPerThread == 16)
+        *reinterpret_cast<uint4 *>(loc) = *reinterpret_cast<const uint4 *>(seg + tid * kSubPerThread);
+    else
+        *reinterpret_cast<uint2 *>(loc) = *reinterpret_cast<const uint2 *>(seg + tid * kSubPerThread);
     int run = 0;
 #pragma unroll
     for (int u = 0; u < kSubPerThread; ++u) run = max(run, (int)loc[u]);
@@ -331,17 +333,22 @@ __device__ __forceinline__ void seg_max_scan(uint8_t *seg, int seed)
         cur = max(cur, (int)loc[u]);
         loc[u] = (uint8_t)cur;
     }
-    *reinterpret_cast<uint4 *>(seg + tid * kSubPerThread) = *reinterpret_cast<const uint4 *>(loc);
+    if constexpr (kSubPerThread == 16)
+        *reinterpret_cast<uint4 *>(seg + tid * kSubPerThread) = *reinterpret_cast<const uint4 *>(loc);
+    else
+        *reinterpret_cast<uint2 *>(seg + tid * kSubPerThread) = *reinterpret_cast<const uint2 *>(loc);
     __syncthreads();
 }
 
-template <class SR>
-__global__ void __launch_bounds__(kThreads, 1) k_numeric(const SpgemmArgs *args, const int64_t *items, int64_t nitems,
+template <class SR, int SUB>
+__global__ void __launch_bounds__(kThreads, SUB <= 2048 ? 2 : 1) k_numeric(const SpgemmArgs *args, const int64_t *items, int64_t nitems,
                                                          const int64_t *ccp, int64_t ccp_base, const int64_t *cap,
                                                          int64_t *out_cnt, int32_t *overflow, int64_t *cir,
                                                          void *cval_v, unsigned long long *work)
 {
     typedef typename SR::V V;
+    constexpr int kSub = SUB;
+    constexpr int kSubPerThread = SUB / kThreads;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ ChunkSmem ch;
     __shared__ V ch_bv[kThreads];
@@ -393,11 +400,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_numeric(const SpgemmArgs *args,
                     for (int q = 0; q < L; q += kSub) {
                         const int n = min(kSub, L - q);
                         // 1. segment ids of products q .. q+n-1
-                        *reinterpret_cast<uint4 *>(seg + tid * kSubPerThread) = make_uint4(0, 0, 0, 0);
+                        if constexpr (kSubPerThread == 16)
+                            *reinterpret_cast<uint4 *>(seg + tid * kSubPerThread) = make_uint4(0, 0, 0, 0);
+                        else
+                            *reinterpret_cast<uint2 *>(seg + tid * kSubPerThread) = make_uint2(0, 0);
                         __syncthreads();
                         if (mylen > 0 && myoff >= q && myoff < q + n) seg[myoff - q] = (uint8_t)tid;
                         __syncthreads();
-                        seg_max_scan(seg, chunk_find(ch, q));
+                        seg_max_scan<SUB>(seg, chunk_find(ch, q));
                         // 2. load (round-major, all loads in flight), owner = 32-row stripe mod kWarps
                         int o_[kSubPerThread];
                         V v_[kSubPerThread];
@@ -565,7 +575,8 @@ static int grid_for(Context *c, int64_t work, int per_sm)
     return (int)std::max<int64_t>(1, std::min<int64_t>(g, work));
 }
 
-int prepare_operands(Workspace &ws, const DevMatrix &A, const DevMatrix &B, SpgemmArgs &a, int64_t **acp_out)
+int prepare_operands(Workspace &ws, const DevMatrix &A, const DevMatrix &B, SpgemmArgs &a, int64_t **acp_out,
+                     int tile_rows)
 {
     Context *ctx = ws.ctx;
     cudaStream_t s = ctx->stream;
@@ -573,7 +584,8 @@ int prepare_operands(Workspace &ws, const DevMatrix &A, const DevMatrix &B, Spge
     a.kdim = A.ncol;
     a.n = B.ncol;
     a.nb = B.nzc;
-    a.R = (int)std::min<int64_t>(kTileRows, ((A.nrow + kThreads - 1) / kThreads) * kThreads);
+    const int rows = (tile_rows == 4096 || tile_rows == 8192 || tile_rows == 16384) ? tile_rows : kTileRows;
+    a.R = (int)std::min<int64_t>(rows, ((A.nrow + kThreads - 1) / kThreads) * kThreads);
     if (a.R < kThreads) a.R = kThreads;
     a.T = (int)((A.nrow + a.R - 1) / a.R);
     if (a.T < 1) a.T = 1;
@@ -646,6 +658,7 @@ struct Plan {
     int max_R = 0, max_key_bits = 0;
     size_t max_sym_smem = 0;
     int64_t s1 = kSmall1, s2 = kSmall2;  // flop thresholds of the column classes
+    int tile_rows = 0;                   // accumulator tile height (0: default)
     unsigned long long *work = nullptr;  // kernel work counters
     int64_t *lbuf = nullptr;             // column lists (3 x (total_cols + 1))
     unsigned long long *lcnt = nullptr;  // list lengths
@@ -664,7 +677,7 @@ static int plan_add(Workspace &ws, Plan &P, const DevMatrix &A, const DevMatrix 
     cudaStream_t s = ctx->stream;
     SpgemmArgs a{};
     int64_t *acp = nullptr;
-    GBC_TRY(prepare_operands(ws, A, B, a, &acp));
+    GBC_TRY(prepare_operands(ws, A, B, a, &acp, P.tile_rows));
     const int64_t nb = B.nzc;
     int64_t m1 = A.nrow > 1 ? A.nrow - 1 : 0;
     a.key_bits = 0;
@@ -711,6 +724,13 @@ static int plan_finalize(Workspace &ws, Plan &P)
     GBC_CUDA_TRY(cudaMemcpyAsync(P.d, P.h.data(), P.h.size() * sizeof(SpgemmArgs), cudaMemcpyHostToDevice,
                                  ws.ctx->stream));
     return GBC_OK;
+}
+
+static void plan_options(Plan &P, const gbc_spgemm_opts &opt)
+{
+    P.tile_rows = opt.tile_rows;
+    if (opt.tiny_limit >= 0) P.s1 = std::min<int64_t>(opt.tiny_limit, kSmall1);
+    if (opt.small_limit >= 0) P.s2 = std::min<int64_t>(std::max(opt.small_limit, P.s1), kSmall2);
 }
 
 static int plan_build(Workspace &ws, const DevMatrix &A, const DevMatrix &B, Plan &P)
@@ -844,12 +864,20 @@ static int run_numeric(Context *ctx, Plan &P, const Lists &L, const int64_t *ccp
                                                           overflow, cir, cval)));
     }
     if (L.n[2] > 0) {
-        const size_t num_smem = numeric_smem_bytes(P.max_R, sizeof(V));
-        GBC_TRY(set_smem(k_numeric<SR>, num_smem));
-        int per_sm = std::max(1, (int)(ctx->smem_optin / (num_smem + 12288)));
         GBC_CUDA_TRY(cudaMemsetAsync(P.work + 1, 0, sizeof(unsigned long long), s));
-        k_numeric<SR><<<grid_for(ctx, L.n[2], std::min(per_sm, 8)), kThreads, num_smem, s>>>(
-            P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir, cval, P.work + 1);
+        if (P.max_R > 8192) {
+            const size_t num_smem = numeric_smem_bytes(P.max_R, sizeof(V), 4096);
+            GBC_TRY(set_smem(k_numeric<SR, 4096>, num_smem));
+            int per_sm = std::max(1, (int)(ctx->smem_optin / (num_smem + 12288)));
+            k_numeric<SR, 4096><<<grid_for(ctx, L.n[2], std::min(per_sm, 8)), kThreads, num_smem, s>>>(
+                P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir, cval, P.work + 1);
+        } else {
+            const size_t num_smem = numeric_smem_bytes(P.max_R, sizeof(V), 2048);
+            GBC_TRY(set_smem(k_numeric<SR, 2048>, num_smem));
+            int per_sm = std::max(1, (int)(ctx->smem_optin / (num_smem + 8192)));
+            k_numeric<SR, 2048><<<grid_for(ctx, L.n[2], std::min(per_sm, 8)), kThreads, num_smem, s>>>(
+                P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir, cval, P.work + 1);
+        }
         note_launch();
     }
     GBC_CUDA_TRY(cudaGetLastError());
@@ -925,7 +953,7 @@ static int spgemm_exact(Context *ctx, const DevMatrix &A, const DevMatrix &B, co
     Workspace ws(ctx);
     cudaEventRecord(ctx->ev[0], s);
     Plan P;
-    if (opt.reserved > 0) P.s2 = std::min<int64_t>(kSmall2, opt.reserved);
+    plan_options(P, opt);
     GBC_TRY(plan_build(ws, A, B, P));
     const int64_t nb = B.nzc;
     int64_t *cnt = nullptr, *ccp = nullptr;
@@ -1309,6 +1337,7 @@ int spgemm_learned(Context *ctx, const DevMatrix &A, const DevMatrix &B, const g
     Workspace ws(ctx);
     cudaEventRecord(ctx->ev[0], s);
     Plan P;
+    plan_options(P, opt);
     LearnedOut O;
     GBC_TRY(learned_into_slots<SR>(ctx, ws, A, B, P, O));
     const int64_t nb = O.nb;
@@ -1438,7 +1467,7 @@ int mcl_expand(gbc_context *ctx, const gbc_matrix *Am, float thr, int64_t select
         return GBC_OK;
     }
     gbc_result *C = nullptr;
-    gbc_spgemm_opts opt{GBC_SIZING_EXACT, GBC_SORTED, 1, 0};
+    gbc_spgemm_opts opt{GBC_SIZING_EXACT, GBC_SORTED, 1, 0, -1, -1};
     gbc_spgemm_stats s1{};
     GBC_TRY(spgemm_exact<PlusTimes<float>>(ctx, A, A, opt, GBC_F32, &C, &s1));
     int rc = mcl_select_device2(ctx, C->nrow, C->nzc, nullptr, nullptr, C->cp, C->ir,
@@ -1537,7 +1566,7 @@ static int spgemm_entry(gbc_context *ctx, int vt, const gbc_matrix *Am, const gb
     if (!ctx || !C) return fail(GBC_EINVAL, "null context or output");
     *C = nullptr;
     GBC_CUDA_TRY(cudaSetDevice(ctx->device));
-    gbc_spgemm_opts opt{GBC_SIZING_EXACT, GBC_SORTED, 1, 0};
+    gbc_spgemm_opts opt{GBC_SIZING_EXACT, GBC_SORTED, 1, 0, -1, -1};
     if (opts) opt = *opts;
     if (Am && Bm && Am->ncol != Bm->nrow) return fail(GBC_EINVAL, "inner dimensions do not match");
     Workspace ws(ctx);

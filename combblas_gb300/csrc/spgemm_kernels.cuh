@@ -13,7 +13,7 @@ constexpr int kWarps = kThreads / 32;    // owner warps per block
 constexpr int kBuckets = kWarps;         // one staging bucket per owner warp
 constexpr int kStage = 2048;             // products staged per sub-batch
 constexpr int kRounds = kStage / kThreads;
-constexpr int kTileRows = 16384;         // rows of the dense accumulator tile
+constexpr int kTileRows = 8192;          // default rows of the dense accumulator tile (two blocks per SM at fp64)
 constexpr int kSymRows = 1 << 20;        // rows covered by one symbolic bitmap
 constexpr int kMaxMaskWords = 64;        // tile-mask words per column (64 tiles each)
 
@@ -123,16 +123,17 @@ __device__ __forceinline__ int chunk_find(const ChunkSmem &ch, int j)
     return lo;
 }
 
-inline size_t numeric_smem_bytes(int R, size_t vsize)
+inline size_t numeric_smem_bytes(int R, size_t vsize, int sub)
 {
-    // acc[R] + sval[4096] (values) + bitmap[R/32] + srow[4096] (u16) + seg[4096] (u8)
-    size_t b = (size_t)R * vsize + (size_t)4096 * vsize;
+    // acc[R] + sval[sub] (values) + bitmap[R/32] + srow[sub] (u16) + seg[sub] (u8)
+    size_t b = (size_t)R * vsize + (size_t)sub * vsize;
     b += (size_t)(R / 32) * 4;
-    b += (size_t)4096 * 2 + 4096;
+    b += (size_t)sub * 2 + sub;
     return (b + 15) & ~size_t(15);
 }
 
-int prepare_operands(Workspace &ws, const DevMatrix &A, const DevMatrix &B, SpgemmArgs &a, int64_t **acp_out);
+int prepare_operands(Workspace &ws, const DevMatrix &A, const DevMatrix &B, SpgemmArgs &a, int64_t **acp_out,
+                     int tile_rows = 0);
 
 template <class SR>
 int spgemm_learned(Context *ctx, const DevMatrix &A, const DevMatrix &B, const gbc_spgemm_opts &opt, int vt,

@@ -257,8 +257,11 @@ def _value_dtype(A, B, sr: str):
 
 
 def spgemm(A, B, sr: str = "plustimes", sizing: str = "exact", sorted: bool = True, keep_empty: bool = True,
-           ctx: Context | None = None, dtype=None) -> SpResult:
-    """C = A * B over ``sr`` on the GPU."""
+           ctx: Context | None = None, dtype=None, tile_rows: int = 0, tiny_limit: int = -1,
+           small_limit: int = -1) -> SpResult:
+    """C = A * B over ``sr`` on the GPU.  tile_rows / tiny_limit /
+    small_limit are tuning knobs (see gbc_spgemm_opts); results do not
+    depend on them."""
     ctx = ctx or default_context()
     dt = np.dtype(dtype) if dtype is not None else _value_dtype(A, B, sr)
     vt = VT_OF_DTYPE[dt]
@@ -266,7 +269,7 @@ def spgemm(A, B, sr: str = "plustimes", sizing: str = "exact", sorted: bool = Tr
     ga = as_gbc_matrix(A, keep, dt)
     gb = as_gbc_matrix(B, keep, dt)
     opts = L.gbc_spgemm_opts(L.SIZING_LEARNED if sizing == "learned" else L.SIZING_EXACT, int(bool(sorted)),
-                             int(bool(keep_empty)), 0)
+                             int(bool(keep_empty)), int(tile_rows), int(tiny_limit), int(small_limit))
     out = C.c_void_p()
     st = L.gbc_spgemm_stats()
     L.check(L.lib().gbc_spgemm(ctx.h, SR_CODES[sr], vt, C.byref(ga), C.byref(gb), C.byref(opts), C.byref(out),

@@ -91,6 +91,20 @@ def test_rmat_semirings_vs_port(gpu_ctx, oracle_lib, sr):
     assert_same(cp, rows, vals, pcp, prow, pval, sr, True, f"sr{sr}")
 
 
+@pytest.mark.parametrize("opts", [dict(tile_rows=8192), dict(tile_rows=4096),
+                                  dict(tile_rows=8192, tiny_limit=64, small_limit=1024),
+                                  dict(tiny_limit=0, small_limit=0)])
+@pytest.mark.parametrize("sr", [0, 5])
+def test_tile_and_class_options_vs_port(gpu_ctx, oracle_lib, opts, sr):
+    """Row-tile height and warp-path limits change the schedule, never the
+    result: every option set is bit-exact against the oracle."""
+    O = oracle_lib
+    A = typed(G.rmat(15, 8, seed=5), sr, 7, O)
+    cp, rows, vals = gpu_csc(A, A, sr, **opts)
+    pcp, prow, pval = O.port_spgemm(A, A, sr)
+    assert_same(cp, rows, vals, pcp, prow, pval, sr, True, str(opts))
+
+
 def test_tall_matrix_many_tiles(gpu_ctx, oracle_lib):
     """m > 1M rows: several row tiles and several symbolic bitmaps."""
     O = oracle_lib
