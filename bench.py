@@ -5,12 +5,16 @@ Default workload (the headline): C = A*A on an R-MAT of scale 20, edge
 factor 16 (a,b,c,d = .57,.19,.19,.05, symmetrized, no self-loops, seeded),
 PlusTimes over fp64 with int64 indices, computed in column phases because
 nnz(C) ~ 2.4e10 exceeds device memory; each phase's output is written to
-HBM and reduced to checksums.  Metric: Gmults/s (multiplications as the
-reference's estimateFLOP counts them, divided by time).  The same line also
-carries BFS GTEPS on the same graph (64 seeded roots, SelectMin parents).
+HBM and reduced to checksums.  Phases are sized by the learned sizing
+network (trained, untimed, on another seed's exact counts); the exact
+two-phase path is timed beside it and must produce the same product (nnz,
+row checksum, 64-bit content hash).  Metric: Gmults/s (multiplications as
+the reference's estimateFLOP counts them, divided by time).  The line also
+carries BFS GTEPS on the same graph (64 seeded roots, SelectMin parents) and
+the MCL expansion step (n = 2^20, fp32) exact vs learned.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload spgemm20|bfs20|spgemm14]
+                  [--workload spgemm20|bfs20|spgemm14] [--scale S] [--no-mcl] [--no-cpu]
 
 --impl reference times the CPU implementation of the same path on the host
 cores (the oracle's C restatement of the reference's algorithm, OpenMP over
@@ -190,10 +194,12 @@ def barrier(world):
         dist.barrier()
 
 
-def make_graph(workload):
+def make_graph(workload, scale_override=0):
     from combblas_gb300 import generators as G
 
     scale, ef = (14, 8) if workload == "spgemm14" else (20, 16)
+    if scale_override:
+        scale = scale_override
     t0 = time.perf_counter()
     A = G.rmat(scale, ef, seed=SEED)
     log(f"generated R-MAT scale {scale} ef {ef}: n={A.ncol} nnz={A.nnz} in {time.perf_counter() - t0:.1f}s")
@@ -210,7 +216,7 @@ def bfs_roots(A, k=BFS_ROOTS):
 def run_reference(args, world, rank):
     if rank != 0:
         return
-    A, scale, ef = make_graph(args.workload)
+    A, scale, ef = make_graph(args.workload, args.scale)
     import oracle as O
 
     O.build(quiet=True) if not os.path.exists(O._PORT_SO) else None
@@ -223,13 +229,13 @@ def run_reference(args, world, rank):
             v, desc, threads = cpu_bfs_rate(A, roots[s % len(roots):], budget / 4)
             if s >= args.warmup:
                 steps.append(v)
-        metric, unit = "BFS GTEPS (R-MAT s20 ef16, SelectMin parents)", "GTEPS"
+        metric, unit = metric_name(args.workload, scale, ef), "GTEPS"
     else:
         for s in range(args.warmup + args.steps):
             v, desc, threads = cpu_spgemm_rate(A, budget / 2)
             if s >= args.warmup:
                 steps.append(v)
-        metric, unit = f"SpGEMM Gmults/s (R-MAT s{scale} ef{ef} A*A, PlusTimes fp64)", "Gmults/s"
+        metric, unit = metric_name(args.workload, scale, ef), "Gmults/s"
     val = float(np.median(steps))
     line = {
         "impl": "reference", "metric": metric, "value": val, "unit": unit, "n_gpus": world, "steps": args.steps,
@@ -244,6 +250,188 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def metric_name(workload, scale, ef):
+    if workload == "bfs20":
+        return f"BFS GTEPS (R-MAT s{scale} ef{ef}, 64 roots, SelectMin parents)"
+    return f"SpGEMM Gmults/s (R-MAT s{scale} ef{ef} A*A, PlusTimes fp64, exact output)"
+
+
+def train_sizing_model(ctx, scale, ef, Ad_like=None):
+    """Sizing network trained (untimed) on the exact column counts of
+    another seed's matrix of the same statistics class."""
+    from combblas_gb300 import generators as G
+    from combblas_gb300 import local as LC
+    from combblas_gb300 import sizing as SZ
+
+    t0 = time.perf_counter()
+    At = G.rmat(scale, ef, seed=SEED + 1)
+    Atd = LC.DeviceMatrix.from_host(At)
+    feat, flop, nnz = SZ.features(Atd, Atd, ctx=ctx)
+    m = SZ.SizingModel(ctx)
+    info = m.fit(feat, nnz, steps=300)
+    m.use()
+    info["train_seconds"] = time.perf_counter() - t0
+    info["trained_on"] = f"R-MAT s{scale} ef{ef} seed {SEED + 1} (exact symbolic counts, {info['samples']} columns)"
+    del Atd
+    return m, info
+
+
+def bench_spgemm(args, world, A, Ad, ctx, stream, scale, ef, hbm, peak_kind):
+    """Headline: A*A in column phases with learned phase sizing; the exact
+    two-phase path is timed beside it and must give the same product
+    (nnz, row checksum and 64-bit content hash)."""
+    import torch
+    from combblas_gb300 import _lib
+    from combblas_gb300 import local as LC
+
+    budget = args.phase_nnz
+    model, info = train_sizing_model(ctx, scale, ef)
+
+    def step(sizing):
+        return LC.spgemm_phased(Ad, Ad, max_phase_nnz=budget, ctx=ctx, sizing=sizing)
+
+    def timed(sizing, steps, clocks=None):
+        torch.cuda.synchronize()
+        barrier(world)
+        if clocks:
+            clocks.start()
+        l0 = _lib.lib().gbc_launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        agg = {"sizing": 0.0, "numeric": 0.0, "rerun": 0.0}
+        torch.cuda.nvtx.range_push(f"timed_{sizing}")  # lets ncu --nvtx-include select the timed steps
+        e0.record(stream)
+        for _ in range(steps):
+            st = step(sizing)
+            agg["sizing"] += st.ms_sizing
+            agg["numeric"] += st.ms_numeric
+            agg["rerun"] += st.ms_rerun
+        e1.record(stream)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        ms = max_over_ranks(e0.elapsed_time(e1), world, "cuda")
+        launches = _lib.lib().gbc_launch_count() - l0
+        ck = clocks.stop() if clocks else None
+        return st, ms, launches, {k: v / steps for k, v in agg.items()}, ck
+
+    for _ in range(args.warmup):
+        step("learned")
+    step("exact")
+    st, ms, launches, agg, ck = timed("learned", args.steps, ClockSampler(int(torch.cuda.current_device())))
+    st_x, ms_x, _, agg_x, _ = timed("exact", args.steps)
+    same = (st.nnz, st.row_checksum, st.content_hash) == (st_x.nnz, st_x.row_checksum, st_x.content_hash)
+    if not same:
+        raise SystemExit("learned and exact phased products differ")
+    flops = st.flops
+    value = flops * args.steps * world / (ms * 1e-3) / 1e9
+    ba = bytes_alg(A.nnz, A.ncol, st.nnz)
+    # dominant kernel (k_numeric, one launch set per phase): A and the
+    # phase's B columns read, the phase's C written
+    ba_num = st.phases * (A.nnz * 16 + (A.ncol + 1) * 8) + (A.nnz * 16 + (A.ncol + 1) * 8) + \
+        st.nnz * 16 + (A.ncol + 1) * 8
+    achieved = ba_num / (agg["numeric"] * 1e-3) / 1e9
+    out = {
+        "metric": metric_name(args.workload, scale, ef),
+        "value": value, "unit": "Gmults/s", "ms_per_step": ms / args.steps,
+        "spgemm": {"path": "column phases, learned phase sizing (MLP), overflowing columns re-run exactly",
+                   "flops": flops, "nnz_c": st.nnz, "phases": st.phases, "max_phase_slots": st.max_phase_nnz,
+                   "alloc_over_nnz": st.alloc_nnz / max(st.nnz, 1), "overflow_cols": st.overflow_cols,
+                   "overflow_rate": st.overflow_cols / max(A.ncol, 1),
+                   "ms_sizing": agg["sizing"], "ms_numeric": agg["numeric"], "ms_rerun": agg["rerun"],
+                   "row_checksum": st.row_checksum, "content_hash": f"{st.content_hash:016x}",
+                   "val_checksum": st.val_checksum, "bytes_alg": ba,
+                   "roofline_frac_whole_step": ba / (ms / args.steps * 1e-3) / 1e9 / hbm,
+                   "model": info},
+        "exact_two_phase": {"value": flops * args.steps * world / (ms_x * 1e-3) / 1e9, "unit": "Gmults/s",
+                            "ms_per_step": ms_x / args.steps, "ms_symbolic": agg_x["sizing"],
+                            "ms_numeric": agg_x["numeric"], "phases": st_x.phases,
+                            "identical_output": same, "learned_speedup": ms_x / ms},
+        "roofline": {"bound": "hbm", "kernel": "k_numeric", "achieved": achieved, "peak": hbm,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "traffic_note": "dram bytes per launch: see profiles/"},
+        "gpu_launches": launches,
+        "clocks": ck,
+    }
+    # ---- e2e: host (pinned) buffers through the public C ABI ---------
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+    hcp, hir, hv = pin(A.colptr), pin(A.rowidx), pin(A.values)
+
+    class _H:
+        pass
+
+    Ah = _H()
+    Ah.nrow, Ah.ncol, Ah.colptr, Ah.rowidx, Ah.values = A.nrow, A.ncol, hcp.numpy(), hir.numpy(), hv.numpy()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st_e = LC.spgemm_phased(Ah, Ah, max_phase_nnz=budget, ctx=ctx, sizing="learned")
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, "cuda")
+    h2d = 2 * (hcp.numel() * 8 + hir.numel() * 8 + hv.numel() * 8)
+    d2h = A.ncol * 8 + 3 * 8 * ctx_sms(ctx) * 6 * st_e.phases  # capacities (phase cuts) + checksum partials
+    out["e2e"] = {"value": st_e.flops * args.steps * world / e2e_s / 1e9, "unit": "Gmults/s",
+                  "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                  "path": "gbc_spgemm_phased (learned sizing) with host pinned A and B: H2D inside the call, "
+                          "checksums read back"}
+    assert (st_e.nnz, st_e.content_hash) == (st.nnz, st.content_hash)
+    model.close()
+    return out
+
+
+def ctx_sms(ctx) -> int:
+    import torch
+
+    return torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+
+
+def bench_mcl(ctx):
+    """MCL expansion (n = 2^20, 1024 planted clusters, fp32; prune 1e-4,
+    select 100): exact two-phase sizing vs learned sizing (network trained
+    on another seed), identical output checked."""
+    import torch
+    from combblas_gb300 import generators as G
+    from combblas_gb300 import local as LC
+    from combblas_gb300 import mcl as MCL
+    from combblas_gb300 import sizing as SZ
+
+    n = 1 << 20
+    A = G.mcl_planted(n, 1024, 24.0, 6.0, seed=3)
+    At = G.mcl_planted(n, 1024, 24.0, 6.0, seed=4)
+    Ad = LC.DeviceMatrix.from_host(A, dtype=np.float32)
+    Atd = LC.DeviceMatrix.from_host(At, dtype=np.float32)
+    feat, flop, nnz = SZ.features(Atd, Atd, ctx=ctx)
+    m = SZ.SizingModel(ctx)
+    info = m.fit(feat, nnz, steps=300)
+    m.use()
+    res = {}
+    outs = {}
+    for sizing in ("exact", "learned"):
+        for _ in range(3):
+            R, st = MCL.mcl_expand(Ad, 1e-4, 100, sizing=sizing, ctx=ctx)
+            R.free()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        reps = 5
+        for _ in range(reps):
+            R, st = MCL.mcl_expand(Ad, 1e-4, 100, sizing=sizing, ctx=ctx)
+            if _ < reps - 1:
+                R.free()
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) / reps * 1e3
+        outs[sizing] = R.to_csc()
+        R.free()
+        res[sizing] = {"ms": ms, "gmults_per_s": st.flops / ms / 1e6, "flops": st.flops, "nnz_c": st.nnz,
+                       "ms_symbolic_or_predict": st.ms_symbolic, "ms_numeric": st.ms_numeric,
+                       "overflow_cols": st.overflow_cols, "alloc_entries": st.alloc_entries}
+    same = all(np.array_equal(x, y) for x, y in zip(outs["exact"], outs["learned"]))
+    m.close()
+    return {"workload": "MCL expansion n=2^20, 1024 clusters, ~24 intra + ~6 inter nnz/col, fp32, prune 1e-4, top-100",
+            "exact": res["exact"], "learned": res["learned"], "identical_output": same,
+            "learned_speedup": res["exact"]["ms"] / res["learned"]["ms"],
+            "model": {"loss": info["loss"], "margin": info["margin"], "samples": info["samples"],
+                      "trained_on": "planted-cluster matrix, seed 4"}}
+
+
+
 # ------------------------------------------------------------------- ours
 def run_ours(args, world, rank, local):
     import torch
@@ -253,7 +441,7 @@ def run_ours(args, world, rank, local):
     from combblas_gb300 import bfs as B
     from combblas_gb300 import local as LC
 
-    A, scale, ef = make_graph(args.workload)
+    A, scale, ef = make_graph(args.workload, args.scale)
     ctx = LC.Context(local)
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
@@ -264,120 +452,55 @@ def run_ours(args, world, rank, local):
     result: dict = {}
 
     # ---- SpGEMM, inputs resident in HBM -------------------------------
-    def spgemm_step():
-        return LC.spgemm_phased(Ad, Ad, max_phase_nnz=budget, ctx=ctx)
-
-    if args.workload in ("spgemm20", "spgemm14"):
-        for _ in range(args.warmup):
-            st = spgemm_step()
-        torch.cuda.synchronize()
-        barrier(world)
-        clocks = ClockSampler(local)
-        clocks.start()
-        l0 = _lib.lib().gbc_launch_count()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        sym_ms = num_ms = 0.0
-        torch.cuda.synchronize()
-        e0.record(stream)
-        for _ in range(args.steps):
-            st = spgemm_step()
-            sym_ms += st.ms_symbolic
-            num_ms += st.ms_numeric
-        e1.record(stream)
-        torch.cuda.synchronize()
-        launches = _lib.lib().gbc_launch_count() - l0
-        ms = e0.elapsed_time(e1)
-        ck = clocks.stop()
-        ms = max_over_ranks(ms, world, "cuda")
-        barrier(world)
-        flops = st.flops
-        value = flops * args.steps * world / (ms * 1e-3) / 1e9
-        ba = bytes_alg(A.nnz, A.ncol, st.nnz)
-        # dominant kernel (numeric): algorithmic bytes over its launch time
-        # (A re-read per phase is counted once per phase launch)
-        ba_num = st.phases * (A.nnz * 16 + (A.ncol + 1) * 8) + (A.nnz * 16 + (A.ncol + 1) * 8) + \
-            st.nnz * 16 + (A.ncol + 1) * 8
-        achieved = ba_num / (num_ms / args.steps * 1e-3) / 1e9
-        result.update({
-            "metric": f"SpGEMM Gmults/s (R-MAT s{scale} ef{ef} A*A, PlusTimes fp64, exact two-phase sizing, "
-                      "column phases)",
-            "value": value, "unit": "Gmults/s", "ms_per_step": ms / args.steps,
-            "spgemm": {"flops": flops, "nnz_c": st.nnz, "phases": st.phases, "max_phase_nnz": st.max_phase_nnz,
-                       "ms_symbolic": sym_ms / args.steps, "ms_numeric": num_ms / args.steps,
-                       "row_checksum": st.row_checksum, "val_checksum": st.val_checksum,
-                       "bytes_alg": ba, "roofline_frac_whole_step": ba / (ms / args.steps * 1e-3) / 1e9 / hbm},
-            "roofline": {"bound": "hbm", "kernel": "k_numeric", "achieved": achieved, "peak": hbm,
-                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": None, "traffic_note": "dram bytes per launch: see profiles/"},
-            "gpu_launches": launches,
-            "clocks": ck,
-        })
-        # ---- e2e: host (pinned) buffers through the public C ABI ---------
-        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
-        hcp, hir, hv = pin(A.colptr), pin(A.rowidx), pin(A.values)
-
-        class _H:
-            pass
-
-        Ah = _H()
-        Ah.nrow, Ah.ncol, Ah.colptr, Ah.rowidx, Ah.values = A.nrow, A.ncol, hcp.numpy(), hir.numpy(), hv.numpy()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            st_e = LC.spgemm_phased(Ah, Ah, max_phase_nnz=budget, ctx=ctx)
-        torch.cuda.synchronize()
-        e2e_s = time.perf_counter() - t0
-        e2e_s = max_over_ranks(e2e_s, world, "cuda")
-        h2d = 2 * (hcp.numel() * 8 + hir.numel() * 8 + hv.numel() * 8)
-        d2h = st_e.phases * 0 + A.ncol * 8 + 64  # per-column counts read back to cut phases + stats
-        result["e2e"] = {"value": st_e.flops * args.steps * world / e2e_s / 1e9, "unit": "Gmults/s",
-                         "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                         "path": "gbc_spgemm_phased with host pinned A/B (H2D inside the call), checksums read back"}
-        assert st_e.nnz == st.nnz and st_e.row_checksum == st.row_checksum
+    if args.workload.startswith("spgemm"):
+        result.update(bench_spgemm(args, world, A, Ad, ctx, stream, scale, ef, hbm, peak_kind))
+        if not args.no_mcl and world >= 1:
+            result["mcl"] = bench_mcl(ctx)
 
     # ---- BFS (configs[1]): 64 roots, level loop as a replayed CUDA graph --
-    g = B.Graph(A.with_values(None), ctx)
-    par = torch.empty(A.ncol, dtype=torch.int64, device="cuda")
-    lev = torch.empty(A.ncol, dtype=torch.int64, device="cuda")
-    roots = bfs_roots(A)
-    for r in roots[:3]:
-        B.bfs_device(g, int(r), par.data_ptr(), lev.data_ptr())
-    torch.cuda.synchronize()
-    edges = 0
-    l0 = _lib.lib().gbc_launch_count()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    if args.workload == "bfs20":
-        clocks = ClockSampler(local)
-        clocks.start()
-    e0.record(stream)
-    for r in roots:
-        st_b = B.bfs_device(g, int(r), par.data_ptr(), lev.data_ptr())
-        edges += st_b.edges
-    e1.record(stream)
-    torch.cuda.synchronize()
-    bfs_ms = e0.elapsed_time(e1)
-    gteps = edges / (bfs_ms * 1e-3) / 1e9
-    bfs_launches = _lib.lib().gbc_launch_count() - l0
-    result["bfs"] = {"gteps": gteps, "roots": len(roots), "ms_total": bfs_ms, "edges": edges,
-                     "semiring": "SelectMin (min parent)", "loop": "captured CUDA graph per level"}
-    if args.workload == "bfs20":
-        result.update({"metric": "BFS GTEPS (R-MAT s20 ef16, 64 roots, SelectMin parents)", "value": gteps * world,
-                       "unit": "GTEPS", "ms_per_step": bfs_ms / len(roots), "gpu_launches": bfs_launches,
-                       "clocks": clocks.stop()})
-        # e2e: host graph upload each step
-        t0 = time.perf_counter()
-        P = A.with_values(None)
-        e_edges = 0
-        for r in roots[:8]:
-            par_h, lev_h, st_h = B.bfs(P, int(r), ctx=ctx)
-            e_edges += st_h.edges
-        e2e_s = time.perf_counter() - t0
-        result["e2e"] = {"value": e_edges / e2e_s / 1e9, "unit": "GTEPS",
-                         "h2d_bytes_per_step": (A.colptr.nbytes + A.rowidx.nbytes),
-                         "d2h_bytes_per_step": 2 * A.ncol * 8}
-        achieved = edges * 2 * 4 / (bfs_ms * 1e-3) / 1e9
-        result["roofline"] = {"bound": "hbm", "kernel": "k_bfs_expand", "achieved": achieved, "peak": hbm,
-                              "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm, "traffic": None}
+    if args.workload == "bfs20" or not args.no_bfs:
+        g = B.Graph(A.with_values(None), ctx)
+        par = torch.empty(A.ncol, dtype=torch.int64, device="cuda")
+        lev = torch.empty(A.ncol, dtype=torch.int64, device="cuda")
+        roots = bfs_roots(A)
+        for r in roots[:3]:
+            B.bfs_device(g, int(r), par.data_ptr(), lev.data_ptr())
+        torch.cuda.synchronize()
+        edges = 0
+        l0 = _lib.lib().gbc_launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if args.workload == "bfs20":
+            clocks = ClockSampler(local)
+            clocks.start()
+        e0.record(stream)
+        for r in roots:
+            st_b = B.bfs_device(g, int(r), par.data_ptr(), lev.data_ptr())
+            edges += st_b.edges
+        e1.record(stream)
+        torch.cuda.synchronize()
+        bfs_ms = e0.elapsed_time(e1)
+        gteps = edges / (bfs_ms * 1e-3) / 1e9
+        bfs_launches = _lib.lib().gbc_launch_count() - l0
+        result["bfs"] = {"gteps": gteps, "roots": len(roots), "ms_total": bfs_ms, "edges": edges,
+                         "semiring": "SelectMin (min parent)", "loop": "captured CUDA graph per level"}
+        if args.workload == "bfs20":
+            result.update({"metric": metric_name(args.workload, scale, ef), "value": gteps * world,
+                           "unit": "GTEPS", "ms_per_step": bfs_ms / len(roots), "gpu_launches": bfs_launches,
+                           "clocks": clocks.stop()})
+            # e2e: host graph upload each step
+            t0 = time.perf_counter()
+            P = A.with_values(None)
+            e_edges = 0
+            for r in roots[:8]:
+                par_h, lev_h, st_h = B.bfs(P, int(r), ctx=ctx)
+                e_edges += st_h.edges
+            e2e_s = time.perf_counter() - t0
+            result["e2e"] = {"value": e_edges / e2e_s / 1e9, "unit": "GTEPS",
+                             "h2d_bytes_per_step": (A.colptr.nbytes + A.rowidx.nbytes),
+                             "d2h_bytes_per_step": 2 * A.ncol * 8}
+            achieved = edges * 2 * 4 / (bfs_ms * 1e-3) / 1e9
+            result["roofline"] = {"bound": "hbm", "kernel": "k_bfs_expand", "achieved": achieved, "peak": hbm,
+                                  "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm, "traffic": None}
 
     # ---- CPU baseline (rank 0, N=1 only) -------------------------------
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -398,7 +521,7 @@ def run_ours(args, world, rank, local):
                    "phase_budget_nnz": budget, "l2": "inputs and outputs larger than L2 (129 MB)",
                    "parallelism": f"replicas x{world}"},
     }
-    for k in ("roofline", "cpu_baseline", "e2e", "gpu_launches", "clocks", "spgemm", "bfs"):
+    for k in ("roofline", "cpu_baseline", "e2e", "gpu_launches", "clocks", "spgemm", "exact_two_phase", "mcl", "bfs"):
         if k in result:
             line[k] = result[k]
     if rank == 0:
@@ -414,6 +537,9 @@ def main():
     ap.add_argument("--workload", choices=["spgemm20", "bfs20", "spgemm14"], default="spgemm20")
     ap.add_argument("--phase-nnz", type=int, default=3 << 30)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-mcl", action="store_true", help="skip the MCL exact-vs-learned comparison")
+    ap.add_argument("--no-bfs", action="store_true", help="skip the BFS sub-measurement of SpGEMM workloads")
+    ap.add_argument("--scale", type=int, default=0, help="override the R-MAT scale (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world, rank, local = dist_setup(args)

@@ -58,8 +58,9 @@ class gbc_spgemm_stats(C.Structure):
 class gbc_phased_stats(C.Structure):
     _fields_ = [
         ("flops", C.c_int64), ("nnz", C.c_int64), ("phases", C.c_int64), ("max_phase_nnz", C.c_int64),
-        ("row_checksum", C.c_int64), ("val_checksum", C.c_double), ("ms_total", C.c_double),
-        ("ms_symbolic", C.c_double), ("ms_numeric", C.c_double),
+        ("row_checksum", C.c_int64), ("val_checksum", C.c_double), ("content_hash", C.c_uint64),
+        ("overflow_cols", C.c_int64), ("alloc_nnz", C.c_int64), ("ms_total", C.c_double),
+        ("ms_sizing", C.c_double), ("ms_numeric", C.c_double), ("ms_rerun", C.c_double),
     ]
 
 
@@ -89,7 +90,7 @@ _SIGS = {
     "gbc_spgemm": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(gbc_matrix), C.POINTER(gbc_matrix),
                              C.POINTER(gbc_spgemm_opts), C.POINTER(C.c_void_p), C.POINTER(gbc_spgemm_stats)]),
     "gbc_spgemm_phased": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(gbc_matrix), C.POINTER(gbc_matrix),
-                                    C.c_int64, C.POINTER(gbc_phased_stats)]),
+                                    C.c_int64, C.c_int, C.POINTER(gbc_phased_stats)]),
     "gbc_spgemm_colstats": (C.c_int, [C.c_void_p, C.POINTER(gbc_matrix), C.POINTER(gbc_matrix), C.c_void_p,
                                       C.c_void_p, C.c_int]),
 }

@@ -1002,145 +1002,6 @@ static int spgemm_exact(Context *ctx, const DevMatrix &A, const DevMatrix &B, co
     return GBC_OK;
 }
 
-// ------------------------------------------------------- column phases
-// Deterministic checksums of one phase's output: block partial sums over
-// contiguous ranges (fixed grid), combined in block order on the host.
-template <typename V>
-__global__ void k_phase_checksum(const int64_t *ir, const V *num, int64_t nnz, int64_t *rsum, double *vsum)
-{
-    __shared__ double sv[kWarps];
-    __shared__ long long sr[kWarps];
-    const int64_t per = (nnz + gridDim.x - 1) / gridDim.x;
-    const int64_t b0 = min(nnz, per * blockIdx.x), b1 = min(nnz, b0 + per);
-    double v = 0;
-    long long r = 0;
-    for (int64_t p = b0 + threadIdx.x; p < b1; p += blockDim.x) {
-        v += (double)num[p];
-        r += ir[p];
-    }
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-        v += __shfl_xor_sync(0xffffffffu, v, o);
-        r += __shfl_xor_sync(0xffffffffu, r, o);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        sv[threadIdx.x >> 5] = v;
-        sr[threadIdx.x >> 5] = r;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double tv = 0;
-        long long tr = 0;
-        for (int w = 0; w < kWarps; ++w) {
-            tv += sv[w];
-            tr += sr[w];
-        }
-        vsum[blockIdx.x] = tv;
-        rsum[blockIdx.x] = tr;
-    }
-}
-
-// C = A*B computed in phases of B's stored columns so that each phase's
-// output holds at most max_phase_nnz entries -- the reference's column
-// phases of MemEfficientSpGEMM (ParFriends.h:553-556, ColSplit).  Each
-// phase's C is written to HBM and reduced to checksums; nothing is kept.
-template <class SR>
-static int spgemm_phased(Context *ctx, const DevMatrix &A, const DevMatrix &B, int64_t max_phase_nnz,
-                         gbc_phased_stats *st)
-{
-    typedef typename SR::V V;
-    cudaStream_t s = ctx->stream;
-    Workspace ws(ctx);
-    cudaEventRecord(ctx->ev[0], s);
-    Plan P;
-    GBC_TRY(plan_build(ws, A, B, P));
-    const int64_t nb = B.nzc;
-    int64_t *cnt = nullptr;
-    GBC_TRY(ws.alloc_n(&cnt, nb + 1));
-    Lists L;
-    GBC_TRY(plan_classify(P, s, -1, 0, -1, L, cnt));
-    cudaEventRecord(ctx->ev[1], s);
-    GBC_TRY(run_symbolic(ctx, P, L, cnt));
-    cudaEventRecord(ctx->ev[2], s);
-    std::vector<int64_t> hcnt(nb > 0 ? nb : 1);
-    if (nb > 0) GBC_CUDA_TRY(cudaMemcpyAsync(hcnt.data(), cnt, nb * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    const int64_t flops = sum_i64(ws, ctx, P.a().flop, nb);
-    // phase boundaries (greedy; a column bigger than the budget is alone)
-    std::vector<int64_t> bounds{0};
-    int64_t acc = 0, maxp = 0, total = 0;
-    for (int64_t j = 0; j < nb; ++j) {
-        if (acc > 0 && acc + hcnt[j] > max_phase_nnz) {
-            bounds.push_back(j);
-            maxp = std::max(maxp, acc);
-            acc = 0;
-        }
-        acc += hcnt[j];
-        total += hcnt[j];
-    }
-    maxp = std::max(maxp, acc);
-    if (bounds.back() != nb) bounds.push_back(nb);
-    int64_t maxcols = 0;
-    for (size_t p = 0; p + 1 < bounds.size(); ++p) maxcols = std::max(maxcols, bounds[p + 1] - bounds[p]);
-    int64_t *ir = nullptr, *ccp = nullptr, *rsum = nullptr;
-    V *num = nullptr;
-    double *vsum = nullptr;
-    const int csb = ctx->num_sms * 2;
-    const int np = (int)bounds.size() - 1;
-    GBC_TRY(ws.alloc_n(&ir, maxp + 1));
-    GBC_TRY(ws.alloc_n(&num, maxp + 1));
-    GBC_TRY(ws.alloc_n(&ccp, maxcols + 1));
-    GBC_TRY(ws.alloc_n(&rsum, (size_t)csb * (np + 1)));
-    GBC_TRY(ws.alloc_n(&vsum, (size_t)csb * (np + 1)));
-    double ms_num = 0;
-    for (int p = 0; p < np; ++p) {
-        const int64_t j0 = bounds[p], j1 = bounds[p + 1];
-        Lists Lp;
-        GBC_TRY(plan_classify(P, s, 0, j0, j1, Lp, nullptr));
-        GBC_TRY(exclusive_scan_i64(ws, cnt + j0, ccp, j1 - j0, s));
-        cudaEventRecord(ctx->ev[5], s);
-        GBC_TRY(run_numeric<SR>(ctx, P, Lp, ccp, j0, nullptr, nullptr, nullptr, ir, num));
-        cudaEventRecord(ctx->ev[6], s);
-        int64_t pn = 0;
-        for (int64_t j = j0; j < j1; ++j) pn += hcnt[j];
-        k_phase_checksum<V><<<csb, kThreads, 0, s>>>(ir, num, pn, rsum + (size_t)p * csb, vsum + (size_t)p * csb);
-        note_launch();
-        GBC_CUDA_TRY(cudaGetLastError());
-        GBC_CUDA_TRY(cudaEventSynchronize(ctx->ev[6]));
-        float ms = 0;
-        cudaEventElapsedTime(&ms, ctx->ev[5], ctx->ev[6]);
-        ms_num += ms;
-    }
-    cudaEventRecord(ctx->ev[4], s);
-    std::vector<int64_t> hr((size_t)csb * np + 1);
-    std::vector<double> hv((size_t)csb * np + 1);
-    if (np > 0) {
-        GBC_CUDA_TRY(cudaMemcpyAsync(hr.data(), rsum, (size_t)csb * np * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-        GBC_CUDA_TRY(cudaMemcpyAsync(hv.data(), vsum, (size_t)csb * np * sizeof(double), cudaMemcpyDeviceToHost, s));
-    }
-    GBC_TRY(check_err(ctx, P));
-    if (st) {
-        float t04 = 0, t12 = 0;
-        cudaEventElapsedTime(&t04, ctx->ev[0], ctx->ev[4]);
-        cudaEventElapsedTime(&t12, ctx->ev[1], ctx->ev[2]);
-        st->flops = flops;
-        st->nnz = total;
-        st->phases = np;
-        st->ms_total = t04;
-        st->ms_symbolic = t12;
-        st->ms_numeric = ms_num;
-        int64_t rs = 0;
-        double vs = 0;
-        for (size_t k = 0; k < (size_t)csb * np; ++k) {
-            rs += hr[k];
-            vs += hv[k];
-        }
-        st->row_checksum = rs;
-        st->val_checksum = vs;
-        st->max_phase_nnz = maxp;
-    }
-    return GBC_OK;
-}
-
 // ------------------------------------------------------- learned sizing
 // Per-column features of the sizing MLP: log2(1+x) of nnz(B(:,j)), flop,
 // the largest and the spread (standard deviation) of the referenced A
@@ -1234,6 +1095,339 @@ __global__ void k_compact(int64_t nb, const int64_t *cnt, const int64_t *dst, co
             ov[d + p] = sv[b + p];
         }
     }
+}
+
+// ------------------------------------------------------- column phases
+// Checksums of one phase's output, independent of where each column's
+// entries sit (contiguous, capacity slots, or the overflow region): per
+// block, over a fixed contiguous range of the phase's columns, the sum of
+// row ids, the sum of values as double (warp-column order, so equal only
+// for equal phase cuts) and the wrap-around sum of a 64-bit mix of
+// (column, row, value bits) -- equal for equal products whatever the phases.
+__device__ __forceinline__ uint64_t mix64(uint64_t x)
+{
+    x ^= x >> 31;
+    x *= 0x7fb5d329728ea185ull;
+    x ^= x >> 27;
+    x *= 0x81dadef4bc2dd44dull;
+    x ^= x >> 33;
+    return x;
+}
+
+template <typename V>
+__device__ __forceinline__ uint64_t value_bits(V v)
+{
+    if constexpr (sizeof(V) == 8) {
+        uint64_t u;
+        memcpy(&u, &v, 8);
+        return u;
+    } else if constexpr (sizeof(V) == 4) {
+        uint32_t u;
+        memcpy(&u, &v, 4);
+        return u;
+    } else {
+        return (uint64_t)(uint8_t)v;
+    }
+}
+
+// One region of a phase's output: column i owns slots [start[i], start[i+1])
+// of (ir, val), of which the first cnt[i] (all, when cnt is null) hold
+// entries; columns with skip[i] set hold none here.
+struct ChecksumRegion {
+    int64_t ncols;
+    const int64_t *col;    // global column id of each (B's jc), or null: j0 + i
+    int64_t j0;
+    const int64_t *start;  // [ncols+1]
+    const int64_t *cnt;    // [ncols] or null
+    const int32_t *skip;   // [ncols] or null
+    const int64_t *ir;
+    const void *val;
+};
+
+// Each block takes one contiguous range of slots, so long columns are
+// shared among blocks; threads walk the columns that meet the range.
+template <typename V>
+__global__ void __launch_bounds__(256) k_phase_checksum(ChecksumRegion R, int64_t *rsum, double *vsum,
+                                                        unsigned long long *hsum)
+{
+    __shared__ double sv[kWarps];
+    __shared__ long long sr[kWarps];
+    __shared__ unsigned long long sh[kWarps];
+    __shared__ int64_t s_first;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t total = R.ncols > 0 ? R.start[R.ncols] : 0;
+    const int64_t per = (total + gridDim.x - 1) / gridDim.x;
+    const int64_t p0 = min(total, per * blockIdx.x), p1 = min(total, p0 + per);
+    if (threadIdx.x == 0) {
+        // last column whose start is <= p0 (upper bound - 1)
+        int64_t lo = 0, hi = R.ncols;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (R.start[mid] <= p0) lo = mid + 1;
+            else hi = mid;
+        }
+        s_first = lo > 0 ? lo - 1 : 0;
+    }
+    __syncthreads();
+    const V *vv = static_cast<const V *>(R.val);
+    double v = 0;
+    long long r = 0;
+    unsigned long long h = 0;
+    if (p1 > p0) {
+        for (int64_t i = s_first; i < R.ncols; ++i) {
+            const int64_t cs = R.start[i];
+            if (cs >= p1) break;
+            if (R.skip && R.skip[i]) continue;
+            const int64_t ce = R.cnt ? cs + R.cnt[i] : R.start[i + 1];
+            const int64_t b = max(cs, p0), e = min(ce, p1);
+            const uint64_t col = (uint64_t)(R.col ? R.col[i] : R.j0 + i);
+            for (int64_t p = b + threadIdx.x; p < e; p += blockDim.x) {
+                const int64_t row = R.ir[p];
+                const V x = vv[p];
+                v += (double)x;
+                r += row;
+                h += mix64((col << 32 ^ (uint64_t)row) * 0x9e3779b97f4a7c15ull ^ value_bits(x));
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 16; k; k >>= 1) {
+        v += __shfl_xor_sync(0xffffffffu, v, k);
+        r += __shfl_xor_sync(0xffffffffu, r, k);
+        h += __shfl_xor_sync(0xffffffffu, h, k);
+    }
+    if (lane == 0) {
+        sv[w] = v;
+        sr[w] = r;
+        sh[w] = h;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tv = 0;
+        long long tr = 0;
+        unsigned long long th = 0;
+        for (int k = 0; k < kWarps; ++k) {
+            tv += sv[k];
+            tr += sr[k];
+            th += sh[k];
+        }
+        vsum[blockIdx.x] = tv;
+        rsum[blockIdx.x] = tr;
+        hsum[blockIdx.x] = th;
+    }
+}
+
+// Grow-only device buffer owned by a Workspace.
+template <typename T>
+static int grow(Workspace &ws, T **p, int64_t *have, int64_t need)
+{
+    if (*p && *have >= need) return GBC_OK;
+    const int64_t n = std::max<int64_t>(need, *have + *have / 2) + 1;
+    GBC_TRY(ws.alloc_n(p, (size_t)n));
+    *have = n;
+    return GBC_OK;
+}
+
+static int learned_capacity(Context *ctx, Workspace &ws, Plan &P, int64_t nb, int64_t m, int64_t *cap)
+{
+    cudaStream_t s = ctx->stream;
+    Mlp *mlp = static_cast<Mlp *>(ctx->mlp);
+    if (!mlp || !mlp->trained)
+        return fail(GBC_EINVAL, "learned sizing needs a trained model (gbc_context_set_mlp)");
+    float *feat = nullptr, *pred = nullptr;
+    GBC_TRY(ws.alloc_n(&feat, (size_t)nb * kNF + 1));
+    GBC_TRY(ws.alloc_n(&pred, nb + 1));
+    if (nb > 0) {
+        k_features<<<grid_for(ctx, (nb + 7) / 8, 8), 256, 0, s>>>(P.a(), nb, feat);
+        note_launch();
+        GBC_TRY(mlp_predict_device(mlp, feat, nb, pred, s));
+        k_capacity<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(nb, P.a().flop, pred, mlp->margin, m, cap);
+        note_launch();
+    }
+    GBC_CUDA_TRY(cudaGetLastError());
+    return GBC_OK;
+}
+
+// C = A*B computed in phases of B's stored columns so that each phase's
+// output holds at most max_phase_nnz entries -- the reference's column
+// phases of MemEfficientSpGEMM (ParFriends.h:553-556, ColSplit).  Each
+// phase's C is written to HBM and reduced to checksums; nothing is kept.
+// Exact sizing cuts phases on the symbolic counts; learned sizing cuts them
+// on predicted capacities, writes each column into its slots and recomputes
+// the columns that overflowed exactly (symbolic + numeric) into a second
+// region before the phase's checksum.
+template <class SR>
+static int spgemm_phased(Context *ctx, const DevMatrix &A, const DevMatrix &B, int64_t max_phase_nnz, int sizing,
+                         gbc_phased_stats *st)
+{
+    typedef typename SR::V V;
+    const bool learned = sizing == GBC_SIZING_LEARNED;
+    cudaStream_t s = ctx->stream;
+    Workspace ws(ctx);
+    cudaEventRecord(ctx->ev[0], s);
+    Plan P;
+    GBC_TRY(plan_build(ws, A, B, P));
+    const int64_t nb = B.nzc;
+    int64_t *size = nullptr;  // exact counts, or capacities when learned
+    GBC_TRY(ws.alloc_n(&size, nb + 1));
+    Lists L;
+    cudaEventRecord(ctx->ev[1], s);
+    if (learned) {
+        GBC_TRY(learned_capacity(ctx, ws, P, nb, A.nrow, size));
+    } else {
+        GBC_TRY(plan_classify(P, s, -1, 0, -1, L, size));
+        GBC_TRY(run_symbolic(ctx, P, L, size));
+    }
+    cudaEventRecord(ctx->ev[2], s);
+    std::vector<int64_t> hsize(nb > 0 ? nb : 1);
+    if (nb > 0) GBC_CUDA_TRY(cudaMemcpyAsync(hsize.data(), size, nb * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    const int64_t flops = sum_i64(ws, ctx, P.a().flop, nb);
+    // phase boundaries (greedy; a column bigger than the budget is alone)
+    std::vector<int64_t> bounds{0};
+    int64_t acc = 0, maxp = 0, alloc = 0;
+    for (int64_t j = 0; j < nb; ++j) {
+        if (acc > 0 && acc + hsize[j] > max_phase_nnz) {
+            bounds.push_back(j);
+            maxp = std::max(maxp, acc);
+            acc = 0;
+        }
+        acc += hsize[j];
+        alloc += hsize[j];
+    }
+    maxp = std::max(maxp, acc);
+    if (bounds.back() != nb) bounds.push_back(nb);
+    int64_t maxcols = 0;
+    for (size_t p = 0; p + 1 < bounds.size(); ++p) maxcols = std::max(maxcols, bounds[p + 1] - bounds[p]);
+    const int csb = ctx->num_sms * 8;  // checksum blocks per region: enough warps to keep HBM busy
+    const int np = (int)bounds.size() - 1;
+    int64_t *ir = nullptr, *ccp = nullptr, *rsum = nullptr;
+    V *num = nullptr;
+    double *vsum = nullptr;
+    unsigned long long *hsum = nullptr;
+    GBC_TRY(ws.alloc_n(&ir, maxp + 1));
+    GBC_TRY(ws.alloc_n(&num, maxp + 1));
+    GBC_TRY(ws.alloc_n(&ccp, maxcols + 1));
+    GBC_TRY(ws.alloc_n(&rsum, (size_t)csb * 2 * (np + 1)));
+    GBC_TRY(ws.alloc_n(&vsum, (size_t)csb * 2 * (np + 1)));
+    GBC_TRY(ws.alloc_n(&hsum, (size_t)csb * 2 * (np + 1)));
+    // learned: per-column counts, overflow flags and the exact-rerun region
+    int64_t *cnt = nullptr, *exact = nullptr, *masked = nullptr, *beg1 = nullptr, *ir1 = nullptr;
+    V *num1 = nullptr;
+    int32_t *flag = nullptr;
+    int64_t have1 = 0, have1v = 0, overflow_cols = 0, total = 0;
+    if (learned) {
+        GBC_TRY(ws.alloc_n(&cnt, nb + 1));
+        GBC_TRY(ws.alloc_n(&exact, nb + 1));
+        GBC_TRY(ws.alloc_n(&masked, maxcols + 1));
+        GBC_TRY(ws.alloc_n(&beg1, maxcols + 1));
+        GBC_TRY(ws.alloc_n(&flag, nb + 1));
+        GBC_CUDA_TRY(cudaMemsetAsync(flag, 0, (nb + 1) * sizeof(int32_t), s));
+        GBC_CUDA_TRY(cudaMemsetAsync(cnt, 0, (nb + 1) * sizeof(int64_t), s));
+    }
+    double ms_num = 0, ms_rerun = 0;
+    for (int p = 0; p < np; ++p) {
+        const int64_t j0 = bounds[p], j1 = bounds[p + 1], nc = j1 - j0;
+        Lists Lp;
+        GBC_TRY(plan_classify(P, s, 0, j0, j1, Lp, nullptr));
+        GBC_TRY(exclusive_scan_i64(ws, size + j0, ccp, nc, s));
+        cudaEventRecord(ctx->ev[5], s);
+        if (learned)
+            GBC_TRY(run_numeric<SR>(ctx, P, Lp, ccp, j0, size, cnt, flag, ir, num));
+        else
+            GBC_TRY(run_numeric<SR>(ctx, P, Lp, ccp, j0, nullptr, nullptr, nullptr, ir, num));
+        cudaEventRecord(ctx->ev[6], s);
+        ChecksumRegion R0{nc, B.jc ? B.jc + j0 : nullptr, j0, ccp, nullptr, nullptr, ir, num};
+        ChecksumRegion R1{0, nullptr, j0, nullptr, nullptr, nullptr, nullptr, nullptr};
+        if (learned) {
+            Lists Lo;
+            GBC_TRY(plan_classify(P, s, 0, j0, j1, Lo, nullptr, flag));
+            const int64_t no = Lo.n[0] + Lo.n[1] + Lo.n[2];
+            overflow_cols += no;
+            if (no > 0) {
+                cudaEventRecord(ctx->ev[3], s);
+                GBC_TRY(run_symbolic(ctx, P, Lo, exact));
+                k_masked_counts<<<(unsigned)((nc + 255) / 256), 256, 0, s>>>(nc, flag + j0, exact + j0, masked);
+                note_launch();
+                GBC_TRY(exclusive_scan_i64(ws, masked, beg1, nc, s));
+                int64_t tot1 = 0;
+                GBC_TRY(read_i64(ctx, beg1 + nc, &tot1));
+                GBC_TRY(grow(ws, &ir1, &have1, tot1));
+                GBC_TRY(grow(ws, &num1, &have1v, tot1));
+                GBC_TRY(run_numeric<SR>(ctx, P, Lo, beg1, j0, nullptr, nullptr, nullptr, ir1, num1));
+                k_final_counts<<<(unsigned)((nc + 255) / 256), 256, 0, s>>>(nc, flag + j0, exact + j0, cnt + j0);
+                note_launch();
+                cudaEventRecord(ctx->ev[4], s);
+                GBC_CUDA_TRY(cudaEventSynchronize(ctx->ev[4]));
+                float ms = 0;
+                cudaEventElapsedTime(&ms, ctx->ev[3], ctx->ev[4]);
+                ms_rerun += ms;
+            }
+            R0.cnt = cnt + j0;
+            R0.skip = flag + j0;
+            if (no > 0) R1 = ChecksumRegion{nc, R0.col, j0, beg1, nullptr, nullptr, ir1, num1};
+        }
+        const size_t o0 = (size_t)(2 * p) * csb, o1 = o0 + csb;
+        GBC_CUDA_TRY(cudaMemsetAsync(rsum + o0, 0, 2 * csb * sizeof(int64_t), s));
+        GBC_CUDA_TRY(cudaMemsetAsync(vsum + o0, 0, 2 * csb * sizeof(double), s));
+        GBC_CUDA_TRY(cudaMemsetAsync(hsum + o0, 0, 2 * csb * sizeof(unsigned long long), s));
+        if (nc > 0) {
+            k_phase_checksum<V><<<csb, kThreads, 0, s>>>(R0, rsum + o0, vsum + o0, hsum + o0);
+            note_launch();
+        }
+        if (R1.ncols > 0) {
+            k_phase_checksum<V><<<csb, kThreads, 0, s>>>(R1, rsum + o1, vsum + o1, hsum + o1);
+            note_launch();
+        }
+        GBC_CUDA_TRY(cudaGetLastError());
+        GBC_CUDA_TRY(cudaEventSynchronize(ctx->ev[6]));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev[5], ctx->ev[6]);
+        ms_num += ms;
+    }
+    if (learned) {
+        total = sum_i64(ws, ctx, cnt, nb);
+    } else {
+        total = alloc;
+    }
+    cudaEventRecord(ctx->ev[4], s);
+    const size_t nparts = (size_t)csb * 2 * np;
+    std::vector<int64_t> hr(nparts + 1);
+    std::vector<double> hv(nparts + 1);
+    std::vector<unsigned long long> hh(nparts + 1);
+    if (np > 0) {
+        GBC_CUDA_TRY(cudaMemcpyAsync(hr.data(), rsum, nparts * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        GBC_CUDA_TRY(cudaMemcpyAsync(hv.data(), vsum, nparts * sizeof(double), cudaMemcpyDeviceToHost, s));
+        GBC_CUDA_TRY(cudaMemcpyAsync(hh.data(), hsum, nparts * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        GBC_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    GBC_TRY(check_err(ctx, P));
+    if (st) {
+        float t04 = 0, t12 = 0;
+        cudaEventElapsedTime(&t04, ctx->ev[0], ctx->ev[4]);
+        cudaEventElapsedTime(&t12, ctx->ev[1], ctx->ev[2]);
+        st->flops = flops;
+        st->nnz = total;
+        st->phases = np;
+        st->ms_total = t04;
+        st->ms_sizing = t12;
+        st->ms_numeric = ms_num;
+        st->ms_rerun = ms_rerun;
+        st->overflow_cols = overflow_cols;
+        st->alloc_nnz = alloc;
+        int64_t rs = 0;
+        double vs = 0;
+        uint64_t hs = 0;
+        for (size_t k = 0; k < nparts; ++k) {
+            rs += hr[k];
+            vs += hv[k];
+            hs += hh[k];
+        }
+        st->row_checksum = rs;
+        st->val_checksum = vs;
+        st->content_hash = hs;
+        st->max_phase_nnz = maxp;
+    }
+    return GBC_OK;
 }
 
 // The learned product before compaction: column i holds cnt[i] entries at
@@ -1650,20 +1844,21 @@ GBC_SPGEMM_INST(gbc_spgemm_select2ndmin_i64_i64, GBC_SR_SELECT2NDMIN, GBC_I64)
 GBC_SPGEMM_INST(gbc_spgemm_bool_i64, GBC_SR_BOOL, GBC_BOOL)
 
 int gbc_spgemm_phased(gbc_context *ctx, int sr, int vt, const gbc_matrix *Am, const gbc_matrix *Bm,
-                      int64_t max_phase_nnz, gbc_phased_stats *st)
+                      int64_t max_phase_nnz, int sizing, gbc_phased_stats *st)
 {
     if (!ctx) return fail(GBC_EINVAL, "null context");
     if (!Am || !Bm || Am->ncol != Bm->nrow) return fail(GBC_EINVAL, "inner dimensions do not match");
     if (max_phase_nnz <= 0) return fail(GBC_EINVAL, "phase budget must be positive");
+    if (sizing != GBC_SIZING_EXACT && sizing != GBC_SIZING_LEARNED) return fail(GBC_EINVAL, "unknown sizing mode");
     GBC_CUDA_TRY(cudaSetDevice(ctx->device));
     Workspace ws(ctx);
     DevMatrix A, B;
     GBC_TRY(upload(ws, Am, vt, &A));
     GBC_TRY(upload(ws, Bm, vt, &B));
-    if (sr == GBC_SR_PLUSTIMES && vt == GBC_F64) return spgemm_phased<PlusTimes<double>>(ctx, A, B, max_phase_nnz, st);
-    if (sr == GBC_SR_PLUSTIMES && vt == GBC_F32) return spgemm_phased<PlusTimes<float>>(ctx, A, B, max_phase_nnz, st);
+    if (sr == GBC_SR_PLUSTIMES && vt == GBC_F64) return spgemm_phased<PlusTimes<double>>(ctx, A, B, max_phase_nnz, sizing, st);
+    if (sr == GBC_SR_PLUSTIMES && vt == GBC_F32) return spgemm_phased<PlusTimes<float>>(ctx, A, B, max_phase_nnz, sizing, st);
     if (sr == GBC_SR_SELECT2NDMIN && vt == GBC_I64)
-        return spgemm_phased<Select2ndMin<int64_t>>(ctx, A, B, max_phase_nnz, st);
+        return spgemm_phased<Select2ndMin<int64_t>>(ctx, A, B, max_phase_nnz, sizing, st);
     return fail(GBC_EUNSUPPORTED, "phased SpGEMM is instantiated for PlusTimes f64/f32 and Select2ndMin i64");
 }
 

@@ -278,9 +278,11 @@ def spgemm(A, B, sr: str = "plustimes", sizing: str = "exact", sorted: bool = Tr
 
 
 def spgemm_phased(A, B, sr: str = "plustimes", max_phase_nnz: int = 1 << 31, ctx: Context | None = None,
-                  dtype=None) -> L.gbc_phased_stats:
+                  dtype=None, sizing: str = "exact") -> L.gbc_phased_stats:
     """C = A * B in column phases of at most ``max_phase_nnz`` output entries;
-    returns the statistics and checksums (the product is not kept)."""
+    returns the statistics and checksums (the product is not kept).
+    ``sizing="learned"`` sizes the phases with the context's sizing model
+    (columns that overflow their predicted capacity are recomputed exactly)."""
     ctx = ctx or default_context()
     dt = np.dtype(dtype) if dtype is not None else _value_dtype(A, B, sr)
     keep: list = []
@@ -288,7 +290,8 @@ def spgemm_phased(A, B, sr: str = "plustimes", max_phase_nnz: int = 1 << 31, ctx
     gb = as_gbc_matrix(B, keep, dt)
     st = L.gbc_phased_stats()
     L.check(L.lib().gbc_spgemm_phased(ctx.h, SR_CODES[sr], VT_OF_DTYPE[dt], C.byref(ga), C.byref(gb),
-                                      int(max_phase_nnz), C.byref(st)))
+                                      int(max_phase_nnz), L.SIZING_LEARNED if sizing == "learned" else L.SIZING_EXACT,
+                                      C.byref(st)))
     return st
 
 

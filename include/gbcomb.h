@@ -148,22 +148,28 @@ int gbc_spgemm_bool_i64(gbc_context *ctx, const gbc_matrix *A, const gbc_matrix 
  * columns are split into phases whose output holds at most max_phase_nnz
  * entries, as the phases of MemEfficientSpGEMM (ParFriends.h:553-556,
  * SpDCCols::ColSplit).  Each phase's C is produced in HBM and reduced to
- * deterministic checksums (sum of row ids, sum of values as double); the
- * product itself is not returned. */
+ * checksums; the product itself is not returned.  sizing = GBC_SIZING_EXACT
+ * cuts phases on the symbolic counts; GBC_SIZING_LEARNED cuts them on the
+ * context's sizing model's capacities and recomputes overflowing columns
+ * exactly, so nnz, row_checksum and content_hash are the same either way. */
 typedef struct {
     int64_t flops;
     int64_t nnz;
     int64_t phases;
-    int64_t max_phase_nnz;
-    int64_t row_checksum;
-    double val_checksum;
+    int64_t max_phase_nnz;  /* largest phase, in output slots */
+    int64_t row_checksum;   /* sum of row ids of all entries */
+    double val_checksum;    /* sum of values (double; rounding depends on the phase cuts) */
+    uint64_t content_hash;  /* wrap-around sum of a 64-bit mix of (column, row, value bits) */
+    int64_t overflow_cols;  /* learned: columns recomputed exactly */
+    int64_t alloc_nnz;      /* output slots allocated over all phases (= nnz when exact) */
     double ms_total;
-    double ms_symbolic;
-    double ms_numeric; /* sum over phases of the numeric kernel */
+    double ms_sizing;       /* exact: symbolic pass; learned: features + MLP + capacities */
+    double ms_numeric;      /* sum over phases of the numeric kernels */
+    double ms_rerun;        /* learned: exact recomputation of overflowing columns */
 } gbc_phased_stats;
 
 int gbc_spgemm_phased(gbc_context *ctx, int sr, int vt, const gbc_matrix *A, const gbc_matrix *B,
-                      int64_t max_phase_nnz, gbc_phased_stats *st);
+                      int64_t max_phase_nnz, int sizing, gbc_phased_stats *st);
 
 /* Symbolic helpers: per stored column of B, flop = estimateFLOP
  * (mtSpGEMM.h:1057-1134) and nnz = estimateNNZ_Hash (mtSpGEMM.h:806-933).

@@ -191,6 +191,24 @@ def test_colstats_vs_reference(gpu_ctx, golden):
         assert np.array_equal(nnz, golden[f"colstats/{name}/nnz"]), name
 
 
+def content_hash(cp, rows, vals, cols=None):
+    """Host restatement of the phased checksum: wrap-around sum over entries
+    of mix64(((col << 32) ^ row) * 0x9e3779b97f4a7c15 ^ value bits)."""
+    u = np.uint64
+    ncol = len(cp) - 1
+    col = np.repeat(np.arange(ncol, dtype=np.uint64) if cols is None else np.asarray(cols, np.uint64),
+                    np.diff(cp))
+    bits = np.asarray(vals).view(np.uint64 if np.asarray(vals).dtype.itemsize == 8 else np.uint32).astype(u)
+    with np.errstate(over="ignore"):
+        x = ((col << u(32)) ^ rows.astype(u)) * u(0x9E3779B97F4A7C15) ^ bits
+        x ^= x >> u(31)
+        x *= u(0x7FB5D329728EA185)
+        x ^= x >> u(27)
+        x *= u(0x81DADEF4BC2DD44D)
+        x ^= x >> u(33)
+        return int(np.sum(x, dtype=u))
+
+
 def test_phased_matches_single_pass(gpu_ctx, oracle_lib):
     """Column phases (small budget -> many phases) give the same nnz and
     checksums as the single-pass product and the oracle."""
@@ -199,9 +217,42 @@ def test_phased_matches_single_pass(gpu_ctx, oracle_lib):
     cp, rows, vals = gpu_csc(A, A, 0)
     pcp, prow, pval = O.port_spgemm(A, A, O.SR_PLUSTIMES_F64)
     ref_rows = int(prow.sum())
+    ref_hash = content_hash(pcp, prow, pval)
     for budget in (len(rows), 200_000, 50_000):
         st = local.spgemm_phased(A, A, max_phase_nnz=budget)
         assert st.nnz == len(prow) and st.row_checksum == ref_rows
+        assert st.content_hash == ref_hash
         assert abs(st.val_checksum - pval.sum()) <= 1e-9 * abs(pval.sum())
         assert st.phases >= (len(prow) + budget - 1) // budget
+        assert st.alloc_nnz == st.nnz and st.overflow_cols == 0
         assert st.flops == int(O.port_spgemm(A, A, O.SR_PLUSTIMES_F64, want_counts=True)[1][0].sum())
+
+
+@pytest.mark.parametrize("margin", [None, 0.0])
+def test_phased_learned_identical_to_exact(gpu_ctx, oracle_lib, margin):
+    """Learned phase sizing (model trained on another seed of the same
+    class; margin 0 forces many overflow re-runs) gives the exact product's
+    nnz, row checksum and content hash."""
+    from combblas_gb300 import sizing
+    O = oracle_lib
+    A = G.rmat(14, 8, seed=43)
+    Atrain = G.rmat(14, 8, seed=44)
+    feat, flop, nnz = sizing.features(Atrain, Atrain)
+    m = sizing.SizingModel(seed=1)
+    m.fit(feat, nnz, steps=300)
+    if margin is not None:
+        m.set_margin(margin)
+    m.use()
+    try:
+        pcp, prow, pval = O.port_spgemm(A, A, O.SR_PLUSTIMES_F64)
+        ref_hash = content_hash(pcp, prow, pval)
+        for budget in (1 << 40, 400_000):
+            ex = local.spgemm_phased(A, A, max_phase_nnz=budget)
+            le = local.spgemm_phased(A, A, max_phase_nnz=budget, sizing="learned")
+            assert ex.content_hash == ref_hash
+            assert (le.nnz, le.row_checksum, le.content_hash) == (ex.nnz, ex.row_checksum, ex.content_hash)
+            assert le.alloc_nnz >= 1 and le.flops == ex.flops
+            if margin == 0.0:
+                assert le.overflow_cols > 0
+    finally:
+        m.close()
