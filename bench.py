@@ -287,8 +287,13 @@ def bench_spgemm(args, world, A, Ad, ctx, stream, scale, ef, hbm, peak_kind):
     budget = args.phase_nnz
     model, info = train_sizing_model(ctx, scale, ef)
 
+    Bh, Bd = A, Ad
+    if args.bcols:  # profiling case: B = A(:, bcols seeded random columns), full row range
+        Bh = column_sample(A, args.bcols / A.ncol)[0]
+        Bd = LC.DeviceMatrix.from_host(Bh)
+
     def step(sizing):
-        return LC.spgemm_phased(Ad, Ad, max_phase_nnz=budget, ctx=ctx, sizing=sizing)
+        return LC.spgemm_phased(Ad, Bd, max_phase_nnz=budget, ctx=ctx, sizing=sizing)
 
     def timed(sizing, steps, clocks=None):
         torch.cuda.synchronize()
@@ -353,20 +358,25 @@ def bench_spgemm(args, world, A, Ad, ctx, stream, scale, ef, hbm, peak_kind):
     }
     # ---- e2e: host (pinned) buffers through the public C ABI ---------
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
-    hcp, hir, hv = pin(A.colptr), pin(A.rowidx), pin(A.values)
 
     class _H:
         pass
 
-    Ah = _H()
-    Ah.nrow, Ah.ncol, Ah.colptr, Ah.rowidx, Ah.values = A.nrow, A.ncol, hcp.numpy(), hir.numpy(), hv.numpy()
+    def pinned(M):
+        H = _H()
+        H.nrow, H.ncol = M.nrow, M.ncol
+        H.colptr, H.rowidx, H.values = pin(M.colptr).numpy(), pin(M.rowidx).numpy(), pin(M.values).numpy()
+        return H
+
+    Ah = pinned(A)
+    Bhp = Ah if Bh is A else pinned(Bh)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        st_e = LC.spgemm_phased(Ah, Ah, max_phase_nnz=budget, ctx=ctx, sizing="learned")
+        st_e = LC.spgemm_phased(Ah, Bhp, max_phase_nnz=budget, ctx=ctx, sizing="learned")
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0, world, "cuda")
-    h2d = 2 * (hcp.numel() * 8 + hir.numel() * 8 + hv.numel() * 8)
+    h2d = sum(M.colptr.nbytes + M.rowidx.nbytes + M.values.nbytes for M in (Ah, Bhp))
     d2h = A.ncol * 8 + 3 * 8 * ctx_sms(ctx) * 6 * st_e.phases  # capacities (phase cuts) + checksum partials
     out["e2e"] = {"value": st_e.flops * args.steps * world / e2e_s / 1e9, "unit": "Gmults/s",
                   "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -519,7 +529,7 @@ def run_ours(args, world, rank, local):
         "config": {"workload": args.workload, "scale": scale, "edge_factor": ef, "seed": SEED,
                    "rmat_abcd": [0.57, 0.19, 0.19, 0.05], "index": "int64",
                    "phase_budget_nnz": budget, "l2": "inputs and outputs larger than L2 (129 MB)",
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}", **({"b_columns": args.bcols} if args.bcols else {})},
     }
     for k in ("roofline", "cpu_baseline", "e2e", "gpu_launches", "clocks", "spgemm", "exact_two_phase", "mcl", "bfs"):
         if k in result:
@@ -540,6 +550,8 @@ def main():
     ap.add_argument("--no-mcl", action="store_true", help="skip the MCL exact-vs-learned comparison")
     ap.add_argument("--no-bfs", action="store_true", help="skip the BFS sub-measurement of SpGEMM workloads")
     ap.add_argument("--scale", type=int, default=0, help="override the R-MAT scale (profiling runs)")
+    ap.add_argument("--bcols", type=int, default=0,
+                    help="profiling case: B = A(:, this many seeded random columns) instead of A")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world, rank, local = dist_setup(args)

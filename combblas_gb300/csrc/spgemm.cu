@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(kThreads) k_symbolic(const SpgemmArgs *args, c
     __shared__ int64_t s_col;
     __shared__ int64_t s_red[kThreads / 32];
     __shared__ SpgemmArgs sa;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (;;) {
         if (tid == 0) {
             s_col = (int64_t)atomicAdd(work, 1ull);
@@ -252,12 +252,25 @@ __global__ void __launch_bounds__(kThreads) k_symbolic(const SpgemmArgs *args, c
                 for (int w = tid; w < words; w += kThreads) bm[w] = 0;
                 __syncthreads();
                 for (int64_t cb = bs; cb < be; cb += kThreads) {
-                    int L = load_chunk(a, ch, cb, be, t0, t1, false, nullptr);
-                    for (int j = tid; j < L; j += kThreads) {
-                        int b = chunk_find(ch, j);
-                        int64_t idx = ch.s[b] + (j - ch.off[b]);
-                        int r = a.arow[idx] - (int)row0;
-                        atomicOr(&bm[r >> 5], 1u << (r & 31));
+                    int nseg;
+                    const int L = load_chunk_nz<int>(a, ch, cb, be, t0, t1, nullptr, nullptr, 0, nseg);
+                    // warp w takes a contiguous span of products in 32-product windows
+                    const int span = ((L + kThreads - 1) / kThreads) * 32;
+                    const int wb = warp * span, we = min(L, wb + span);
+                    if (wb < we) {
+                        int bcur = chunk_find_nz(ch, nseg, wb);
+                        for (int P = wb; P < we; P += 32) {
+                            const int p = P + lane;
+                            const int b = window_seg(ch, nseg, bcur, p);
+                            if (p < we) {
+                                const int64_t idx = (int64_t)ch.s[b] + (p - ch.off[b]);
+                                const int r = a.arow[idx] - (int)row0;
+                                atomicOr(&bm[r >> 5], 1u << (r & 31));
+                            }
+                            int bn = __shfl_sync(0xffffffffu, b, 31);
+                            if (bn + 1 < nseg && ch.off[bn + 1] <= P + 32) ++bn;
+                            bcur = bn;
+                        }
                     }
                     __syncthreads();
                 }
@@ -288,57 +301,28 @@ __global__ void __launch_bounds__(kThreads) k_symbolic(const SpgemmArgs *args, c
 //  * dense accumulator acc[R] and touched bitmap in shared memory;
 //  * the column's B entries are walked in chunks of kThreads; the chunk's A
 //    segments restricted to tile t form a flattened product list, processed
-//    in sub-batches of kSub products.  Segment ids of a sub-batch come from a
-//    block max-scan over segment-start markers;
+//    in sub-batches of SUB products (only the rounds of kThreads products
+//    that hold any are executed).  Empty segments are dropped when the
+//    chunk is loaded; the first segment of every 32-product window comes
+//    from a binary search (one thread per window), the segments of its
+//    lanes from a five-step search over the next 32 boundaries held in
+//    registers (window_seg);
 //  * staging: all threads load the sub-batch's rows and values with
-//    coalesced reads (one load per product), multiply by B(k,j) and store
-//    them to shared memory in flattened (k-major) order;
-//  * folding: every warp walks every 32-product window of the staged list
-//    but folds only the rows of its 32-row stripes (stripe mod kWarps), in
-//    window order.  A window inside one A segment has distinct rows; a
-//    window spanning segments groups equal rows with __match_any_sync and the
-//    lowest lane folds the group in lane order.  Each output entry is thus
-//    the left fold acc = add(mrhs, acc) over k ascending.
-// Inclusive max-scan of seg[0..n) (uint8 segment-start markers, 0 where no
-// segment starts) seeded with `seed`: seg[j] = id of the segment holding j.
-template <int SUB>
-__device__ __forceinline__ void seg_max_scan(uint8_t *seg, int seed)
-{
-    constexpr int kSubPerThread = SUB / kThreads;
-    __shared__ int ws[kWarps];
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    uint8_t loc[kSubPerThread];
-    if constexpr (kSubPerThread == 16)
-        *reinterpret_cast<uint4 *>(loc) = *reinterpret_cast<const uint4 *>(seg + tid * kSubPerThread);
-    else
-        *reinterpret_cast<uint2 *>(loc) = *reinterpret_cast<const uint2 *>(seg + tid * kSubPerThread);
-    int run = 0;
-#pragma unroll
-    for (int u = 0; u < kSubPerThread; ++u) run = max(run, (int)loc[u]);
-    int x = run;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        int y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x = max(x, y);
-    }
-    if (lane == 31) ws[wid] = x;
-    __syncthreads();
-    int pre = seed;
-    for (int w = 0; w < wid; ++w) pre = max(pre, ws[w]);
-    int excl = __shfl_up_sync(0xffffffffu, x, 1);
-    if (lane > 0) pre = max(pre, excl);
-    int cur = pre;
-#pragma unroll
-    for (int u = 0; u < kSubPerThread; ++u) {
-        cur = max(cur, (int)loc[u]);
-        loc[u] = (uint8_t)cur;
-    }
-    if constexpr (kSubPerThread == 16)
-        *reinterpret_cast<uint4 *>(seg + tid * kSubPerThread) = *reinterpret_cast<const uint4 *>(loc);
-    else
-        *reinterpret_cast<uint2 *>(seg + tid * kSubPerThread) = *reinterpret_cast<const uint2 *>(loc);
-    __syncthreads();
-}
+//    coalesced reads (one load per product, k-major order) and multiply by
+//    B(k,j); a stable partition by owner warp (row_owner: a hash of the
+//    row), ranked with three ballots and one block scan of the group sizes,
+//    writes each product into its owner's bucket in shared memory, keeping
+//    k order inside every bucket;
+//  * folding: each warp walks its bucket in 32-product windows.  Equal rows
+//    in a window are grouped with __match_any_sync and the lowest lane folds
+//    the group in lane order.  Each output entry is thus the left fold
+//    acc = add(mrhs, acc) over k ascending, with no atomics on values.
+// Owner warp of tile row o: the top bits of a multiplicative hash.  Every
+// bit of an R-MAT row id is skewed (set with probability c + d), so any
+// owner taken from a few row bits gets a fixed share far above 1/kWarps;
+// the hash spreads rows evenly and leaves only single hot rows.
+static_assert(kWarps == 8, "row_owner returns 3 bits");
+__device__ __forceinline__ int row_owner(int o) { return (int)(((uint32_t)o * 0x9E3779B1u) >> 29); }
 
 template <class SR, int SUB>
 __global__ void __launch_bounds__(kThreads, SUB <= 2048 ? 2 : 1) k_numeric(const SpgemmArgs *args, const int64_t *items, int64_t nitems,
@@ -353,6 +337,8 @@ __global__ void __launch_bounds__(kThreads, SUB <= 2048 ? 2 : 1) k_numeric(const
     __shared__ ChunkSmem ch;
     __shared__ V ch_bv[kThreads];
     __shared__ int32_t s_cnt[kWarps * kSubPerThread * kWarps + 1];  // [owner][round][warp]
+    __shared__ int32_t s_wsum[kWarps];
+    __shared__ int32_t s_win[SUB / 32];
     __shared__ int64_t s_col;
     __shared__ SpgemmArgs sa;
     V *cval = static_cast<V *>(cval_v);
@@ -373,10 +359,10 @@ __global__ void __launch_bounds__(kThreads, SUB <= 2048 ? 2 : 1) k_numeric(const
         const int64_t i = item_col(items[ci]);
         const int64_t g = a.col_base + i;
         V *acc = reinterpret_cast<V *>(smem);                            // [R]
-        V *sval = acc + a.R;                                             // [kSub]
+        V *sval = acc + a.R;                                             // [kSub] owner buckets
         uint32_t *bm = reinterpret_cast<uint32_t *>(sval + kSub);        // [R/32]
         uint16_t *srow = reinterpret_cast<uint16_t *>(bm + (a.R >> 5));  // [kSub]
-        uint8_t *seg = reinterpret_cast<uint8_t *>(srow + kSub);         // [kSub]
+        uint8_t *tag = reinterpret_cast<uint8_t *>(srow + kSub);         // [R] window row tags
         const V *aval = static_cast<const V *>(a.aval);
         const V *bval = static_cast<const V *>(a.bval);
         const int words = a.R >> 5;
@@ -395,57 +381,68 @@ __global__ void __launch_bounds__(kThreads, SUB <= 2048 ? 2 : 1) k_numeric(const
                 for (int w = tid; w < words; w += kThreads) bm[w] = 0;
                 __syncthreads();
                 for (int64_t cb = bs; cb < be; cb += kThreads) {
-                    const int L = load_chunk<V>(a, ch, cb, be, t, t + 1, bval, ch_bv, SR::one());
-                    const int myoff = ch.off[tid], mylen = ch.off[tid + 1] - myoff;
+                    int nseg;
+                    const int L = load_chunk_nz<V>(a, ch, cb, be, t, t + 1, bval, ch_bv, SR::one(), nseg);
                     for (int q = 0; q < L; q += kSub) {
                         const int n = min(kSub, L - q);
-                        // 1. segment ids of products q .. q+n-1
-                        if constexpr (kSubPerThread == 16)
-                            *reinterpret_cast<uint4 *>(seg + tid * kSubPerThread) = make_uint4(0, 0, 0, 0);
-                        else
-                            *reinterpret_cast<uint2 *>(seg + tid * kSubPerThread) = make_uint2(0, 0);
+                        // 1. first segment of every 32-product window of the sub-batch:
+                        //    one binary search per window, in parallel
+                        const int rounds = (n + kThreads - 1) / kThreads;  // block-uniform
+                        if (tid < (n + 31) >> 5) s_win[tid] = chunk_find_nz(ch, nseg, q + tid * 32);
                         __syncthreads();
-                        if (mylen > 0 && myoff >= q && myoff < q + n) seg[myoff - q] = (uint8_t)tid;
-                        __syncthreads();
-                        seg_max_scan<SUB>(seg, chunk_find(ch, q));
-                        // 2. load (round-major, all loads in flight), owner = 32-row stripe mod kWarps
+                        // 2. load: round r covers products [r*kThreads, (r+1)*kThreads) of
+                        //    the sub-batch, warp w its window at r*kThreads + 32w
+                        //    (coalesced; the unrolled rounds keep all loads in flight);
+                        //    the lanes' segments come from window_seg
                         int o_[kSubPerThread];
                         V v_[kSubPerThread];
 #pragma unroll
                         for (int r = 0; r < kSubPerThread; ++r) {
-                            const int j = r * kThreads + tid;
                             o_[r] = -1;
-                            if (j < n) {
-                                const int b = seg[j];
-                                const int64_t idx = (int64_t)ch.s[b] + (q + j - ch.off[b]);
-                                o_[r] = a.arow[idx] - row0;
-                                const V av = aval ? aval[idx] : SR::one();
-                                v_[r] = SR::mul(av, ch_bv[b]);
+                            const int P = q + r * kThreads + warp * 32;
+                            if (r < rounds && P < q + n) {  // warp-uniform
+                                const int p = P + lane;
+                                const int b = window_seg(ch, nseg, s_win[r * kWarps + warp], p);
+                                if (p < q + n) {
+                                    const int64_t idx = (int64_t)ch.s[b] + (p - ch.off[b]);
+                                    o_[r] = a.arow[idx] - row0;
+                                    const V av = aval ? aval[idx] : SR::one();
+                                    v_[r] = SR::mul(av, ch_bv[b]);
+                                }
                             }
                         }
-                        // 3. stable partition by owner: rank within (round, warp) from 3 ballots
+                        // 3. stable partition by owner warp (row_owner): rank
+                        //    within (round, warp) from 3 ballots; counts laid out
+                        //    [owner][round][warp] so the scan follows product order
                         int rk_[kSubPerThread];
 #pragma unroll
                         for (int r = 0; r < kSubPerThread; ++r) {
-                            const bool act = o_[r] >= 0;
-                            const int w = (o_[r] >> 5) & (kWarps - 1);
-                            const unsigned va = __ballot_sync(0xffffffffu, act);
-                            const unsigned b0 = __ballot_sync(0xffffffffu, act && (w & 1));
-                            const unsigned b1 = __ballot_sync(0xffffffffu, act && (w & 2));
-                            const unsigned b2 = __ballot_sync(0xffffffffu, act && (w & 4));
-                            const unsigned same = va & ((w & 1) ? b0 : ~b0) & ((w & 2) ? b1 : ~b1) & ((w & 4) ? b2 : ~b2);
-                            rk_[r] = __popc(same & lt);
-                            // lanes 0..kWarps-1 publish the size of owner `lane`'s group (0 if absent)
-                            if (lane < kWarps) {
-                                const unsigned sl = va & ((lane & 1) ? b0 : ~b0) & ((lane & 2) ? b1 : ~b1) &
-                                                    ((lane & 4) ? b2 : ~b2);
-                                s_cnt[(lane * kSubPerThread + r) * kWarps + warp] = __popc(sl);
+                            if (r < rounds) {
+                                const bool act = o_[r] >= 0;
+                                const int w = row_owner(o_[r]);
+                                const unsigned va = __ballot_sync(0xffffffffu, act);
+                                const unsigned b0 = __ballot_sync(0xffffffffu, act && (w & 1));
+                                const unsigned b1 = __ballot_sync(0xffffffffu, act && (w & 2));
+                                const unsigned b2 = __ballot_sync(0xffffffffu, act && (w & 4));
+                                const unsigned same =
+                                    va & ((w & 1) ? b0 : ~b0) & ((w & 2) ? b1 : ~b1) & ((w & 4) ? b2 : ~b2);
+                                rk_[r] = __popc(same & lt);
+                                // lanes 0..kWarps-1 publish the size of owner `lane`'s group
+                                if (lane < kWarps) {
+                                    const unsigned sl = va & ((lane & 1) ? b0 : ~b0) & ((lane & 2) ? b1 : ~b1) &
+                                                        ((lane & 4) ? b2 : ~b2);
+                                    s_cnt[(lane * kSubPerThread + r) * kWarps + warp] = __popc(sl);
+                                }
+                            } else if (lane < kWarps) {
+                                s_cnt[(lane * kSubPerThread + r) * kWarps + warp] = 0;
                             }
                         }
                         __syncthreads();
-                        // 4. exclusive scan of the (owner, round, warp) counts
+                        // 4. exclusive scan of the (owner, round, warp) counts: PER
+                        //    consecutive counts per thread, warp scan, one barrier for
+                        //    the warp totals
                         {
-                            constexpr int PER = (NC + kThreads - 1) / kThreads;
+                            constexpr int PER = NC / kThreads;
                             int loc[PER];
                             int sum = 0;
 #pragma unroll
@@ -453,47 +450,70 @@ __global__ void __launch_bounds__(kThreads, SUB <= 2048 ? 2 : 1) k_numeric(const
                                 loc[u] = s_cnt[tid * PER + u];
                                 sum += loc[u];
                             }
-                            int64_t tot64;
-                            int base = (int)block_exclusive_sum64(sum, &tot64);
+                            int x = sum;
+#pragma unroll
+                            for (int o = 1; o < 32; o <<= 1) {
+                                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                                if (lane >= o) x += y;
+                            }
+                            if (lane == 31) s_wsum[warp] = x;
+                            __syncthreads();
+                            int base = x - sum, tot = 0;
+#pragma unroll
+                            for (int u = 0; u < kWarps; ++u) {
+                                const int ws = s_wsum[u];
+                                base += u < warp ? ws : 0;
+                                tot += ws;
+                            }
 #pragma unroll
                             for (int u = 0; u < PER; ++u) {
                                 s_cnt[tid * PER + u] = base;
                                 base += loc[u];
                             }
-                            if (tid == 0) s_cnt[NC] = (int)tot64;
+                            if (tid == 0) s_cnt[NC] = tot;
                         }
                         __syncthreads();
                         // 5. scatter into owner buckets
 #pragma unroll
                         for (int r = 0; r < kSubPerThread; ++r) {
-                            if (o_[r] >= 0) {
-                                const int w = (o_[r] >> 5) & (kWarps - 1);
+                            if (r < rounds && o_[r] >= 0) {
+                                const int w = row_owner(o_[r]);
                                 const int pos = s_cnt[(w * kSubPerThread + r) * kWarps + warp] + rk_[r];
                                 srow[pos] = (uint16_t)o_[r];
                                 sval[pos] = v_[r];
                             }
                         }
                         __syncthreads();
-                        // 6. each warp folds its bucket in staging (= k) order
+                        // 6. each warp folds its bucket in staging (= k) order.  A window
+                        //    whose rows are distinct (tag test: every lane stores its id
+                        //    at its row's tag and reads it back) folds lane-parallel;
+                        //    otherwise equal rows are grouped with __match_any_sync and
+                        //    the lowest lane folds the group in lane order
                         {
-                            const int beg = s_cnt[(warp * kSubPerThread) * kWarps];
-                            const int end = s_cnt[((warp + 1) * kSubPerThread) * kWarps];
+                            const int beg = s_cnt[warp * kWarps * kSubPerThread];
+                            const int end = s_cnt[(warp + 1) * kWarps * kSubPerThread];
                             for (int p0 = beg; p0 < end; p0 += 32) {
                                 const int p = p0 + lane;
                                 const bool act = p < end;
                                 const int o = act ? (int)srow[p] : (0x10000 + lane);
-                                const unsigned grp = __match_any_sync(0xffffffffu, o);
+                                if (act) tag[o] = (uint8_t)lane;
+                                __syncwarp();
+                                const bool clash = act && tag[o] != (uint8_t)lane;
+                                const unsigned grp = __ballot_sync(0xffffffffu, clash)
+                                                         ? __match_any_sync(0xffffffffu, o)
+                                                         : (1u << lane);
                                 if (act && (grp & lt) == 0) {
                                     const uint32_t bit = 1u << (o & 31);
                                     const bool touched = (bm[o >> 5] & bit) != 0;
-                                    V cur = touched ? SR::add(sval[p], acc[o]) : sval[p];
+                                    V *ap = acc + o;
+                                    V cur = touched ? SR::add(sval[p], *ap) : sval[p];
                                     unsigned rest = grp & ~(1u << lane);
                                     while (rest) {
                                         const int m = __ffs(rest) - 1;
                                         rest &= rest - 1;
                                         cur = SR::add(sval[p0 + m], cur);
                                     }
-                                    acc[o] = cur;
+                                    *ap = cur;
                                     if (!touched) atomicOr(&bm[o >> 5], bit);
                                 }
                                 __syncwarp();
@@ -509,8 +529,22 @@ __global__ void __launch_bounds__(kThreads, SUB <= 2048 ? 2 : 1) k_numeric(const
                     const int wpt = (words + kThreads - 1) / kThreads;
                     const int w0 = min(words, tid * wpt), w1 = min(words, (tid + 1) * wpt);
                     for (int w = w0; w < w1; ++w) wl += __popc(bm[w]);
-                    int64_t tot;
-                    int64_t pos = out + block_exclusive_sum64(wl, &tot);
+                    int x = wl;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int y = __shfl_up_sync(0xffffffffu, x, o);
+                        if (lane >= o) x += y;
+                    }
+                    if (lane == 31) s_wsum[warp] = x;
+                    __syncthreads();
+                    int before = 0, tot = 0;
+#pragma unroll
+                    for (int u = 0; u < kWarps; ++u) {
+                        const int ws = s_wsum[u];
+                        before += u < warp ? ws : 0;
+                        tot += ws;
+                    }
+                    int64_t pos = out + before + x - wl;
                     for (int w = w0; w < w1; ++w) {
                         uint32_t x = bm[w];
                         while (x) {

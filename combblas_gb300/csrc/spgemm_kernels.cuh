@@ -80,42 +80,48 @@ struct ChunkSmem {
     int32_t off[kThreads + 1];
 };
 
+// Load one chunk, keeping only the non-empty segments: ch.s / ch.off (and
+// ch_bv) hold the nseg non-empty segments in entry order, ch.off[nseg] =
+// total.
+// One block scan packs the segment length (high word) with a non-empty
+// flag (low word), giving offsets and compacted positions together.
 template <typename V>
-__device__ __forceinline__ int load_chunk(const SpgemmArgs &a, ChunkSmem &ch, int64_t cb, int64_t be, int t0, int t1,
-                                          const V *bval, V *ch_bv, V one)
+__device__ __forceinline__ int load_chunk_nz(const SpgemmArgs &a, ChunkSmem &ch, int64_t cb, int64_t be, int t0,
+                                             int t1, const V *bval, V *ch_bv, V one, int &nseg)
 {
     const int tid = threadIdx.x;
     const int64_t b = cb + tid;
     int len = 0;
+    uint32_t s = 0;
+    V bv = one;
     if (b < be) {
         const int k = a.brow[b];
         const uint32_t *tp = a.tptr + (int64_t)k * (a.T + 1);
-        const uint32_t s = tp[t0], e = tp[t1];
-        ch.s[tid] = s;
-        len = (int)(e - s);
-        if (ch_bv) ch_bv[tid] = bval ? bval[b] : one;
+        s = tp[t0];
+        len = (int)(tp[t1] - s);
+        if (ch_bv && bval) bv = bval[b];
     }
     int64_t tot;
-    const int off = (int)block_exclusive_sum64(len, &tot);
-    ch.off[tid] = off;
-    if (tid == kThreads - 1) ch.off[kThreads] = off + len;
+    const int64_t ex = block_exclusive_sum64(((int64_t)len << 32) | (len > 0 ? 1 : 0), &tot);
+    if (len > 0) {
+        const int c = (int)(ex & 0xffffffff);
+        ch.s[c] = s;
+        ch.off[c] = (int)(ex >> 32);
+        if (ch_bv) ch_bv[c] = bv;
+    }
+    nseg = (int)(tot & 0xffffffff);
+    if (tid == 0) ch.off[nseg] = (int)(tot >> 32);
     __syncthreads();
-    return (int)tot;
+    return (int)(tot >> 32);
 }
 
-__device__ __forceinline__ int load_chunk(const SpgemmArgs &a, ChunkSmem &ch, int64_t cb, int64_t be, int t0, int t1,
-                                          bool, const void *)
+// Largest segment b < nseg with ch.off[b] <= p (warp-uniform p: broadcast reads).
+__device__ __forceinline__ int chunk_find_nz(const ChunkSmem &ch, int nseg, int p)
 {
-    return load_chunk<int>(a, ch, cb, be, t0, t1, nullptr, nullptr, 0);
-}
-
-// Index b of the chunk entry holding flattened product j (off[b] <= j < off[b+1]).
-__device__ __forceinline__ int chunk_find(const ChunkSmem &ch, int j)
-{
-    int lo = 0, hi = kThreads;
+    int lo = 0, hi = nseg;
     while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
-        if (ch.off[mid] <= j)
+        if (ch.off[mid] <= p)
             lo = mid;
         else
             hi = mid;
@@ -123,12 +129,30 @@ __device__ __forceinline__ int chunk_find(const ChunkSmem &ch, int j)
     return lo;
 }
 
+// Segment of product p for a warp whose 32-product window starts inside
+// segment bcur (segments non-empty, so at most 31 boundaries follow the
+// window start within it): lane k holds the boundary ch.off[bcur+1+k] and a
+// five-step binary search over the lanes counts the boundaries <= p.  All
+// lanes of the warp must call it.
+__device__ __forceinline__ int window_seg(const ChunkSmem &ch, int nseg, int bcur, int p)
+{
+    const int lane = threadIdx.x & 31;
+    const int o = ch.off[min(bcur + 1 + lane, nseg)];
+    int c = 0;
+#pragma unroll
+    for (int step = 16; step; step >>= 1) {
+        const int v = __shfl_sync(0xffffffffu, o, c + step - 1);
+        if (v <= p) c += step;
+    }
+    return bcur + c;
+}
+
 inline size_t numeric_smem_bytes(int R, size_t vsize, int sub)
 {
-    // acc[R] + sval[sub] (values) + bitmap[R/32] + srow[sub] (u16) + seg[sub] (u8)
+    // acc[R] + sval[sub] (values) + bitmap[R/32] + srow[sub] (u16) + tag[R] (u8)
     size_t b = (size_t)R * vsize + (size_t)sub * vsize;
     b += (size_t)(R / 32) * 4;
-    b += (size_t)sub * 2 + sub;
+    b += (size_t)sub * 2 + (size_t)R;
     return (b + 15) & ~size_t(15);
 }
 
