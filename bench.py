@@ -40,6 +40,7 @@ sys.path.insert(0, ROOT)
 
 SEED = 1
 BFS_ROOTS = 64
+MS_ROOTS = 512
 
 
 def log(*a):
@@ -197,7 +198,7 @@ def barrier(world):
 def make_graph(workload, scale_override=0):
     from combblas_gb300 import generators as G
 
-    scale, ef = (14, 8) if workload == "spgemm14" else (20, 16)
+    scale, ef = {"spgemm14": (14, 8), "msbfs22": (22, 16)}.get(workload, (20, 16))
     if scale_override:
         scale = scale_override
     t0 = time.perf_counter()
@@ -223,7 +224,7 @@ def run_reference(args, world, rank):
     budget = 20.0
     steps = []
     desc, threads = "", 1
-    if args.workload == "bfs20":
+    if args.workload in ("bfs20", "msbfs22"):
         roots = bfs_roots(A)
         for s in range(args.warmup + args.steps):
             v, desc, threads = cpu_bfs_rate(A, roots[s % len(roots):], budget / 4)
@@ -239,7 +240,8 @@ def run_reference(args, world, rank):
     val = float(np.median(steps))
     line = {
         "impl": "reference", "metric": metric, "value": val, "unit": unit, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.workload.startswith("spgemm") else "int64",
         "data": "synthetic (seeded R-MAT)",
         "config": {"workload": args.workload, "scale": scale, "edge_factor": ef, "seed": SEED},
         "cpu_baseline": {"value": val, "unit": unit, "cores": threads, "kind": "port",
@@ -251,6 +253,8 @@ def run_reference(args, world, rank):
 
 
 def metric_name(workload, scale, ef):
+    if workload == "msbfs22":
+        return f"multi-source BFS GTEPS (R-MAT s{scale} ef{ef}, {MS_ROOTS} roots, Select2ndMin SpGEMM loop)"
     if workload == "bfs20":
         return f"BFS GTEPS (R-MAT s{scale} ef{ef}, 64 roots, SelectMin parents)"
     return f"SpGEMM Gmults/s (R-MAT s{scale} ef{ef} A*A, PlusTimes fp64, exact output)"
@@ -442,6 +446,85 @@ def bench_mcl(ctx):
 
 
 
+def bench_msbfs(args, world, A, ctx, stream, hbm, peak_kind, scale, ef):
+    """Multi-source BFS from MS_ROOTS seeded roots at once (the masked
+    Select2ndMin SpGEMM loop); a step is one whole traversal."""
+    import torch
+    from combblas_gb300 import _lib
+    from combblas_gb300 import bfs as B
+
+    P = A.with_values(None)
+    g = B.Graph(P, ctx)
+    deg = np.diff(A.colptr)
+    roots = np.random.default_rng(SEED + 200).choice(np.nonzero(deg)[0], MS_ROOTS, replace=False)
+    par = torch.empty((MS_ROOTS, A.ncol), dtype=torch.int64, device="cuda")
+    for _ in range(args.warmup):
+        B.msbfs(g, roots, par.data_ptr())
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = ClockSampler(int(torch.cuda.current_device()))
+    clocks.start()
+    l0 = _lib.lib().gbc_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    edges = 0
+    e0.record(stream)
+    for _ in range(args.steps):
+        _, st = B.msbfs(g, roots, par.data_ptr())
+        edges += st.edges
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = max_over_ranks(e0.elapsed_time(e1), world, "cuda")
+    launches = _lib.lib().gbc_launch_count() - l0
+    ck = clocks.stop()
+    value = edges * world / (ms * 1e-3) / 1e9
+    # expand kernel bytes per traversal: per scanned edge a 4-byte row id, a
+    # visited-bit word and a 4-byte candidate read (8-byte frontier entry per
+    # (root, vertex)), parents written once per reached pair
+    scanned = 2 * st.edges
+    bytes_trav = scanned * (4 + 4 + 4) + st.reached * (8 + 8 + 8)
+    achieved = bytes_trav / (ms / args.steps * 1e-3) / 1e9
+    out = {
+        "metric": metric_name(args.workload, scale, ef), "value": value, "unit": "GTEPS",
+        "ms_per_step": ms / args.steps, "gpu_launches": launches, "clocks": ck,
+        "msbfs": {"roots": MS_ROOTS, "levels": st.levels, "reached_pairs": st.reached, "edges_per_step": st.edges,
+                  "loop": "masked Select2ndMin product into a per-(root, vertex) candidate array; one captured "
+                          "CUDA graph per level"},
+        "roofline": {"bound": "hbm", "kernel": "k_ms_expand + k_ms_finalize", "achieved": achieved, "peak": hbm,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm, "traffic": None},
+    }
+    # e2e: graph upload from host + traversal + parents read back into pinned host memory
+    hp = torch.empty((MS_ROOTS, A.ncol), dtype=torch.int64, pin_memory=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e_edges = 0
+    for _ in range(args.steps):
+        g2 = B.Graph(P, ctx)
+        st_h = _msbfs_to_host(B, g2, roots, hp)
+        e_edges += st_h.edges
+        g2.close()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, "cuda")
+    out["e2e"] = {"value": e_edges * world / e2e_s / 1e9, "unit": "GTEPS",
+                  "h2d_bytes_per_step": int(A.colptr.nbytes + A.rowidx.nbytes + roots.nbytes),
+                  "d2h_bytes_per_step": int(hp.numel() * 8),
+                  "path": "gbc_graph_create from host CSC + gbc_msbfs writing parents to pinned host memory"}
+    assert np.array_equal(hp[:4].numpy(), par[:4].cpu().numpy())
+    g.close()
+    return out
+
+
+def _msbfs_to_host(B, g, roots, hp):
+    import ctypes as C
+
+    from combblas_gb300 import _lib as L
+
+    roots = np.ascontiguousarray(roots, np.int64)
+    st = L.gbc_msbfs_stats()
+    L.check(L.lib().gbc_msbfs(g.ctx.h, g.h, roots.ctypes.data, len(roots), C.c_void_p(hp.data_ptr()), L.GBC_HOST,
+                              C.byref(st)))
+    return st
+
+
+
 # ------------------------------------------------------------------- ours
 def run_ours(args, world, rank, local):
     import torch
@@ -467,8 +550,11 @@ def run_ours(args, world, rank, local):
         if not args.no_mcl and world >= 1:
             result["mcl"] = bench_mcl(ctx)
 
-    # ---- BFS (configs[1]): 64 roots, level loop as a replayed CUDA graph --
-    if args.workload == "bfs20" or not args.no_bfs:
+    if args.workload == "msbfs22":
+        result.update(bench_msbfs(args, world, A, ctx, stream, hbm, peak_kind, scale, ef))
+
+    # ---- BFS: 64 roots, level loop as a replayed CUDA graph --------------
+    if args.workload == "bfs20" or (args.workload.startswith("spgemm") and not args.no_bfs):
         g = B.Graph(A.with_values(None), ctx)
         par = torch.empty(A.ncol, dtype=torch.int64, device="cuda")
         lev = torch.empty(A.ncol, dtype=torch.int64, device="cuda")
@@ -514,9 +600,12 @@ def run_ours(args, world, rank, local):
 
     # ---- CPU baseline (rank 0, N=1 only) -------------------------------
     if rank == 0 and world == 1 and not args.no_cpu:
-        if args.workload == "bfs20":
-            v, desc, th = cpu_bfs_rate(A, roots[:8], 15.0)
-            result["cpu_baseline"] = {"value": v, "unit": "GTEPS", "cores": th, "kind": "port", "sample": desc}
+        if args.workload in ("bfs20", "msbfs22"):
+            v, desc, th = cpu_bfs_rate(A, bfs_roots(A)[:8], 15.0)
+            result["cpu_baseline"] = {"value": v, "unit": "GTEPS", "cores": th, "kind": "port",
+                                      "sample": desc + " (single-source BFS of the oracle's C restatement; the "
+                                                       "multi-source loop does the same work per root)"
+                                      if args.workload == "msbfs22" else desc}
         else:
             v, desc, th = cpu_spgemm_rate(A, 15.0)
             result["cpu_baseline"] = {"value": v, "unit": "Gmults/s", "cores": th, "kind": "port",
@@ -524,14 +613,15 @@ def run_ours(args, world, rank, local):
     line = {
         "metric": result["metric"], "value": result["value"], "unit": result["unit"], "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": result["ms_per_step"], "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.workload != "bfs20" else "int64",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.workload.startswith("spgemm") else "int64",
         "data": "synthetic (seeded R-MAT, numpy generator)",
         "config": {"workload": args.workload, "scale": scale, "edge_factor": ef, "seed": SEED,
                    "rmat_abcd": [0.57, 0.19, 0.19, 0.05], "index": "int64",
                    "phase_budget_nnz": budget, "l2": "inputs and outputs larger than L2 (129 MB)",
                    "parallelism": f"replicas x{world}", **({"b_columns": args.bcols} if args.bcols else {})},
     }
-    for k in ("roofline", "cpu_baseline", "e2e", "gpu_launches", "clocks", "spgemm", "exact_two_phase", "mcl", "bfs"):
+    for k in ("roofline", "cpu_baseline", "e2e", "gpu_launches", "clocks", "spgemm", "exact_two_phase", "mcl", "bfs",
+              "msbfs"):
         if k in result:
             line[k] = result[k]
     if rank == 0:
@@ -544,7 +634,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["spgemm20", "bfs20", "spgemm14"], default="spgemm20")
+    ap.add_argument("--workload", choices=["spgemm20", "bfs20", "spgemm14", "msbfs22"], default="spgemm20")
     ap.add_argument("--phase-nnz", type=int, default=3 << 30)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mcl", action="store_true", help="skip the MCL exact-vs-learned comparison")

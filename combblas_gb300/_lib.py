@@ -70,6 +70,12 @@ class gbc_bfs_stats(C.Structure):
     ]
 
 
+class gbc_msbfs_stats(C.Structure):
+    _fields_ = [
+        ("levels", C.c_int64), ("reached", C.c_int64), ("edges", C.c_int64), ("ms", C.c_double),
+    ]
+
+
 _lib = None
 
 # name -> (restype, argtypes)
@@ -132,6 +138,8 @@ _SIGS.update({
                                                   C.POINTER(C.c_int32), C.c_void_p]),
     "gbc_bfs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.POINTER(gbc_bfs_stats),
                           C.c_int]),
+    "gbc_msbfs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int,
+                            C.POINTER(gbc_msbfs_stats)]),
 })
 
 # entry points added by later modules register here (see extend_signatures)

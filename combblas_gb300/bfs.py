@@ -1,6 +1,8 @@
 """SpMSpV over SelectMin and the BFS built on it -- host mirror of
 ``SpMXSpV_Bucket`` (SpImpl.cpp:389) and the BFS_CSC level loop of
-Applications/SpMSpV-IPDPS2017/SpMSpVBench.cpp:128-156.  GPU only."""
+Applications/SpMSpV-IPDPS2017/SpMSpVBench.cpp:128-156 -- plus the
+multi-source BFS of the Select2ndMin SpGEMM loop in
+Applications/Ordering/MD.cpp:211-217.  GPU only."""
 from __future__ import annotations
 
 import ctypes as C
@@ -73,3 +75,19 @@ def bfs_device(graph: Graph, source: int, parents_ptr: int, levels_ptr: int):
     L.check(L.lib().gbc_bfs(graph.ctx.h, graph.h, int(source), C.c_void_p(parents_ptr), C.c_void_p(levels_ptr),
                             C.byref(st), L.GBC_DEVICE))
     return st
+
+
+def msbfs(graph: Graph, roots, parents_ptr: int | None = None):
+    """BFS from every root at once (F_{l+1} = A * F_l masked by visited,
+    Select2ndMin, values = row ids).  Returns (parents int64[len(roots), n]
+    or None when written to the device buffer at ``parents_ptr``, stats)."""
+    roots = np.ascontiguousarray(roots, np.int64)
+    st = L.gbc_msbfs_stats()
+    if parents_ptr is None:
+        parents = np.empty((len(roots), graph.n), np.int64)
+        L.check(L.lib().gbc_msbfs(graph.ctx.h, graph.h, roots.ctypes.data, len(roots), parents.ctypes.data,
+                                  L.GBC_HOST, C.byref(st)))
+        return parents, st
+    L.check(L.lib().gbc_msbfs(graph.ctx.h, graph.h, roots.ctypes.data, len(roots), C.c_void_p(parents_ptr),
+                              L.GBC_DEVICE, C.byref(st)))
+    return None, st

@@ -46,6 +46,16 @@ struct Graph {
     int64_t *g_parents = nullptr, *g_levels = nullptr;  // pointers baked into the graph
     bool bfs_ready = false;
     int policy = 0;  // direction policy (see gbc_graph_set_policy)
+    // multi-source BFS state, sized for ms_roots roots (allocated on use)
+    int64_t ms_roots = 0;
+    int32_t *ms_cand = nullptr;       // [roots * n] candidate parent per (root, vertex)
+    uint32_t *ms_visited = nullptr;   // [roots * n / 32]
+    int64_t *ms_front[2] = {nullptr, nullptr};  // frontier entries (root << 32 | vertex)
+    int64_t *ms_ctl = nullptr;        // device control block (MS_*)
+    int64_t *h_ms_ctl = nullptr;      // pinned mirror
+    cudaGraphExec_t ms_exec = nullptr;
+    long long ms_kernels = 0;
+    int64_t *ms_g_parents = nullptr;  // parents pointer baked into ms_exec
 };
 
 // control block layout
@@ -701,6 +711,310 @@ static int bfs_device(Graph *g, int64_t source, int64_t *parents, int64_t *level
     return GBC_OK;
 }
 
+// ------------------------------------------------------ multi-source BFS
+// Many BFS trees at once, the Select2ndMin SpGEMM loop of the reference's
+// multi-source traversals (Applications/Ordering/MD.cpp:211-217,
+// Applications/BetwCent.cpp:185-186):
+//     F_{l+1} = (A * F_l) masked by the complement of visited,
+// where column r of F holds root r's frontier with every value equal to its
+// own row id, so (A*F)(u, r) = min over frontier neighbours v of v: the
+// parent.  Because min is order independent the masked product can go
+// straight into a dense per-(root, vertex) accumulator (cand, atomicMin)
+// with the visited test in front of it -- no symbolic pass and no output
+// sizing -- and every (root, vertex) entering the next frontier is appended
+// once (the atomicMin that saw the empty candidate).  F is held as a list
+// of (root << 32 | vertex) entries; blocks take fixed chunks of it and
+// flatten their edges across the block.
+enum {
+    MS_NF = 0,       // current frontier entries
+    MS_NNEXT = 1,    // next frontier entries
+    MS_LEVEL = 2,    // levels done
+    MS_WORK = 3,     // chunk counter of the expand kernel
+    MS_EDGES = 4,    // sum of degrees of reached (root, vertex) pairs
+    MS_REACHED = 5,  // reached (root, vertex) pairs
+    MS_CUR = 6,      // which frontier buffer is current
+    MS_N
+};
+constexpr int kMsCtlWords = 8;  // then the frontier pointer table [2]
+
+__global__ void __launch_bounds__(kThreads) k_ms_expand(const uint32_t *cp32, const int32_t *row, int64_t n,
+                                                        const uint32_t *visited, int32_t *cand, int64_t *ctl,
+                                                        int64_t *const *fronts)
+{
+    __shared__ int32_t s_v[kThreads];
+    __shared__ int64_t s_root[kThreads];
+    __shared__ int64_t s_base[kThreads];  // root * n
+    __shared__ uint32_t s_st[kThreads];
+    __shared__ int32_t s_off[kThreads + 1];
+    __shared__ int64_t q[kQueue];
+    __shared__ int s_qn;
+    __shared__ unsigned long long s_gbase;
+    __shared__ int64_t s_chunk;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int cur = (int)ctl[MS_CUR];
+    const int64_t *front = fronts[cur];
+    int64_t *next = fronts[cur ^ 1];
+    const int64_t nf = ctl[MS_NF];
+    if (tid == 0) s_qn = 0;
+    __syncthreads();
+    for (;;) {
+        if (tid == 0) s_chunk = (int64_t)atomicAdd((unsigned long long *)&ctl[MS_WORK], 1ull);
+        __syncthreads();
+        const int64_t f = s_chunk * kThreads + tid;
+        if (s_chunk * kThreads >= nf) break;
+        int len = 0;
+        if (f < nf) {
+            const int64_t x = front[f];
+            const int32_t v = (int32_t)(x & 0xffffffff);
+            s_v[tid] = v;
+            s_root[tid] = x >> 32;
+            s_base[tid] = (x >> 32) * n;
+            s_st[tid] = cp32[v];
+            len = (int)(cp32[v + 1] - cp32[v]);
+        }
+        int64_t tot;
+        const int off = (int)block_exclusive_sum64(len, &tot);
+        s_off[tid] = off;
+        if (tid == kThreads - 1) s_off[kThreads] = off + len;
+        __syncthreads();
+        const int L = (int)tot;
+        for (int e0 = 0; e0 < L; e0 += kThreads) {
+            const int e = e0 + tid;
+            bool fresh = false;
+            int64_t entry = 0;
+            if (e < L) {
+                int lo = 0, hi = kThreads;
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (s_off[mid] <= e) lo = mid; else hi = mid;
+                }
+                const int32_t u = row[s_st[lo] + (e - s_off[lo])];
+                const int64_t idx = s_base[lo] + u;
+                if (!(visited[idx >> 5] & (1u << (idx & 31)))) {
+                    const int32_t v = s_v[lo];
+                    if (v < cand[idx]) {
+                        const int32_t old = atomicMin(&cand[idx], v);
+                        fresh = old == kNoCand;
+                        entry = (s_root[lo] << 32) | (uint32_t)u;
+                    }
+                }
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, fresh);
+            if (m) {
+                int slot = 0;
+                if (lane == __ffs(m) - 1) slot = atomicAdd(&s_qn, __popc(m));
+                slot = __shfl_sync(0xffffffffu, slot, __ffs(m) - 1);
+                if (fresh) q[slot + __popc(m & ((1u << lane) - 1))] = entry;
+            }
+            __syncthreads();
+            if (s_qn > kQueue - kThreads) {
+                if (tid == 0) s_gbase = atomicAdd((unsigned long long *)&ctl[MS_NNEXT], (unsigned long long)s_qn);
+                __syncthreads();
+                for (int k = tid; k < s_qn; k += kThreads) next[s_gbase + k] = q[k];
+                __syncthreads();
+                if (tid == 0) s_qn = 0;
+                __syncthreads();
+            }
+        }
+        __syncthreads();
+    }
+    if (s_qn > 0) {
+        if (tid == 0) s_gbase = atomicAdd((unsigned long long *)&ctl[MS_NNEXT], (unsigned long long)s_qn);
+        __syncthreads();
+        for (int k = tid; k < s_qn; k += kThreads) next[s_gbase + k] = q[k];
+    }
+}
+
+// parents.Set(fringe) for the new frontier entries, visited update and the
+// reached-edge sums.
+__global__ void k_ms_finalize(int32_t *cand, uint32_t *visited, int64_t *parents, const uint32_t *cp32, int64_t n,
+                              int64_t *ctl, int64_t *const *fronts)
+{
+    const int64_t *next = fronts[ctl[MS_CUR] ^ 1];
+    const int64_t nn = ctl[MS_NNEXT];
+    int64_t deg = 0, reached = 0;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < nn; i += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t x = next[i];
+        const int32_t u = (int32_t)(x & 0xffffffff);
+        const int64_t idx = (x >> 32) * n + u;
+        parents[idx] = cand[idx];
+        cand[idx] = kNoCand;
+        atomicOr(&visited[idx >> 5], 1u << (idx & 31));
+        deg += cp32[u + 1] - cp32[u];
+        ++reached;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        deg += __shfl_xor_sync(0xffffffffu, deg, o);
+        reached += __shfl_xor_sync(0xffffffffu, reached, o);
+    }
+    if ((threadIdx.x & 31) == 0 && reached) {
+        atomicAdd((unsigned long long *)&ctl[MS_EDGES], (unsigned long long)deg);
+        atomicAdd((unsigned long long *)&ctl[MS_REACHED], (unsigned long long)reached);
+    }
+}
+
+__global__ void k_ms_advance(int64_t *ctl)
+{
+    if (ctl[MS_NF] == 0) return;
+    ctl[MS_NF] = ctl[MS_NNEXT];
+    ctl[MS_NNEXT] = 0;
+    ctl[MS_WORK] = 0;
+    ctl[MS_CUR] ^= 1;
+    ctl[MS_LEVEL] += 1;
+}
+
+// Roots: frontier entries, visited bits, parents[root] = root (as the
+// reference's visited matrix starts with the sources), degree sums.
+__global__ void k_ms_init(const int64_t *roots, int64_t nroots, int64_t n, const uint32_t *cp32, uint32_t *visited,
+                          int64_t *parents, int64_t *ctl, int64_t *const *fronts)
+{
+    const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (r >= nroots) return;
+    const int64_t v = roots[r];
+    const int64_t idx = r * n + v;
+    fronts[0][r] = (r << 32) | v;
+    parents[idx] = v;
+    atomicOr(&visited[idx >> 5], 1u << (idx & 31));
+    atomicAdd((unsigned long long *)&ctl[MS_EDGES], (unsigned long long)(cp32[v + 1] - cp32[v]));
+    atomicAdd((unsigned long long *)&ctl[MS_REACHED], 1ull);
+}
+
+__global__ void k_fill_i32(int32_t *p, int64_t n, int32_t v)
+{
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+        p[i] = v;
+}
+
+static int64_t *const *ms_fronts_dev(Graph *g) { return reinterpret_cast<int64_t *const *>(g->ms_ctl + kMsCtlWords); }
+
+static void ms_free(Graph *g)
+{
+    Context *c = g->ctx;
+    if (g->ms_exec) cudaGraphExecDestroy(g->ms_exec);
+    g->ms_exec = nullptr;
+    device_free(c, g->ms_cand);
+    device_free(c, g->ms_visited);
+    device_free(c, g->ms_front[0]);
+    device_free(c, g->ms_front[1]);
+    device_free(c, g->ms_ctl);
+    if (g->h_ms_ctl) cudaFreeHost(g->h_ms_ctl);
+    g->ms_cand = nullptr;
+    g->ms_visited = nullptr;
+    g->ms_front[0] = g->ms_front[1] = nullptr;
+    g->ms_ctl = nullptr;
+    g->h_ms_ctl = nullptr;
+    g->ms_roots = 0;
+}
+
+static int ms_alloc(Graph *g, int64_t nroots)
+{
+    if (g->ms_roots >= nroots) return GBC_OK;
+    cudaStreamSynchronize(g->ctx->stream);
+    ms_free(g);
+    Context *ctx = g->ctx;
+    const int64_t cells = nroots * g->n;
+    GBC_TRY(device_alloc(ctx, (void **)&g->ms_cand, cells * sizeof(int32_t) + 16));
+    GBC_TRY(device_alloc(ctx, (void **)&g->ms_visited, ((cells + 31) / 32 + 1) * sizeof(uint32_t)));
+    // a (root, vertex) pair enters a frontier at most once
+    GBC_TRY(device_alloc(ctx, (void **)&g->ms_front[0], cells * sizeof(int64_t) + 16));
+    GBC_TRY(device_alloc(ctx, (void **)&g->ms_front[1], cells * sizeof(int64_t) + 16));
+    GBC_TRY(device_alloc(ctx, (void **)&g->ms_ctl, (kMsCtlWords + 4) * sizeof(int64_t)));
+    GBC_CUDA_TRY(cudaMallocHost(&g->h_ms_ctl, (kMsCtlWords + 4) * sizeof(int64_t)));
+    void *tab[2] = {g->ms_front[0], g->ms_front[1]};
+    GBC_CUDA_TRY(cudaMemcpyAsync(g->ms_ctl + kMsCtlWords, tab, sizeof(tab), cudaMemcpyHostToDevice, ctx->stream));
+    k_fill_i32<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(g->ms_cand, cells, kNoCand);
+    note_launch();
+    GBC_CUDA_TRY(cudaGetLastError());
+    g->ms_roots = nroots;
+    return GBC_OK;
+}
+
+static int ms_launch_level(Graph *g, int64_t *parents, cudaStream_t s)
+{
+    const int grid = g->ctx->num_sms * 4;
+    k_ms_expand<<<grid, kThreads, 0, s>>>(g->cp32, g->row, g->n, g->ms_visited, g->ms_cand, g->ms_ctl,
+                                          ms_fronts_dev(g));
+    k_ms_finalize<<<grid, 256, 0, s>>>(g->ms_cand, g->ms_visited, parents, g->cp32, g->n, g->ms_ctl,
+                                       ms_fronts_dev(g));
+    k_ms_advance<<<1, 1, 0, s>>>(g->ms_ctl);
+    note_launches(3);
+    GBC_CUDA_TRY(cudaGetLastError());
+    return GBC_OK;
+}
+
+static int ms_level_graph(Graph *g, int64_t *parents)
+{
+    if (g->ms_exec && g->ms_g_parents == parents) return GBC_OK;
+    if (g->ms_exec) {
+        cudaGraphExecDestroy(g->ms_exec);
+        g->ms_exec = nullptr;
+    }
+    cudaStream_t cs;
+    GBC_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t graph;
+    const long long c0 = launch_count();
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(cs);
+        return fail(GBC_ECUDA, std::string("capture: ") + cudaGetErrorString(e));
+    }
+    int rc = ms_launch_level(g, parents, cs);
+    e = cudaStreamEndCapture(cs, &graph);
+    g->ms_kernels = launch_count() - c0;
+    note_launches(-g->ms_kernels);
+    cudaStreamDestroy(cs);
+    if (rc != GBC_OK) return rc;
+    if (e != cudaSuccess) return fail(GBC_ECUDA, std::string("capture end: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&g->ms_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(GBC_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    g->ms_g_parents = parents;
+    return GBC_OK;
+}
+
+// parents: device [nroots * n], root-major.
+static int msbfs_device(Graph *g, const int64_t *d_roots, int64_t nroots, int64_t *parents, gbc_msbfs_stats *st)
+{
+    Context *ctx = g->ctx;
+    cudaStream_t s = ctx->stream;
+    GBC_TRY(ms_alloc(g, nroots));
+    const int64_t cells = nroots * g->n;
+    cudaEventRecord(ctx->ev[5], s);
+    GBC_CUDA_TRY(cudaMemsetAsync(parents, 0xff, cells * sizeof(int64_t), s));  // -1: unreached
+    GBC_CUDA_TRY(cudaMemsetAsync(g->ms_visited, 0, ((cells + 31) / 32 + 1) * sizeof(uint32_t), s));
+    GBC_CUDA_TRY(cudaMemsetAsync(g->ms_ctl, 0, kMsCtlWords * sizeof(int64_t), s));
+    k_ms_init<<<(unsigned)((nroots + 255) / 256), 256, 0, s>>>(d_roots, nroots, g->n, g->cp32, g->ms_visited,
+                                                                parents, g->ms_ctl, ms_fronts_dev(g));
+    note_launch();
+    int64_t nf = nroots;
+    GBC_CUDA_TRY(cudaMemcpyAsync(g->ms_ctl + MS_NF, &nf, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    GBC_CUDA_TRY(cudaGetLastError());
+    GBC_TRY(ms_level_graph(g, parents));
+    const int batch = 2;
+    for (int64_t lvl = 0; lvl <= g->n + 1; lvl += batch) {
+        for (int k = 0; k < batch; ++k) {
+            GBC_CUDA_TRY(cudaGraphLaunch(g->ms_exec, s));
+            note_launches(g->ms_kernels);
+        }
+        GBC_CUDA_TRY(
+            cudaMemcpyAsync(g->h_ms_ctl, g->ms_ctl, kMsCtlWords * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        GBC_CUDA_TRY(cudaStreamSynchronize(s));
+        if (g->h_ms_ctl[MS_NF] == 0) break;
+    }
+    cudaEventRecord(ctx->ev[6], s);
+    GBC_CUDA_TRY(cudaEventSynchronize(ctx->ev[6]));
+    if (st) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev[5], ctx->ev[6]);
+        st->levels = g->h_ms_ctl[MS_LEVEL];
+        st->reached = g->h_ms_ctl[MS_REACHED];
+        st->edges = g->h_ms_ctl[MS_EDGES] / 2;
+        st->ms = ms;
+    }
+    return GBC_OK;
+}
+
 }  // namespace gbc
 
 using namespace gbc;
@@ -757,6 +1071,7 @@ int gbc_graph_destroy(gbc_graph *g)
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     if (g->level_exec) cudaGraphExecDestroy(g->level_exec);
+    ms_free(g);
     device_free(c, g->cp);
     device_free(c, g->cp32);
     device_free(c, g->row);
@@ -864,6 +1179,34 @@ int gbc_bfs(gbc_context *ctx, gbc_graph *g, int64_t source, int64_t *parents, in
     if (where == GBC_HOST) {
         if (parents) GBC_CUDA_TRY(cudaMemcpyAsync(parents, dp, g->n * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
         if (levels) GBC_CUDA_TRY(cudaMemcpyAsync(levels, dl, g->n * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        GBC_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    return GBC_OK;
+}
+
+int gbc_msbfs(gbc_context *ctx, gbc_graph *g, const int64_t *roots, int64_t nroots, int64_t *parents, int where,
+              gbc_msbfs_stats *st)
+{
+    if (!ctx || !g || !roots || !parents) return fail(GBC_EINVAL, "null argument");
+    if (nroots <= 0 || nroots >= (int64_t(1) << 31)) return fail(GBC_EINVAL, "root count out of range");
+    if (where != GBC_HOST && where != GBC_DEVICE) return fail(GBC_EINVAL, "bad memory location");
+    if (g->n >= (int64_t(1) << 31) || nroots > (int64_t(1) << 62) / std::max<int64_t>(g->n, 1))
+        return fail(GBC_EOVERFLOW, "roots x vertices too large");
+    for (int64_t r = 0; r < nroots; ++r)
+        if (roots[r] < 0 || roots[r] >= g->n) return fail(GBC_EINVAL, "root out of range");
+    GBC_CUDA_TRY(cudaSetDevice(ctx->device));
+    g->ctx = ctx;
+    cudaStream_t s = ctx->stream;
+    Workspace ws(ctx);
+    int64_t *d_roots = nullptr;
+    GBC_TRY(ws.alloc_n(&d_roots, nroots));
+    GBC_CUDA_TRY(cudaMemcpyAsync(d_roots, roots, nroots * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    const int64_t cells = nroots * g->n;
+    int64_t *dp = parents;
+    if (where == GBC_HOST) GBC_TRY(ws.alloc_n(&dp, cells));
+    GBC_TRY(msbfs_device(g, d_roots, nroots, dp, st));
+    if (where == GBC_HOST) {
+        GBC_CUDA_TRY(cudaMemcpyAsync(parents, dp, cells * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
         GBC_CUDA_TRY(cudaStreamSynchronize(s));
     }
     return GBC_OK;

@@ -278,6 +278,25 @@ int gbc_spmspv_select2ndmin_i64(gbc_context *ctx, gbc_graph *g, const int32_t *i
 int gbc_bfs(gbc_context *ctx, gbc_graph *g, int64_t source, int64_t *parents, int64_t *levels, gbc_bfs_stats *st,
             int where);
 
+/* Multi-source BFS: nroots BFS trees over the graph at once, the
+ * Select2ndMin SpGEMM loop of the reference's multi-source traversals
+ * (Applications/Ordering/MD.cpp:211-217 getReachesSPMM, BetwCent.cpp:185-186):
+ * F_{l+1} = (A * F_l) masked by !visited, F's column r holding root r's
+ * frontier with values equal to their row ids.  parents[r * n + v] (root-
+ * major, int64) = the smallest frontier neighbour through which v was
+ * reached from roots[r], roots[r] itself for the root (the reference's
+ * visited matrix starts with the sources), -1 if unreached.  roots is a host
+ * array; parents is where-located and holds nroots * n entries. */
+typedef struct {
+    int64_t levels;   /* loop iterations until every frontier was empty */
+    int64_t reached;  /* reached (root, vertex) pairs, roots included */
+    int64_t edges;    /* sum over roots of undirected edges of the reached vertices */
+    double ms;        /* device time */
+} gbc_msbfs_stats;
+
+int gbc_msbfs(gbc_context *ctx, gbc_graph *g, const int64_t *roots, int64_t nroots, int64_t *parents, int where,
+              gbc_msbfs_stats *st);
+
 /* Allocation-free form of gbc_spmspv_select2ndmin_i64, for callers that
  * cannot call cudaMalloc where they need the product: code running while
  * another component has reserved the device's free memory, latency-critical

@@ -252,6 +252,65 @@ def port_bfs(A, source: int, with_levels: bool = True):
     return parents, levels, it
 
 
+def msbfs_loop(A, roots, multiply):
+    """Multi-source BFS as the reference's Select2ndMin SpGEMM loop
+    (Applications/Ordering/MD.cpp:200-217): F starts with F(root_r, r) =
+    root_r and visited = the sources; each level F = multiply(A, F) (a
+    Select2ndMin product returning a CSC), then EWiseMult(F, visited,
+    exclude=true), visited += F, and every value becomes its own row id.
+    parents[r, v] = the product's value when v entered; parents[r, root_r]
+    = root_r; -1 if never reached.  Returns (parents, levels)."""
+    n = A.ncol
+    R = len(roots)
+    roots = np.asarray(roots, np.int64)
+    parents = np.full((R, n), -1, np.int64)
+    visited = np.zeros((R, n), bool)
+    visited[np.arange(R), roots] = True
+    parents[np.arange(R), roots] = roots
+
+    class _F:
+        pass
+
+    F = _F()
+    F.nrow, F.ncol = n, R
+    F.colptr = np.arange(R + 1, dtype=np.int64)
+    F.rowidx = roots.copy()
+    F.values = roots.copy()
+    levels = 0
+    while F.rowidx.size:
+        cp, rows, vals = multiply(A, F)
+        cols = np.repeat(np.arange(R, dtype=np.int64), np.diff(cp))
+        keep = ~visited[cols, rows]
+        rows, cols, vals = rows[keep], cols[keep], vals[keep]
+        visited[cols, rows] = True
+        parents[cols, rows] = vals
+        F = _F()
+        F.nrow, F.ncol = n, R
+        F.colptr = np.zeros(R + 1, np.int64)
+        F.colptr[1:] = np.cumsum(np.bincount(cols, minlength=R))
+        F.rowidx = rows.astype(np.int64)
+        F.values = rows.astype(np.int64)
+        levels += 1
+    return parents, levels
+
+
+def port_msbfs(A, roots):
+    """msbfs_loop over the C restatement's Select2ndMin product."""
+    Ap = A.with_values(np.ones(A.nnz, np.int64))
+    return msbfs_loop(Ap, roots, lambda X, F: port_spgemm(X, F, SR_SELECT2NDMIN_I64))
+
+
+def ref_msbfs(A, roots):
+    """msbfs_loop over the reference's own PSpGEMM<Select2ndMinSR> on a 1x1 grid."""
+    Ap = A.with_values(np.ones(A.nnz, np.int64))
+
+    def mult(X, F):
+        r, c, v, _ = ref_spgemm(X, F, SR_SELECT2NDMIN_I64, V_PSPGEMM)
+        return tuples_to_csc(r, c, v, F.ncol)
+
+    return msbfs_loop(Ap, roots, mult)
+
+
 def port_mcl_select(Ccp, Cri, Cv, thr: float, select: int):
     lib = _port()
     n = len(Ccp) - 1

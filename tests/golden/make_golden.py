@@ -155,6 +155,15 @@ def main(ref_root: str):
     d["spmspv/rmat8/x_val"] = xv
     d["spmspv/rmat8/y_ind"] = yr
     d["spmspv/rmat8/y_val"] = yv
+    # multi-source BFS (MD.cpp's Select2ndMin SpGEMM loop) on rmat8 and torus
+    for name, Mm in (("rmat8", rm), ("torus", torus)):
+        P = Mm.with_values(None)
+        deg = np.diff(P.colptr)
+        roots = np.random.default_rng(11).choice(np.nonzero(deg)[0], 12, replace=False).astype(np.int64)
+        par, lv = O.ref_msbfs(P, roots)
+        d[f"msbfs/{name}/roots"] = roots
+        d[f"msbfs/{name}/parents"] = par
+        d[f"msbfs/{name}/levels"] = np.array(lv)
     # MCL expansion + prune/select
     M = G.mcl_planted(4096, 256, 10, 3, seed=5)
     put_mat(d, "in/mcl4096", M)

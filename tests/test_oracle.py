@@ -146,3 +146,21 @@ def test_oracle_detects_planted_error(oracle_lib, golden):
     vals[len(vals) // 2] *= 1.0 + 1e-9
     with pytest.raises(AssertionError):
         check_csc(cp, rows, vals, golden, "prod/rmat8/AA_hash_sorted/0", 0, O.V_HASH_SORTED, A.ncol, O, True)
+
+
+def test_port_msbfs(oracle_lib, golden):
+    """The multi-source BFS loop over the C restatement reproduces the
+    reference's own PSpGEMM<Select2ndMin> loop (golden), and away from the
+    roots its parents are the single-source BFS parents."""
+    O = oracle_lib
+    for name in ("rmat8", "torus"):
+        M = golden_matrix(golden, name).with_values(None)
+        roots = golden[f"msbfs/{name}/roots"]
+        par, lv = O.port_msbfs(M, roots)
+        assert np.array_equal(par, golden[f"msbfs/{name}/parents"]), name
+        assert lv == int(golden[f"msbfs/{name}/levels"])
+        for r, s in enumerate(roots):
+            single, _, _ = O.port_bfs(M, int(s))
+            other = np.arange(M.ncol) != s
+            assert np.array_equal(par[r][other], single[other]), (name, s)
+            assert par[r][s] == s
