@@ -1,0 +1,307 @@
+/* Drop-in GPU forms of CombBLAS's node-local multiplies.
+ *
+ * Include this header after the CombBLAS headers (it names
+ * combblas::SpDCCols, SpCCols, SpTuples, Csc, PreAllocatedSPA and the stock
+ * semirings) and call gbcomb::X where the reference calls combblas::X:
+ *
+ *   gbcomb::LocalHybridSpGEMM<SR, NTO>(A, B, clearA, clearB)   mtSpGEMM.h:213-217
+ *   gbcomb::LocalSpGEMM<SR, NTO>(A, B, clearA, clearB)         mtSpGEMM.h:74-78
+ *   gbcomb::LocalSpGEMMHash<SR, NTO>(A, B, clearA, clearB, sort) mtSpGEMM.h:463-467
+ *   gbcomb::LocalHybridSpGEMM<SR, NTO>(SpCCols A, SpCCols B, ...)  mtSpGEMM.h:1142-1152
+ *   gbcomb::SpMXSpV<SR>(Csc, mA, indx, numx, veclen, indy, numy, SPA)  SpImpl.h:115-124
+ *
+ * Same arguments, same ownership (inputs borrowed; clearA / clearB delete
+ * them; the returned SpTuples owns a tuple array from ::operator new with
+ * isOpNew = true; an empty operand gives new SpTuples(0, m, n); SpMXSpV
+ * appends to indy / numy), same results.  A call runs on the GPU when its
+ * (semiring, index, value) combination is registered in gbcomb::semiring_of
+ * and the index type is int64_t; every other combination falls through to
+ * the reference template unchanged.  A nonzero status from the C ABI is
+ * reported on stderr and thrown as std::runtime_error (the reference's
+ * local kernels have no error path; its distributed layer aborts).
+ *
+ * Stock semirings registered here: PlusTimesSRing<double,double>,
+ * <float,float>, <int64_t,int64_t>; MinPlusSRing<double,double>,
+ * <int64_t,int64_t>.  Application-defined semirings (Select2ndMinSR of
+ * FastSV.h / CC.h, SelectMinSR of SpMSpVBench.cpp, boolean or-and) are
+ * registered by the application with GBCOMB_REGISTER_SEMIRING.
+ */
+#pragma once
+
+#include <cstdint>
+#include <cstdio>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <type_traits>
+#include <vector>
+
+#include "../gbcomb.h"
+
+namespace gbcomb {
+
+// (semiring, value type) codes of the C ABI for a CombBLAS semiring type;
+// sr < 0: not registered (the reference template runs).
+template <class SR>
+struct semiring_of {
+    static constexpr int sr = -1;
+    static constexpr int vt = -1;
+};
+
+template <int VT>
+struct value_c;
+template <>
+struct value_c<GBC_F64> {
+    typedef double type;
+};
+template <>
+struct value_c<GBC_F32> {
+    typedef float type;
+};
+template <>
+struct value_c<GBC_I64> {
+    typedef int64_t type;
+};
+template <>
+struct value_c<GBC_BOOL> {
+    typedef bool type;
+};
+
+}  // namespace gbcomb
+
+#define GBCOMB_REGISTER_SEMIRING(SRTYPE, SR_CODE, VT_CODE) \
+    namespace gbcomb {                                     \
+    template <>                                            \
+    struct semiring_of<SRTYPE> {                           \
+        static constexpr int sr = (SR_CODE);               \
+        static constexpr int vt = (VT_CODE);               \
+    };                                                     \
+    }
+
+// SRTYPE must be a single token or parenthesis-free name: use a typedef for
+// a template with several arguments, e.g.
+//   typedef combblas::Select2ndMinSR<int64_t, int64_t> S2M;
+//   GBCOMB_REGISTER_SEMIRING(S2M, GBC_SR_SELECT2NDMIN, GBC_I64)
+
+namespace gbcomb {
+
+#define GBCOMB_STOCK(T1, T2, SRT, SR_CODE, VT_CODE) \
+    template <>                                      \
+    struct semiring_of<combblas::SRT<T1, T2>> {      \
+        static constexpr int sr = (SR_CODE);         \
+        static constexpr int vt = (VT_CODE);         \
+    };
+GBCOMB_STOCK(double, double, PlusTimesSRing, GBC_SR_PLUSTIMES, GBC_F64)
+GBCOMB_STOCK(float, float, PlusTimesSRing, GBC_SR_PLUSTIMES, GBC_F32)
+GBCOMB_STOCK(int64_t, int64_t, PlusTimesSRing, GBC_SR_PLUSTIMES, GBC_I64)
+GBCOMB_STOCK(double, double, MinPlusSRing, GBC_SR_MINPLUS, GBC_F64)
+GBCOMB_STOCK(int64_t, int64_t, MinPlusSRing, GBC_SR_MINPLUS, GBC_I64)
+#undef GBCOMB_STOCK
+
+namespace detail {
+
+inline void check(int rc, const char *what)
+{
+    if (rc != GBC_OK) {
+        std::string msg = std::string(what) + ": " + gbc_last_error();
+        std::fprintf(stderr, "gbcomb: %s\n", msg.c_str());
+        throw std::runtime_error(msg);
+    }
+}
+
+// One library context per process (device 0 unless gbcomb::set_device ran
+// first); the reference calls its local kernels from a single thread.
+inline gbc_context *&context_slot()
+{
+    static gbc_context *ctx = nullptr;
+    return ctx;
+}
+
+inline int &device_slot()
+{
+    static int dev = 0;
+    return dev;
+}
+
+inline gbc_context *context()
+{
+    gbc_context *&c = context_slot();
+    if (!c) check(gbc_context_create(&c, device_slot()), "gbc_context_create");
+    return c;
+}
+
+// Offload test: registered semiring, int64 indices, every value type equal
+// to the semiring's.
+template <class SR, class NTO, class IT, class NT1, class NT2>
+constexpr bool offloaded()
+{
+    if constexpr (semiring_of<SR>::sr < 0) {
+        return false;
+    } else {
+        typedef typename value_c<semiring_of<SR>::vt>::type V;
+        return std::is_same<IT, int64_t>::value && std::is_same<NT1, V>::value && std::is_same<NT2, V>::value &&
+               std::is_same<NTO, V>::value;
+    }
+}
+
+template <class IT, class NT>
+gbc_matrix view(const combblas::SpDCCols<IT, NT> &M)
+{
+    gbc_matrix g{};
+    g.nrow = M.getnrow();
+    g.ncol = M.getncol();
+    const combblas::Dcsc<IT, NT> *d = M.GetDCSC();
+    g.nzc = d ? d->nzc : 0;
+    g.nnz = d ? d->nz : 0;
+    g.cp = d ? d->cp : nullptr;
+    g.jc = d ? d->jc : nullptr;
+    g.ir = d ? d->ir : nullptr;
+    g.num = d ? d->numx : nullptr;
+    g.where = GBC_HOST;
+    return g;
+}
+
+template <class IT, class NT>
+gbc_matrix view(const combblas::SpCCols<IT, NT> &M)
+{
+    gbc_matrix g{};
+    g.nrow = M.getnrow();
+    g.ncol = M.getncol();
+    const combblas::Csc<IT, NT> *c = M.GetCSC();
+    g.nzc = M.getncol();
+    g.nnz = c ? c->nz : 0;
+    g.cp = c ? c->jc : nullptr;  // Csc::jc holds the column pointers
+    g.jc = nullptr;
+    g.ir = c ? c->ir : nullptr;
+    g.num = c ? c->num : nullptr;
+    g.where = GBC_HOST;
+    return g;
+}
+
+// Run the product and wrap it as the reference does: (row, col, value)
+// tuples in column-major order, rows ascending within a column.
+template <class SR, class NTO, class IT>
+combblas::SpTuples<IT, NTO> *multiply(const gbc_matrix &A, const gbc_matrix &B, int sorted)
+{
+    gbc_spgemm_opts opt{GBC_SIZING_EXACT, sorted, 1, 0, -1, -1};
+    gbc_result *C = nullptr;
+    check(gbc_spgemm(context(), semiring_of<SR>::sr, semiring_of<SR>::vt, &A, &B, &opt, &C, nullptr), "gbc_spgemm");
+    int64_t nrow = 0, ncol = 0, nzc = 0, nnz = 0;
+    int vt = 0;
+    gbc_result_info(C, &nrow, &ncol, &nzc, &nnz, &vt);
+    std::vector<int64_t> cp(nzc + 1), jc(nzc), ir(nnz);
+    std::unique_ptr<NTO[]> num(new NTO[nnz > 0 ? nnz : 1]);  // NTO may be bool: no std::vector
+    int rc = gbc_result_copy(C, cp.data(), nzc ? jc.data() : nullptr, nnz ? ir.data() : nullptr,
+                             nnz ? static_cast<void *>(num.get()) : nullptr, GBC_HOST);
+    gbc_result_free(C);
+    check(rc, "gbc_result_copy");
+    typedef std::tuple<IT, IT, NTO> T;
+    T *tuples = static_cast<T *>(::operator new(sizeof(T) * (nnz > 0 ? nnz : 1)));
+    for (int64_t k = 0; k < nzc; ++k)
+        for (int64_t p = cp[k]; p < cp[k + 1]; ++p) new (tuples + p) T(ir[p], jc[k], num[p]);
+    return new combblas::SpTuples<IT, NTO>(nnz, (IT)A.nrow, (IT)B.ncol, tuples, true, true);
+}
+
+template <class SR, class NTO, class M1, class M2>
+auto run(const M1 &A, const M2 &B, bool clearA, bool clearB, int sorted)
+{
+    typedef decltype(A.getnrow()) IT;
+    const IT m = A.getnrow(), n = B.getncol();
+    combblas::SpTuples<IT, NTO> *out;
+    if (A.isZero() || B.isZero())
+        out = new combblas::SpTuples<IT, NTO>(0, m, n);
+    else
+        out = multiply<SR, NTO, IT>(view(A), view(B), sorted);
+    if (clearA) delete const_cast<M1 *>(&A);
+    if (clearB) delete const_cast<M2 *>(&B);
+    return out;
+}
+
+}  // namespace detail
+
+inline void set_device(int device) { detail::device_slot() = device; }
+
+template <class SR, class NTO, class IT, class NT1, class NT2>
+combblas::SpTuples<IT, NTO> *LocalHybridSpGEMM(const combblas::SpDCCols<IT, NT1> &A,
+                                               const combblas::SpDCCols<IT, NT2> &B, bool clearA, bool clearB,
+                                               IT *aux = nullptr)
+{
+    if constexpr (detail::offloaded<SR, NTO, IT, NT1, NT2>())
+        return detail::run<SR, NTO>(A, B, clearA, clearB, GBC_SORTED);
+    else
+        return combblas::LocalHybridSpGEMM<SR, NTO>(A, B, clearA, clearB, aux);
+}
+
+template <class SR, class NTO, class IT, class NT1, class NT2>
+combblas::SpTuples<IT, NTO> *LocalSpGEMM(const combblas::SpDCCols<IT, NT1> &A, const combblas::SpDCCols<IT, NT2> &B,
+                                         bool clearA, bool clearB)
+{
+    if constexpr (detail::offloaded<SR, NTO, IT, NT1, NT2>())
+        return detail::run<SR, NTO>(A, B, clearA, clearB, GBC_SORTED);
+    else
+        return combblas::LocalSpGEMM<SR, NTO>(A, B, clearA, clearB);
+}
+
+// sort = false asks for the reference's unsorted hash output; the GPU path
+// returns rows ascending either way (a valid unsorted order), and the
+// SpTuples is flagged sorted as the reference flags it.
+template <class SR, class NTO, class IT, class NT1, class NT2>
+combblas::SpTuples<IT, NTO> *LocalSpGEMMHash(const combblas::SpDCCols<IT, NT1> &A,
+                                             const combblas::SpDCCols<IT, NT2> &B, bool clearA, bool clearB,
+                                             bool sort = true)
+{
+    if constexpr (detail::offloaded<SR, NTO, IT, NT1, NT2>())
+        return detail::run<SR, NTO>(A, B, clearA, clearB, GBC_SORTED);
+    else
+        return combblas::LocalSpGEMMHash<SR, NTO>(A, B, clearA, clearB, sort);
+}
+
+template <class SR, class NTO, class IT, class NT1, class NT2>
+combblas::SpTuples<IT, NTO> *LocalHybridSpGEMM(const combblas::SpCCols<IT, NT1> &A,
+                                               const combblas::SpCCols<IT, NT2> &B, bool clearA, bool clearB)
+{
+    if constexpr (detail::offloaded<SR, NTO, IT, NT1, NT2>())
+        return detail::run<SR, NTO>(A, B, clearA, clearB, GBC_SORTED);
+    else
+        return combblas::LocalHybridSpGEMM<SR, NTO>(A, B, clearA, clearB);
+}
+
+// y = A x over a min-select semiring (registered with GBC_SR_SELECT2NDMIN /
+// GBC_I64): appended to indy / numy sorted by row, as SpMXSpV_Bucket does.
+template <class SR, class IT, class NUM, class IVT, class OVT>
+void SpMXSpV(const combblas::Csc<IT, NUM> &Acsc, int32_t mA, const int32_t *indx, const IVT *numx, int32_t veclen,
+             std::vector<int32_t> &indy, std::vector<OVT> &numy, combblas::PreAllocatedSPA<OVT> &SPA)
+{
+    constexpr bool gpu = semiring_of<SR>::sr == GBC_SR_SELECT2NDMIN && std::is_same<IT, int64_t>::value &&
+                         std::is_same<IVT, int64_t>::value && std::is_same<OVT, int64_t>::value;
+    if constexpr (!gpu) {
+        combblas::SpMXSpV<SR>(Acsc, mA, indx, numx, veclen, indy, numy, SPA);
+    } else {
+        gbc_matrix g{};
+        g.nrow = mA;
+        g.ncol = Acsc.n;
+        g.nzc = Acsc.n;
+        g.nnz = Acsc.nz;
+        g.cp = Acsc.jc;
+        g.ir = Acsc.ir;
+        g.num = nullptr;
+        g.where = GBC_HOST;
+        if (mA != Acsc.n) throw std::runtime_error("gbcomb::SpMXSpV: the GPU path takes a square matrix");
+        gbc_graph *gr = nullptr;
+        detail::check(gbc_graph_create(detail::context(), &g, &gr), "gbc_graph_create");
+        const size_t base = indy.size();
+        indy.resize(base + mA);
+        numy.resize(base + mA);
+        int32_t ny = 0;
+        const int rc = gbc_spmspv_select2ndmin_i64(detail::context(), gr, indx, numx, veclen, indy.data() + base,
+                                                   numy.data() + base, &ny, GBC_HOST);
+        gbc_graph_destroy(gr);
+        detail::check(rc, "gbc_spmspv_select2ndmin_i64");
+        indy.resize(base + ny);
+        numy.resize(base + ny);
+    }
+}
+
+}  // namespace gbcomb

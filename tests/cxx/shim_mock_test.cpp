@@ -1,0 +1,206 @@
+// Runs include/gbcomb/combblas_shim.hpp against the stand-in types of
+// mock_combblas.hpp: GPU results must equal the CPU product bit for bit,
+// ownership rules must hold, unregistered semirings must fall back.
+#include "mock_combblas.hpp"
+
+#include <cstdio>
+#include <cstring>
+#include <random>
+
+#include "gbcomb/combblas_shim.hpp"
+
+namespace app {
+template <class T1, class T2>
+struct Select2ndMinSR {  // an application-defined semiring, as in FastSV.h
+    typedef T1 T_promote;
+    static T1 add(const T1 &a, const T1 &b) { return std::min(a, b); }
+    static T1 multiply(const T1 &, const T2 &b) { return b; }
+};
+template <class T1, class T2>
+struct MaxTimes {  // not registered: must run the reference template
+    typedef T1 T_promote;
+    static T1 add(const T1 &a, const T1 &b) { return std::max(a, b); }
+    static T1 multiply(const T1 &a, const T2 &b) { return a * b; }
+};
+}  // namespace app
+typedef app::Select2ndMinSR<int64_t, int64_t> S2M;
+GBCOMB_REGISTER_SEMIRING(S2M, GBC_SR_SELECT2NDMIN, GBC_I64)
+
+using namespace combblas;
+typedef int64_t I;
+
+static int failures = 0;
+#define EXPECT(...)                                                    \
+    do {                                                               \
+        if (!(__VA_ARGS__)) {                                                  \
+            std::printf("FAILED %s:%d: %s\n", __FILE__, __LINE__, #__VA_ARGS__); \
+            ++failures;                                                \
+        }                                                              \
+    } while (0)
+
+template <class NT>
+SpDCCols<I, NT> *random_dcsc(I m, I n, double density, double empty_cols, unsigned seed)
+{
+    std::mt19937_64 g(seed);
+    std::uniform_real_distribution<double> u(0.0, 1.0);
+    std::vector<I> cp{0}, jc, ir;
+    std::vector<NT> v;
+    for (I j = 0; j < n; ++j) {
+        if (u(g) < empty_cols) continue;
+        I cnt = 0;
+        for (I r = 0; r < m; ++r)
+            if (u(g) < density) {
+                ir.push_back(r);
+                v.push_back((NT)(std::is_floating_point<NT>::value ? 1.0 - u(g) : (double)(1 + (int)(u(g) * 40))));
+                ++cnt;
+            }
+        if (cnt) {
+            jc.push_back(j);
+            cp.push_back(cp.back() + cnt);
+        }
+    }
+    return new SpDCCols<I, NT>(m, n, cp, jc, ir, v);
+}
+
+template <class NT>
+bool same(const SpTuples<I, NT> *a, const SpTuples<I, NT> *b)
+{
+    if (a->getnnz() != b->getnnz() || a->getnrow() != b->getnrow() || a->getncol() != b->getncol()) return false;
+    for (int64_t p = 0; p < a->getnnz(); ++p) {
+        if (std::get<0>(a->tuples[p]) != std::get<0>(b->tuples[p])) return false;
+        if (std::get<1>(a->tuples[p]) != std::get<1>(b->tuples[p])) return false;
+        NT x = std::get<2>(a->tuples[p]), y = std::get<2>(b->tuples[p]);
+        if (std::memcmp(&x, &y, sizeof(NT)) != 0) return false;
+    }
+    return true;
+}
+
+int main()
+{
+    typedef PlusTimesSRing<double, double> PT;
+    // 1. PlusTimes fp64 over DCSC, bit-exact against the CPU product
+    SpDCCols<I, double> *A = random_dcsc<double>(700, 500, 0.02, 0.3, 1);
+    SpDCCols<I, double> *B = random_dcsc<double>(500, 400, 0.03, 0.3, 2);
+    const int fb0 = fallback_calls();
+    SpTuples<I, double> *g = gbcomb::LocalHybridSpGEMM<PT, double>(*A, *B, false, false);
+    EXPECT(fallback_calls() == fb0);  // ran on the GPU
+    SpTuples<I, double> *c = combblas::LocalHybridSpGEMM<PT, double>(*A, *B, false, false);
+    EXPECT(g->getnnz() > 0 && same(g, c));
+    EXPECT(g->sorted_ && g->opnew_);
+    SpTuples<I, double> *h = gbcomb::LocalSpGEMMHash<PT, double>(*A, *B, false, false, true);
+    EXPECT(same(h, c));
+    SpTuples<I, double> *l = gbcomb::LocalSpGEMM<PT, double>(*A, *B, false, false);
+    EXPECT(same(l, c));
+    delete g;
+    delete c;
+    delete h;
+    delete l;
+    // 2. clearA / clearB delete the inputs
+    const int del0 = SpDCCols<I, double>::deleted;
+    SpTuples<I, double> *d = gbcomb::LocalHybridSpGEMM<PT, double>(*A, *B, true, true);
+    EXPECT(SpDCCols<I, double>::deleted == del0 + 2);
+    delete d;
+    // 3. an empty operand gives an empty product of the right shape
+    SpDCCols<I, double> Z(700, 500, {0}, {}, {}, {});
+    SpDCCols<I, double> *B2 = random_dcsc<double>(500, 40, 0.05, 0.0, 3);
+    SpTuples<I, double> *e = gbcomb::LocalHybridSpGEMM<PT, double>(Z, *B2, false, false);
+    EXPECT(e->getnnz() == 0 && e->getnrow() == 700 && e->getncol() == 40);
+    delete e;
+    // 4. an application semiring registered by the application
+    SpDCCols<I, int64_t> *Ai = random_dcsc<int64_t>(300, 300, 0.03, 0.2, 4);
+    SpTuples<I, int64_t> *gi = gbcomb::LocalHybridSpGEMM<S2M, int64_t>(*Ai, *Ai, false, false);
+    SpTuples<I, int64_t> *ci = combblas::LocalHybridSpGEMM<S2M, int64_t>(*Ai, *Ai, false, false);
+    EXPECT(gi->getnnz() > 0 && same(gi, ci));
+    delete gi;
+    delete ci;
+    // 5. an unregistered semiring runs the reference template
+    SpDCCols<I, double> *Bs = random_dcsc<double>(500, 500, 0.01, 0.0, 5);
+    const int fb1 = fallback_calls();
+    SpTuples<I, double> *mx = gbcomb::LocalHybridSpGEMM<app::MaxTimes<double, double>, double>(*Bs, *Bs, false, false);
+    EXPECT(fallback_calls() == fb1 + 1);
+    delete mx;
+    // ... and so does a registered semiring with other value types
+    const int fb2 = fallback_calls();
+    SpTuples<I, float> *f = gbcomb::LocalHybridSpGEMM<PT, float>(*Bs, *Bs, false, false);
+    EXPECT(fallback_calls() == fb2 + 1);
+    delete f;
+    // 6. the CSC overload
+    {
+        std::vector<I> cp{0}, ir;
+        std::vector<double> v;
+        const Dcsc<I, double> *dd = B2->GetDCSC();
+        I q = 0;
+        for (I j = 0; j < B2->getncol(); ++j) {
+            if (q < dd->nzc && dd->jc[q] == j) {
+                for (I p = dd->cp[q]; p < dd->cp[q + 1]; ++p) {
+                    ir.push_back(dd->ir[p]);
+                    v.push_back(dd->numx[p]);
+                }
+                ++q;
+            }
+            cp.push_back((I)ir.size());
+        }
+        SpCCols<I, double> Bc(B2->getnrow(), B2->getncol(), cp, ir, v);
+        std::vector<I> acp{0}, air;
+        std::vector<double> av;
+        const Dcsc<I, double> *ad = Bs->GetDCSC();
+        q = 0;
+        for (I j = 0; j < Bs->getncol(); ++j) {
+            if (q < ad->nzc && ad->jc[q] == j) {
+                for (I p = ad->cp[q]; p < ad->cp[q + 1]; ++p) {
+                    air.push_back(ad->ir[p]);
+                    av.push_back(ad->numx[p]);
+                }
+                ++q;
+            }
+            acp.push_back((I)air.size());
+        }
+        SpCCols<I, double> Ac(Bs->getnrow(), Bs->getncol(), acp, air, av);
+        SpTuples<I, double> *gc = gbcomb::LocalHybridSpGEMM<PT, double>(Ac, Bc, false, false);
+        SpTuples<I, double> *cc = combblas::LocalHybridSpGEMM<PT, double>(*Bs, *B2, false, false);
+        EXPECT(gc->getnnz() > 0 && same(gc, cc));
+        delete gc;
+        delete cc;
+        // 7. SpMXSpV over the application's Select2ndMin on a square CSC
+        std::vector<I> scp{0}, sir;
+        std::vector<int64_t> sv;
+        for (I j = 0; j < Ac.getncol(); ++j) {
+            for (I p = acp[j]; p < acp[j + 1]; ++p) {
+                sir.push_back(air[p]);
+                sv.push_back(1);
+            }
+            scp.push_back((I)sir.size());
+        }
+        Csc<I, int64_t> csc;
+        csc.jc = scp.data();
+        csc.ir = sir.data();
+        csc.num = sv.data();
+        csc.n = Ac.getncol();
+        csc.nz = (I)sir.size();
+        std::vector<int32_t> indx{3, 17, 40, 41, 250, 499};
+        std::vector<int64_t> numx{9, 2, 7, 7, 1, 5};
+        std::vector<int32_t> indy{-1};  // results are appended
+        std::vector<int64_t> numy{-1};
+        PreAllocatedSPA<int64_t> spa;
+        gbcomb::SpMXSpV<S2M>(csc, (int32_t)Ac.getnrow(), indx.data(), numx.data(), (int32_t)indx.size(), indy, numy,
+                             spa);
+        std::map<I, int64_t> ref;
+        for (size_t t = 0; t < indx.size(); ++t)
+            for (I p = scp[indx[t]]; p < scp[indx[t] + 1]; ++p) {
+                auto it = ref.find(sir[p]);
+                if (it == ref.end()) ref[sir[p]] = numx[t];
+                else it->second = std::min(it->second, numx[t]);
+            }
+        EXPECT(indy.size() == ref.size() + 1 && indy[0] == -1 && numy[0] == -1);
+        size_t k = 1;
+        for (auto &e : ref) {
+            EXPECT(k < indy.size() && indy[k] == e.first && numy[k] == e.second);
+            ++k;
+        }
+    }
+    delete B2;
+    delete Bs;
+    delete Ai;
+    if (failures == 0) std::printf("OK\n");
+    return failures == 0 ? 0 : 1;
+}
