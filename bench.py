@@ -40,6 +40,13 @@ sys.path.insert(0, ROOT)
 
 SEED = 1
 BFS_ROOTS = 64
+# DRAM bytes of k_numeric measured by ncu on a scale-20 column sample
+# (profiles/k_numeric_s20_cols4096.txt), used to scale roofline.traffic
+NUMERIC_DRAM_READ_PER_MULT = 5.96
+NUMERIC_DRAM_WRITE_PER_ENTRY = 15.67
+# DRAM bytes of the multi-source BFS kernels per scanned edge (expand +
+# finalize, profiles/launches_msbfs22.txt)
+MSBFS_DRAM_PER_SCANNED_EDGE = 19.5
 MS_ROOTS = 512
 
 
@@ -165,6 +172,28 @@ def cpu_bfs_rate(A, roots, budget_s: float):
     return edges / secs / 1e9, f"{used} BFS roots", O.port_num_threads()
 
 
+def cpu_batch_rate(budget_s: float):
+    """Oracle restatement over the batch's problems in order until about
+    budget_s seconds: Gmults/s."""
+    import oracle as O
+    from combblas_gb300 import generators as G
+
+    rm, gk = G.batch_c4(256, seed=4)
+    pairs = [(A, A) for A in rm] + [(A, Rt) for A, R, Rt in gk]
+    order = np.random.default_rng(SEED).permutation(len(pairs))
+    flops, secs, used = 0, 0.0, 0
+    for p in order:
+        A, B = pairs[p]
+        t0 = time.perf_counter()
+        (_, _, _), (fl, _) = O.port_spgemm(A, B, O.SR_PLUSTIMES_F64, want_counts=True)
+        secs += time.perf_counter() - t0
+        flops += int(fl.sum())
+        used += 1
+        if secs > budget_s:
+            break
+    return flops / secs / 1e9, f"{used} of the 256 first-stage products (seeded random order)", O.port_num_threads()
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -217,14 +246,20 @@ def bfs_roots(A, k=BFS_ROOTS):
 def run_reference(args, world, rank):
     if rank != 0:
         return
-    A, scale, ef = make_graph(args.workload, args.scale)
     import oracle as O
 
     O.build(quiet=True) if not os.path.exists(O._PORT_SO) else None
+    A, scale, ef = make_graph(args.workload, args.scale) if args.workload != "batch256" else (None, 0, 0)
     budget = 20.0
     steps = []
     desc, threads = "", 1
-    if args.workload in ("bfs20", "msbfs22"):
+    if args.workload == "batch256":
+        for s in range(args.warmup + args.steps):
+            v, desc, threads = cpu_batch_rate(budget / 4)
+            if s >= args.warmup:
+                steps.append(v)
+        metric, unit = metric_name(args.workload, scale, ef), "Gmults/s"
+    elif args.workload in ("bfs20", "msbfs22"):
         roots = bfs_roots(A)
         for s in range(args.warmup + args.steps):
             v, desc, threads = cpu_bfs_rate(A, roots[s % len(roots):], budget / 4)
@@ -253,6 +288,8 @@ def run_reference(args, world, rank):
 
 
 def metric_name(workload, scale, ef):
+    if workload == "batch256":
+        return "batched SpGEMM Gmults/s (256 uneven problems: R-MAT A*A 2^10..2^18, Galerkin R*A*R^T)"
     if workload == "msbfs22":
         return f"multi-source BFS GTEPS (R-MAT s{scale} ef{ef}, {MS_ROOTS} roots, Select2ndMin SpGEMM loop)"
     if workload == "bfs20":
@@ -356,7 +393,11 @@ def bench_spgemm(args, world, A, Ad, ctx, stream, scale, ef, hbm, peak_kind):
                             "identical_output": same, "learned_speedup": ms_x / ms},
         "roofline": {"bound": "hbm", "kernel": "k_numeric", "achieved": achieved, "peak": hbm,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "traffic_note": "dram bytes per launch: see profiles/"},
+                     "traffic": (NUMERIC_DRAM_READ_PER_MULT * flops + NUMERIC_DRAM_WRITE_PER_ENTRY * st.nnz)
+                     / max(st.phases, 1),
+                     "algorithmic_bytes_per_launch": ba_num / max(st.phases, 1),
+                     "traffic_note": "DRAM bytes per launch scaled from profiles/k_numeric_s20_cols4096.txt "
+                                     "(reads per multiplication, writes per output entry)"},
         "gpu_launches": launches,
         "clocks": ck,
     }
@@ -467,12 +508,14 @@ def bench_msbfs(args, world, A, ctx, stream, hbm, peak_kind, scale, ef):
     l0 = _lib.lib().gbc_launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     edges = 0
+    torch.cuda.nvtx.range_push("timed_msbfs")
     e0.record(stream)
     for _ in range(args.steps):
         _, st = B.msbfs(g, roots, par.data_ptr())
         edges += st.edges
     e1.record(stream)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     ms = max_over_ranks(e0.elapsed_time(e1), world, "cuda")
     launches = _lib.lib().gbc_launch_count() - l0
     ck = clocks.stop()
@@ -490,7 +533,10 @@ def bench_msbfs(args, world, A, ctx, stream, hbm, peak_kind, scale, ef):
                   "loop": "masked Select2ndMin product into a per-(root, vertex) candidate array; one captured "
                           "CUDA graph per level"},
         "roofline": {"bound": "hbm", "kernel": "k_ms_expand + k_ms_finalize", "achieved": achieved, "peak": hbm,
-                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm, "traffic": None},
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": MSBFS_DRAM_PER_SCANNED_EDGE * scanned, "algorithmic_bytes": bytes_trav,
+                     "traffic_note": "DRAM bytes per traversal scaled by scanned edges from "
+                                     "profiles/launches_msbfs22.txt"},
     }
     # e2e: graph upload from host + traversal + parents read back into pinned host memory
     hp = torch.empty((MS_ROOTS, A.ncol), dtype=torch.int64, pin_memory=True)
@@ -525,6 +571,113 @@ def _msbfs_to_host(B, g, roots, hp):
 
 
 
+def bench_batch(args, world, ctx, stream, hbm, peak_kind):
+    """The uneven batch: 128 R-MAT A*A (n = 2^10..2^18, edge factor 4..16)
+    and 128 Galerkin products R*(A*R^T) (27-point Poisson, side 16..64).
+    Batched: products grouped so each group's output fits the device budget,
+    each group one gbc_batch (plan, symbolic, one captured graph), Galerkin
+    second stages in a batch fed from the first stages' device results.
+    One by one: the same products through gbc_spgemm in sequence.  A step is
+    the whole set; both arms include symbolic pass and allocation."""
+    import torch
+    from combblas_gb300 import _lib
+    from combblas_gb300 import batch as BT
+    from combblas_gb300 import generators as G
+    from combblas_gb300 import local as LC
+
+    t0 = time.perf_counter()
+    rm, gk = G.batch_c4(256, seed=4)
+    log(f"generated the 256-problem batch in {time.perf_counter() - t0:.1f}s")
+    dev = lambda M: LC.DeviceMatrix.from_host(M)
+    first = [(dev(A), dev(A)) for A in rm] + [(dev(A), dev(Rt)) for A, R, Rt in gk]
+    Rs = [dev(R) for A, R, Rt in gk]
+    dims = [(A.nrow, Rt.ncol) for A, R, Rt in gk]
+    nnz_first = [int(LC._colstats(a, b, ctx)[1].sum()) for a, b in first]
+    budget = args.batch_budget_nnz
+    groups, cur, acc = [], [], 0
+    for p in sorted(range(len(first)), key=lambda q: nnz_first[q]):
+        if cur and acc + nnz_first[p] > budget:
+            groups.append(cur)
+            cur, acc = [], 0
+        cur.append(p)
+        acc += nnz_first[p]
+    groups.append(cur)
+    ng = len(rm)
+
+    def batched():
+        flops = 0
+        ars = {}
+        for grp in groups:
+            b = BT.Batch([first[p][0] for p in grp], [first[p][1] for p in grp], ctx=ctx)
+            flops += b.flops()
+            for i, p in enumerate(grp):
+                if p >= ng:
+                    ars[p - ng] = b.result_device(i, *dims[p - ng])
+            b.close()
+        b2 = BT.Batch(Rs, [ars[q] for q in range(len(gk))], ctx=ctx)
+        flops += b2.flops()
+        b2.close()
+        return flops
+
+    def one_by_one():
+        for p, (a, b) in enumerate(first):
+            R = LC.spgemm(a, b, ctx=ctx)
+            if p >= ng:
+                q = p - ng
+                ar = LC.DeviceMatrix(dims[q][0], dims[q][1], *result_to_torch(R))
+                R2 = LC.spgemm(Rs[q], ar, ctx=ctx)
+                R2.free()
+            R.free()
+
+    for _ in range(args.warmup):
+        batched()
+    one_by_one()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(int(torch.cuda.current_device()))
+    clocks.start()
+    l0 = _lib.lib().gbc_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("timed_batch")
+    e0.record(stream)
+    for _ in range(args.steps):
+        flops = batched()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    ms = max_over_ranks(e0.elapsed_time(e1), world, "cuda")
+    launches = _lib.lib().gbc_launch_count() - l0
+    ck = clocks.stop()
+    e0.record(stream)
+    for _ in range(args.steps):
+        one_by_one()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_1 = max_over_ranks(e0.elapsed_time(e1), world, "cuda")
+    return {
+        "metric": metric_name(args.workload, 0, 0), "value": flops * args.steps * world / (ms * 1e-3) / 1e9,
+        "unit": "Gmults/s", "ms_per_step": ms / args.steps, "gpu_launches": launches, "clocks": ck,
+        "batch": {"problems": 256, "groups": len(groups), "budget_nnz": budget, "flops": flops,
+                  "one_by_one_gmults": flops * args.steps / (ms_1 * 1e-3) / 1e9,
+                  "one_by_one_ms_per_step": ms_1 / args.steps, "batched_speedup": ms_1 / ms},
+        "roofline": {"bound": "hbm", "kernel": "k_numeric", "achieved": None, "peak": hbm, "peak_kind": peak_kind,
+                     "unit": "GB/s", "frac": None, "traffic": None,
+                     "note": "per-kernel figures for this workload are not derived"},
+    }
+
+
+def result_to_torch(R):
+    """(cp, ir, num) device copies of a product (CSC over the stored columns
+    of B), to feed a second product."""
+    import torch
+
+    t_cp = torch.empty(R.nzc + 1, dtype=torch.int64, device="cuda")
+    t_ir = torch.empty(max(R.nnz, 1), dtype=torch.int64, device="cuda")
+    t_num = torch.empty(max(R.nnz, 1), dtype=torch.float64, device="cuda")
+    R.copy_to(t_cp.data_ptr(), None, t_ir.data_ptr(), t_num.data_ptr(), where=1)
+    return t_cp, t_ir[:R.nnz], t_num[:R.nnz]
+
+
+
 # ------------------------------------------------------------------- ours
 def run_ours(args, world, rank, local):
     import torch
@@ -534,15 +687,19 @@ def run_ours(args, world, rank, local):
     from combblas_gb300 import bfs as B
     from combblas_gb300 import local as LC
 
-    A, scale, ef = make_graph(args.workload, args.scale)
     ctx = LC.Context(local)
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
     hbm, peak_kind = peaks()
-    Ad = LC.DeviceMatrix.from_host(A)
-    torch.cuda.synchronize()
     budget = args.phase_nnz
     result: dict = {}
+    if args.workload == "batch256":
+        A, scale, ef = None, 0, 0
+        result.update(bench_batch(args, world, ctx, stream, hbm, peak_kind))
+    else:
+        A, scale, ef = make_graph(args.workload, args.scale)
+        Ad = LC.DeviceMatrix.from_host(A)
+        torch.cuda.synchronize()
 
     # ---- SpGEMM, inputs resident in HBM -------------------------------
     if args.workload.startswith("spgemm"):
@@ -568,12 +725,14 @@ def run_ours(args, world, rank, local):
         if args.workload == "bfs20":
             clocks = ClockSampler(local)
             clocks.start()
+        torch.cuda.nvtx.range_push("timed_bfs")
         e0.record(stream)
         for r in roots:
             st_b = B.bfs_device(g, int(r), par.data_ptr(), lev.data_ptr())
             edges += st_b.edges
         e1.record(stream)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         bfs_ms = e0.elapsed_time(e1)
         gteps = edges / (bfs_ms * 1e-3) / 1e9
         bfs_launches = _lib.lib().gbc_launch_count() - l0
@@ -595,12 +754,15 @@ def run_ours(args, world, rank, local):
                              "h2d_bytes_per_step": (A.colptr.nbytes + A.rowidx.nbytes),
                              "d2h_bytes_per_step": 2 * A.ncol * 8}
             achieved = edges * 2 * 4 / (bfs_ms * 1e-3) / 1e9
-            result["roofline"] = {"bound": "hbm", "kernel": "k_bfs_expand", "achieved": achieved, "peak": hbm,
+            result["roofline"] = {"bound": "hbm", "kernel": "k_bfs_td + k_bfs_bu", "achieved": achieved, "peak": hbm,
                                   "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm, "traffic": None}
 
     # ---- CPU baseline (rank 0, N=1 only) -------------------------------
     if rank == 0 and world == 1 and not args.no_cpu:
-        if args.workload in ("bfs20", "msbfs22"):
+        if args.workload == "batch256":
+            v, desc, th = cpu_batch_rate(15.0)
+            result["cpu_baseline"] = {"value": v, "unit": "Gmults/s", "cores": th, "kind": "port", "sample": desc}
+        elif args.workload in ("bfs20", "msbfs22"):
             v, desc, th = cpu_bfs_rate(A, bfs_roots(A)[:8], 15.0)
             result["cpu_baseline"] = {"value": v, "unit": "GTEPS", "cores": th, "kind": "port",
                                       "sample": desc + " (single-source BFS of the oracle's C restatement; the "
@@ -634,12 +796,15 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["spgemm20", "bfs20", "spgemm14", "msbfs22"], default="spgemm20")
+    ap.add_argument("--workload", choices=["spgemm20", "bfs20", "spgemm14", "msbfs22", "batch256"],
+                    default="spgemm20")
     ap.add_argument("--phase-nnz", type=int, default=3 << 30)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mcl", action="store_true", help="skip the MCL exact-vs-learned comparison")
     ap.add_argument("--no-bfs", action="store_true", help="skip the BFS sub-measurement of SpGEMM workloads")
     ap.add_argument("--scale", type=int, default=0, help="override the R-MAT scale (profiling runs)")
+    ap.add_argument("--batch-budget-nnz", type=int, default=6 << 30,
+                    help="batch256: output entries one batch group may hold")
     ap.add_argument("--bcols", type=int, default=0,
                     help="profiling case: B = A(:, this many seeded random columns) instead of A")
     args = ap.parse_args()

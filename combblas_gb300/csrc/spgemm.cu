@@ -544,20 +544,46 @@ __global__ void __launch_bounds__(kThreads, SUB <= 2048 ? 2 : 1) k_numeric(const
                         before += u < warp ? ws : 0;
                         tot += ws;
                     }
-                    int64_t pos = out + before + x - wl;
-                    for (int w = w0; w < w1; ++w) {
-                        uint32_t x = bm[w];
-                        while (x) {
-                            const int bit = __ffs(x) - 1;
-                            x &= x - 1;
-                            const int o = w * 32 + bit;
+                    if (tot <= kSub) {
+                        // stage the tile's entries in row order in shared memory,
+                        // then store them with consecutive threads on
+                        // consecutive positions
+                        int q = before + x - wl;
+                        for (int w = w0; w < w1; ++w) {
+                            uint32_t bits = bm[w];
+                            while (bits) {
+                                const int o = w * 32 + __ffs(bits) - 1;
+                                bits &= bits - 1;
+                                srow[q] = (uint16_t)o;
+                                sval[q] = acc[o];
+                                ++q;
+                            }
+                        }
+                        __syncthreads();
+                        for (int p = tid; p < tot; p += kThreads) {
+                            const int64_t pos = out + p;
                             if (pos < lim) {
-                                cir[pos] = (int64_t)row0 + o;
-                                cval[pos] = acc[o];
+                                cir[pos] = (int64_t)row0 + srow[p];
+                                cval[pos] = sval[p];
                             } else {
                                 over = true;  // never write past the column's range
                             }
-                            ++pos;
+                        }
+                    } else {
+                        int64_t pos = out + before + x - wl;
+                        for (int w = w0; w < w1; ++w) {
+                            uint32_t bits = bm[w];
+                            while (bits) {
+                                const int o = w * 32 + __ffs(bits) - 1;
+                                bits &= bits - 1;
+                                if (pos < lim) {
+                                    cir[pos] = (int64_t)row0 + o;
+                                    cval[pos] = acc[o];
+                                } else {
+                                    over = true;
+                                }
+                                ++pos;
+                            }
                         }
                     }
                     out += tot;
