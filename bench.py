@@ -276,7 +276,7 @@ def run_reference(args, world, rank):
     line = {
         "impl": "reference", "metric": metric, "value": val, "unit": unit, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.workload.startswith("spgemm") else "int64",
+        "dtype": "f64" if args.workload.startswith("spgemm") or args.workload == "batch256" else "int64",
         "data": "synthetic (seeded R-MAT)",
         "config": {"workload": args.workload, "scale": scale, "edge_factor": ef, "seed": SEED},
         "cpu_baseline": {"value": val, "unit": unit, "cores": threads, "kind": "port",
@@ -604,20 +604,25 @@ def bench_batch(args, world, ctx, stream, hbm, peak_kind):
     groups.append(cur)
     ng = len(rm)
 
-    def batched():
-        flops = 0
+    def batched(inputs=None, R_in=None, read_back=False):
+        inputs = inputs or first
+        flops, d2h = 0, 0
         ars = {}
         for grp in groups:
-            b = BT.Batch([first[p][0] for p in grp], [first[p][1] for p in grp], ctx=ctx)
+            b = BT.Batch([inputs[p][0] for p in grp], [inputs[p][1] for p in grp], ctx=ctx)
             flops += b.flops()
             for i, p in enumerate(grp):
                 if p >= ng:
                     ars[p - ng] = b.result_device(i, *dims[p - ng])
+                if read_back:
+                    d2h += b.column_pointers(i).nbytes
             b.close()
-        b2 = BT.Batch(Rs, [ars[q] for q in range(len(gk))], ctx=ctx)
+        b2 = BT.Batch(R_in or Rs, [ars[q] for q in range(len(gk))], ctx=ctx)
         flops += b2.flops()
+        if read_back:
+            d2h += sum(b2.column_pointers(q).nbytes for q in range(len(gk)))
         b2.close()
-        return flops
+        return flops, d2h
 
     def one_by_one():
         for p, (a, b) in enumerate(first):
@@ -632,6 +637,8 @@ def bench_batch(args, world, ctx, stream, hbm, peak_kind):
     for _ in range(args.warmup):
         batched()
     one_by_one()
+    first_host = [(A, A) for A in rm] + [(A, Rt) for A, R, Rt in gk]
+    Rs_host = [R for A, R, Rt in gk]
     torch.cuda.synchronize()
     clocks = ClockSampler(int(torch.cuda.current_device()))
     clocks.start()
@@ -640,7 +647,7 @@ def bench_batch(args, world, ctx, stream, hbm, peak_kind):
     torch.cuda.nvtx.range_push("timed_batch")
     e0.record(stream)
     for _ in range(args.steps):
-        flops = batched()
+        flops, _ = batched()
     e1.record(stream)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
@@ -653,7 +660,21 @@ def bench_batch(args, world, ctx, stream, hbm, peak_kind):
     e1.record(stream)
     torch.cuda.synchronize()
     ms_1 = max_over_ranks(e0.elapsed_time(e1), world, "cuda")
+    # e2e: first-stage inputs from host memory (copied inside gbc_batch_create),
+    # every product's column pointers read back
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        _, d2h = batched(first_host, Rs_host, read_back=True)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, "cuda")
+    h2d = sum(M.colptr.nbytes + M.rowidx.nbytes + M.values.nbytes for pair in first_host for M in pair) + \
+        sum(M.colptr.nbytes + M.rowidx.nbytes + M.values.nbytes for M in Rs_host)
     return {
+        "e2e": {"value": flops * args.steps * world / e2e_s / 1e9, "unit": "Gmults/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "path": "gbc_batch_create from host CSC arrays + gbc_batch_run; column pointers of every product "
+                        "read back (the products stay on the device)"},
         "metric": metric_name(args.workload, 0, 0), "value": flops * args.steps * world / (ms * 1e-3) / 1e9,
         "unit": "Gmults/s", "ms_per_step": ms / args.steps, "gpu_launches": launches, "clocks": ck,
         "batch": {"problems": 256, "groups": len(groups), "budget_nnz": budget, "flops": flops,
@@ -775,7 +796,8 @@ def run_ours(args, world, rank, local):
     line = {
         "metric": result["metric"], "value": result["value"], "unit": result["unit"], "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": result["ms_per_step"], "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.workload.startswith("spgemm") else "int64",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.workload.startswith("spgemm") or args.workload == "batch256" else "int64",
         "data": "synthetic (seeded R-MAT, numpy generator)",
         "config": {"workload": args.workload, "scale": scale, "edge_factor": ef, "seed": SEED,
                    "rmat_abcd": [0.57, 0.19, 0.19, 0.05], "index": "int64",
@@ -783,7 +805,7 @@ def run_ours(args, world, rank, local):
                    "parallelism": f"replicas x{world}", **({"b_columns": args.bcols} if args.bcols else {})},
     }
     for k in ("roofline", "cpu_baseline", "e2e", "gpu_launches", "clocks", "spgemm", "exact_two_phase", "mcl", "bfs",
-              "msbfs"):
+              "msbfs", "batch"):
         if k in result:
             line[k] = result[k]
     if rank == 0:

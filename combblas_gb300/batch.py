@@ -60,6 +60,13 @@ class Batch:
                                          num.ctypes.data if nnz else None, L.GBC_HOST))
         return cp, ir, num
 
+    def column_pointers(self, p: int) -> np.ndarray:
+        """Product p's column pointers only (host copy)."""
+        nzc, _, _ = self.info(p)
+        cp = np.empty(nzc + 1, np.int64)
+        L.check(L.lib().gbc_batch_result(self.h, p, cp.ctypes.data, None, None, L.GBC_HOST))
+        return cp
+
     def result_device(self, p: int, nrow: int, ncol: int):
         """Product p as a DeviceMatrix (CSC over the stored columns of B_p,
         which must be a CSC matrix)."""
