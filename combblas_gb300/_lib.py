@@ -140,6 +140,8 @@ _SIGS.update({
                           C.c_int]),
     "gbc_msbfs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int,
                             C.POINTER(gbc_msbfs_stats)]),
+    "gbc_multiway_merge": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int64, C.c_int64,
+                                     C.POINTER(C.c_void_p), C.POINTER(gbc_spgemm_stats)]),
 })
 
 # entry points added by later modules register here (see extend_signatures)

@@ -1,5 +1,7 @@
 // Device semirings: one static-method struct per reference semiring, the same
 // shape as the reference's SR::multiply / SR::add / SR::id (Semirings.h).
+// one() is the value of an entry stored without a value array (a pattern
+// matrix); unit() is the multiplicative identity: mul(unit(), x) == x.
 // Floating-point multiply and add use the _rn intrinsics so that the
 // compiler can never fuse them into an FMA: each product is rounded before
 // it is added, as in the reference's `SR::add(SR::multiply(a, b), acc)`.
@@ -19,6 +21,7 @@ struct PlusTimes<double> {
     static __device__ __forceinline__ V mul(V a, V b) { return __dmul_rn(a, b); }
     static __device__ __forceinline__ V add(V a, V b) { return __dadd_rn(a, b); }
     static __host__ __device__ __forceinline__ V one() { return 1.0; }
+    static __host__ __device__ __forceinline__ V unit() { return 1.0; }
 };
 
 template <>
@@ -27,6 +30,7 @@ struct PlusTimes<float> {
     static __device__ __forceinline__ V mul(V a, V b) { return __fmul_rn(a, b); }
     static __device__ __forceinline__ V add(V a, V b) { return __fadd_rn(a, b); }
     static __host__ __device__ __forceinline__ V one() { return 1.0f; }
+    static __host__ __device__ __forceinline__ V unit() { return 1.0f; }
 };
 
 // Integer PlusTimes wraps modulo 2^64 (the reference's signed overflow on
@@ -37,6 +41,7 @@ struct PlusTimes<int64_t> {
     static __device__ __forceinline__ V mul(V a, V b) { return (V)((uint64_t)a * (uint64_t)b); }
     static __device__ __forceinline__ V add(V a, V b) { return (V)((uint64_t)a + (uint64_t)b); }
     static __host__ __device__ __forceinline__ V one() { return 1; }
+    static __host__ __device__ __forceinline__ V unit() { return 1; }
 };
 
 // PlusTimesSRing<bool,bool>: promote_trait<bool,bool> is bool, so add is
@@ -46,6 +51,7 @@ struct BoolOrAnd {
     static __device__ __forceinline__ V mul(V a, V b) { return (V)((a != 0) & (b != 0)); }
     static __device__ __forceinline__ V add(V a, V b) { return (V)((a != 0) | (b != 0)); }
     static __host__ __device__ __forceinline__ V one() { return 1; }
+    static __host__ __device__ __forceinline__ V unit() { return 1; }
 };
 
 // MinPlusSRing (Semirings.h:235-255) with inf_plus (Semirings.h:40-47):
@@ -60,6 +66,7 @@ struct MinPlus<double> {
     static __device__ __forceinline__ V mul(V a, V b) { return (a == inf() || b == inf()) ? inf() : __dadd_rn(a, b); }
     static __device__ __forceinline__ V add(V a, V b) { return (b < a) ? b : a; }  // std::min(a, b)
     static __host__ __device__ __forceinline__ V one() { return 1.0; }
+    static __host__ __device__ __forceinline__ V unit() { return 0.0; }
 };
 
 template <>
@@ -72,6 +79,7 @@ struct MinPlus<int64_t> {
     }
     static __device__ __forceinline__ V add(V a, V b) { return (b < a) ? b : a; }
     static __host__ __device__ __forceinline__ V one() { return 1; }
+    static __host__ __device__ __forceinline__ V unit() { return 0; }
 };
 
 // Select2ndMinSR (Applications/FastSV.h:25-44): multiply returns the second
@@ -82,6 +90,7 @@ struct Select2ndMin {
     static __device__ __forceinline__ V mul(V, V b) { return b; }
     static __device__ __forceinline__ V add(V a, V b) { return (b < a) ? b : a; }
     static __host__ __device__ __forceinline__ V one() { return 1; }
+    static __host__ __device__ __forceinline__ V unit() { return 0; }  // any value: mul returns b
 };
 
 }  // namespace gbc

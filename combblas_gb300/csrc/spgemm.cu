@@ -1868,6 +1868,126 @@ int spgemm_colstats(gbc_context *ctx, const gbc_matrix *Am, const gbc_matrix *Bm
     return GBC_OK;
 }
 
+// ------------------------------------------------------- multiway merge
+// Sum of K matrices of one shape, entries combined with SR::add in list
+// order -- MultiwayMerge (MultiwayMerge.h:428-708) of the SpTuples that
+// several SUMMA stages or phases produce for the same block.  It is the
+// product [I I ... I] * [L_1; L_2; ...; L_K]: column j of the stacked right
+// operand holds L_1(:,j), L_2(:,j) (rows + m), ... in that order, the left
+// operand's column k*m + r is e_r with the semiring's multiplicative
+// identity, so every output entry is the left fold over the lists in order,
+// computed by the SpGEMM kernels.
+__global__ void k_stack_counts(int nlists, const int64_t *const *dcp, int64_t n, int64_t *cnt)
+{
+    const int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    int64_t c = 0;
+    for (int k = 0; k < nlists; ++k) c += dcp[k][j + 1] - dcp[k][j];
+    cnt[j] = c;
+}
+
+template <typename V>
+__global__ void k_stack_fill(int nlists, const int64_t *const *dcp, const int64_t *const *ir,
+                             const void *const *num, V one, int64_t m, int64_t n, const int64_t *bcp, int64_t *bir,
+                             V *bnum)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t j = warp; j < n; j += nwarps) {
+        int64_t o = bcp[j];
+        for (int k = 0; k < nlists; ++k) {
+            const int64_t s0 = dcp[k][j], s1 = dcp[k][j + 1];
+            const V *v = static_cast<const V *>(num[k]);
+            for (int64_t p = s0 + lane; p < s1; p += 32) {
+                bir[o + (p - s0)] = ir[k][p] + (int64_t)k * m;
+                bnum[o + (p - s0)] = v ? v[p] : one;
+            }
+            o += s1 - s0;
+        }
+    }
+}
+
+template <typename V>
+__global__ void k_identity_stack(int64_t m, int64_t cols, V unit, int64_t *cp, int64_t *ir, V *val)
+{
+    const int64_t c = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c < cols) {
+        cp[c] = c;
+        ir[c] = c % m;
+        val[c] = unit;
+    }
+    if (c == cols) cp[c] = cols;
+}
+
+template <class SR>
+static int multiway_merge(Context *ctx, int vt, int nlists, const gbc_matrix *lists, int64_t m, int64_t n,
+                          gbc_result **out, gbc_spgemm_stats *st)
+{
+    typedef typename SR::V V;
+    cudaStream_t s = ctx->stream;
+    Workspace ws(ctx);
+    gbc_spgemm_opts opt{GBC_SIZING_EXACT, GBC_SORTED, 1, 0, -1, -1};
+    if (nlists == 0 || m == 0 || n == 0) {  // an empty m x n product
+        int64_t *z = nullptr;
+        GBC_TRY(ws.alloc_n(&z, (size_t)n + 2));
+        GBC_CUDA_TRY(cudaMemsetAsync(z, 0, (n + 2) * sizeof(int64_t), s));
+        const DevMatrix A{m, 1, 1, 0, z, nullptr, z, nullptr};
+        const DevMatrix B{1, n, n, 0, z, nullptr, z, nullptr};
+        return spgemm_exact<SR>(ctx, A, B, opt, vt, out, st);
+    }
+    std::vector<const int64_t *> hdcp(nlists), hir(nlists);
+    std::vector<const void *> hnum(nlists);
+    for (int k = 0; k < nlists; ++k) {
+        DevMatrix L;
+        GBC_TRY(upload(ws, &lists[k], vt, &L));
+        const int64_t *dcp = L.cp;
+        if (L.jc) {
+            int64_t *d = nullptr;
+            GBC_TRY(ws.alloc_n(&d, n + 1));
+            k_dense_colptr<<<(unsigned)((L.nzc + 1 + 255) / 256), 256, 0, s>>>(n, L.nzc, L.cp, L.jc, d);
+            note_launch();
+            dcp = d;
+        }
+        hdcp[k] = dcp;
+        hir[k] = L.ir;
+        hnum[k] = L.num;
+    }
+    const int64_t **ddcp = nullptr, **dir = nullptr;
+    const void **dnum = nullptr;
+    GBC_TRY(ws.alloc_n(&ddcp, nlists));
+    GBC_TRY(ws.alloc_n(&dir, nlists));
+    GBC_TRY(ws.alloc_n(&dnum, nlists));
+    GBC_CUDA_TRY(cudaMemcpyAsync(ddcp, hdcp.data(), nlists * sizeof(void *), cudaMemcpyHostToDevice, s));
+    GBC_CUDA_TRY(cudaMemcpyAsync(dir, hir.data(), nlists * sizeof(void *), cudaMemcpyHostToDevice, s));
+    GBC_CUDA_TRY(cudaMemcpyAsync(dnum, hnum.data(), nlists * sizeof(void *), cudaMemcpyHostToDevice, s));
+    int64_t *cnt = nullptr, *bcp = nullptr;
+    GBC_TRY(ws.alloc_n(&cnt, n + 1));
+    GBC_TRY(ws.alloc_n(&bcp, n + 1));
+    k_stack_counts<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(nlists, ddcp, n, cnt);
+    note_launch();
+    GBC_TRY(exclusive_scan_i64(ws, cnt, bcp, n, s));
+    int64_t total = 0;
+    GBC_TRY(read_i64(ctx, bcp + n, &total));
+    int64_t *bir = nullptr, *acp = nullptr, *air = nullptr;
+    V *bnum = nullptr, *aval = nullptr;
+    GBC_TRY(ws.alloc_n(&bir, total + 1));
+    GBC_TRY(ws.alloc_n(&bnum, total + 1));
+    k_stack_fill<V><<<grid_for(ctx, (n + 7) / 8, 8), 256, 0, s>>>(nlists, ddcp, dir, dnum, SR::one(), m, n, bcp, bir,
+                                                                    bnum);
+    note_launch();
+    const int64_t cols = (int64_t)nlists * m;
+    GBC_TRY(ws.alloc_n(&acp, cols + 1));
+    GBC_TRY(ws.alloc_n(&air, cols + 1));
+    GBC_TRY(ws.alloc_n(&aval, cols + 1));
+    k_identity_stack<V><<<(unsigned)((cols + 1 + 255) / 256), 256, 0, s>>>(m, cols, SR::unit(), acp, air, aval);
+    note_launch();
+    GBC_CUDA_TRY(cudaGetLastError());
+    const DevMatrix A{m, cols, cols, cols, acp, nullptr, air, aval};
+    const DevMatrix B{cols, n, n, total, bcp, nullptr, bir, bnum};
+    return spgemm_exact<SR>(ctx, A, B, opt, vt, out, st);
+}
+
 }  // namespace gbc
 
 using namespace gbc;
@@ -2074,6 +2194,39 @@ int gbc_spgemm_colstats(gbc_context *ctx, const gbc_matrix *A, const gbc_matrix 
                         int where)
 {
     return spgemm_colstats(ctx, A, B, flop, nnz, where);
+}
+
+int gbc_multiway_merge(gbc_context *ctx, int sr, int vt, int nlists, const gbc_matrix *lists, int64_t nrow,
+                       int64_t ncol, gbc_result **C, gbc_spgemm_stats *st)
+{
+    if (!ctx || !C || (nlists > 0 && !lists) || nlists < 0) return fail(GBC_EINVAL, "null or bad argument");
+    *C = nullptr;
+    for (int k = 0; k < nlists; ++k)
+        if (lists[k].nrow != nrow || lists[k].ncol != ncol)
+            return fail(GBC_EINVAL, "dimensions of the merged matrices do not match");
+    if ((int64_t)nlists * nrow >= (int64_t(1) << 31)) return fail(GBC_EOVERFLOW, "lists x rows must be below 2^31");
+    GBC_CUDA_TRY(cudaSetDevice(ctx->device));
+    switch (sr) {
+        case GBC_SR_PLUSTIMES:
+            if (vt == GBC_F64) return multiway_merge<PlusTimes<double>>(ctx, vt, nlists, lists, nrow, ncol, C, st);
+            if (vt == GBC_F32) return multiway_merge<PlusTimes<float>>(ctx, vt, nlists, lists, nrow, ncol, C, st);
+            if (vt == GBC_I64) return multiway_merge<PlusTimes<int64_t>>(ctx, vt, nlists, lists, nrow, ncol, C, st);
+            if (vt == GBC_BOOL) return multiway_merge<BoolOrAnd>(ctx, vt, nlists, lists, nrow, ncol, C, st);
+            break;
+        case GBC_SR_BOOL:
+            if (vt == GBC_BOOL) return multiway_merge<BoolOrAnd>(ctx, vt, nlists, lists, nrow, ncol, C, st);
+            break;
+        case GBC_SR_MINPLUS:
+            if (vt == GBC_F64) return multiway_merge<MinPlus<double>>(ctx, vt, nlists, lists, nrow, ncol, C, st);
+            if (vt == GBC_I64) return multiway_merge<MinPlus<int64_t>>(ctx, vt, nlists, lists, nrow, ncol, C, st);
+            break;
+        case GBC_SR_SELECT2NDMIN:
+            if (vt == GBC_I64)
+                return multiway_merge<Select2ndMin<int64_t>>(ctx, vt, nlists, lists, nrow, ncol, C, st);
+            break;
+        default: break;
+    }
+    return fail(GBC_EUNSUPPORTED, "semiring/value type combination not instantiated");
 }
 
 }  // extern "C"

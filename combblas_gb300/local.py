@@ -9,6 +9,8 @@ Names and argument meaning follow the reference calls the C ABI replaces:
 * ``LocalSpGEMMHash(A, B, clearA, clearB, sort)`` -- mtSpGEMM.h:463-467
 * ``estimateFLOP(A, B)`` -- mtSpGEMM.h:1057; ``estimateNNZ_Hash(A, B)`` --
   mtSpGEMM.h:806
+* ``MultiwayMerge(lists, mdim, ndim)`` -- MultiwayMerge.h:428-708 (the sum of
+  several stages' products, equal entries combined in list order)
 
 The semiring is given by name (the reference's template argument ``SR``):
 ``"plustimes"`` (PlusTimesSRing), ``"minplus"`` (MinPlusSRing),
@@ -293,6 +295,24 @@ def spgemm_phased(A, B, sr: str = "plustimes", max_phase_nnz: int = 1 << 31, ctx
                                       int(max_phase_nnz), L.SIZING_LEARNED if sizing == "learned" else L.SIZING_EXACT,
                                       C.byref(st)))
     return st
+
+
+def MultiwayMerge(lists, mdim: int, ndim: int, sr: str = "plustimes", dtype=None,
+                  ctx: Context | None = None) -> SpResult:
+    """Sum of matrices of one shape with duplicates combined by the
+    semiring's add in list order (MultiwayMerge.h:428-708)."""
+    ctx = ctx or default_context()
+    if lists:
+        dt = np.dtype(dtype) if dtype is not None else _value_dtype(lists[0], lists[0], sr)
+    else:
+        dt = np.dtype(dtype or np.float64)
+    keep: list = []
+    arr = (L.gbc_matrix * max(len(lists), 1))(*[as_gbc_matrix(M, keep, dt) for M in lists])
+    out = C.c_void_p()
+    st = L.gbc_spgemm_stats()
+    L.check(L.lib().gbc_multiway_merge(ctx.h, SR_CODES[sr], VT_OF_DTYPE[dt], len(lists), arr, int(mdim), int(ndim),
+                                       C.byref(out), C.byref(st)))
+    return SpResult(out, st)
 
 
 def LocalHybridSpGEMM(A, B, clearA: bool = False, clearB: bool = False, sr: str = "plustimes", **kw) -> SpResult:

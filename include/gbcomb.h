@@ -172,6 +172,15 @@ typedef struct {
 int gbc_spgemm_phased(gbc_context *ctx, int sr, int vt, const gbc_matrix *A, const gbc_matrix *B,
                       int64_t max_phase_nnz, int sizing, gbc_phased_stats *st);
 
+/* Sum of nlists matrices of one shape (nrow x ncol), entries with the same
+ * (row, column) combined with the semiring's add in list order: replaces
+ * MultiwayMerge<SR>(vector<SpTuples*>&, mdim, ndim, delarrs)
+ * (MultiwayMerge.h:428-708), which merges the outputs of several SUMMA
+ * stages or column phases.  The result has one column per column of the
+ * shape (SpTuples view), rows ascending. */
+int gbc_multiway_merge(gbc_context *ctx, int sr, int vt, int nlists, const gbc_matrix *lists, int64_t nrow,
+                       int64_t ncol, gbc_result **C, gbc_spgemm_stats *stats);
+
 /* Symbolic helpers: per stored column of B, flop = estimateFLOP
  * (mtSpGEMM.h:1057-1134) and nnz = estimateNNZ_Hash (mtSpGEMM.h:806-933).
  * Output arrays have B->nzc entries and live where `where` says. */

@@ -9,6 +9,7 @@
  *   gbcomb::LocalSpGEMMHash<SR, NTO>(A, B, clearA, clearB, sort) mtSpGEMM.h:463-467
  *   gbcomb::LocalHybridSpGEMM<SR, NTO>(SpCCols A, SpCCols B, ...)  mtSpGEMM.h:1142-1152
  *   gbcomb::SpMXSpV<SR>(Csc, mA, indx, numx, veclen, indy, numy, SPA)  SpImpl.h:115-124
+ *   gbcomb::MultiwayMerge<SR>(ArrSpTups, mdim, ndim, delarrs)  MultiwayMerge.h:428-708
  *
  * Same arguments, same ownership (inputs borrowed; clearA / clearB delete
  * them; the returned SpTuples owns a tuple array from ::operator new with
@@ -266,6 +267,78 @@ combblas::SpTuples<IT, NTO> *LocalHybridSpGEMM(const combblas::SpCCols<IT, NT1> 
         return detail::run<SR, NTO>(A, B, clearA, clearB, GBC_SORTED);
     else
         return combblas::LocalHybridSpGEMM<SR, NTO>(A, B, clearA, clearB);
+}
+
+// Sum of column-sorted SpTuples of one shape, equal (row, col) combined by
+// SR::add in list order.  One or no list, or a shape mismatch, behave as the
+// reference (copy, empty result, message and an empty 0 x 0 result); the
+// result's tuple array comes from new[] (isOpNew = false) as the
+// reference's; delarrs deletes the inputs.  With three or more lists the
+// reference combines equal keys in its heap's order, so PlusTimes sums of
+// floating values can differ in the last bit.
+template <class SR, class IT, class NT>
+combblas::SpTuples<IT, NT> *MultiwayMerge(std::vector<combblas::SpTuples<IT, NT> *> &ArrSpTups, IT mdim = 0,
+                                          IT ndim = 0, bool delarrs = false)
+{
+    constexpr bool gpu = detail::offloaded<SR, NT, IT, NT, NT>();
+    const int nlists = (int)ArrSpTups.size();
+    if constexpr (!gpu) {
+        return combblas::MultiwayMerge<SR>(ArrSpTups, mdim, ndim, delarrs);
+    } else {
+        if (nlists <= 1) return combblas::MultiwayMerge<SR>(ArrSpTups, mdim, ndim, delarrs);
+        for (int k = 0; k < nlists; ++k)
+            if (mdim != ArrSpTups[k]->getnrow() || ndim != ArrSpTups[k]->getncol()) {
+                std::fprintf(stderr, "Dimensions of SpTuples do not match on multiwayMerge()\n");
+                return new combblas::SpTuples<IT, NT>(0, 0, 0);
+            }
+        // each list as a host CSC (tuples are column sorted)
+        std::vector<std::vector<int64_t>> cps(nlists), irs(nlists);
+        std::vector<std::unique_ptr<NT[]>> nums(nlists);
+        std::vector<gbc_matrix> mats(nlists);
+        for (int k = 0; k < nlists; ++k) {
+            const combblas::SpTuples<IT, NT> &T = *ArrSpTups[k];
+            const int64_t nnz = T.getnnz();
+            cps[k].assign(ndim + 1, 0);
+            irs[k].resize(nnz);
+            nums[k].reset(new NT[nnz > 0 ? nnz : 1]);
+            for (int64_t p = 0; p < nnz; ++p) {
+                ++cps[k][T.colindex(p) + 1];
+                irs[k][p] = T.rowindex(p);
+                nums[k][p] = T.numvalue(p);
+            }
+            for (IT j = 0; j < ndim; ++j) cps[k][j + 1] += cps[k][j];
+            gbc_matrix &g = mats[k];
+            g = gbc_matrix{};
+            g.nrow = mdim;
+            g.ncol = ndim;
+            g.nzc = ndim;
+            g.nnz = nnz;
+            g.cp = cps[k].data();
+            g.jc = nullptr;
+            g.ir = nnz ? irs[k].data() : nullptr;
+            g.num = nnz ? static_cast<const void *>(nums[k].get()) : nullptr;
+            g.where = GBC_HOST;
+        }
+        gbc_result *C = nullptr;
+        detail::check(gbc_multiway_merge(detail::context(), semiring_of<SR>::sr, semiring_of<SR>::vt, nlists,
+                                         mats.data(), mdim, ndim, &C, nullptr),
+                      "gbc_multiway_merge");
+        int64_t nrow = 0, ncol = 0, nzc = 0, nnz = 0;
+        int vt = 0;
+        gbc_result_info(C, &nrow, &ncol, &nzc, &nnz, &vt);
+        std::vector<int64_t> cp(nzc + 1), jc(nzc), ir(nnz);
+        std::unique_ptr<NT[]> num(new NT[nnz > 0 ? nnz : 1]);
+        const int rc = gbc_result_copy(C, cp.data(), nzc ? jc.data() : nullptr, nnz ? ir.data() : nullptr,
+                                       nnz ? static_cast<void *>(num.get()) : nullptr, GBC_HOST);
+        gbc_result_free(C);
+        detail::check(rc, "gbc_result_copy");
+        auto *tuples = new std::tuple<IT, IT, NT>[nnz > 0 ? nnz : 1];
+        for (int64_t k = 0; k < nzc; ++k)
+            for (int64_t p = cp[k]; p < cp[k + 1]; ++p) tuples[p] = std::tuple<IT, IT, NT>(ir[p], jc[k], num[p]);
+        if (delarrs)
+            for (int k = 0; k < nlists; ++k) delete ArrSpTups[k];
+        return new combblas::SpTuples<IT, NT>(nnz, mdim, ndim, tuples, true, false);
+    }
 }
 
 // y = A x over a min-select semiring (registered with GBC_SR_SELECT2NDMIN /

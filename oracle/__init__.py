@@ -92,6 +92,9 @@ def _ref():
         lib.ref_mcl_expand.argtypes = [C.c_int64, _P64, _P64, np.ctypeslib.ndpointer(dtype=np.float32),
                                        C.c_float, C.c_int64, C.c_int64, C.c_float]
         lib.ref_num_threads.restype = C.c_int
+        lib.ref_multiway_merge.restype = C.c_int64
+        lib.ref_multiway_merge.argtypes = [C.c_int, C.c_int, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
+                                           C.c_void_p]
         _ref_lib = lib
     return _ref_lib
 
@@ -250,6 +253,68 @@ def port_bfs(A, source: int, with_levels: bool = True):
     it = lib.gbc_o_bfs(n, np.ascontiguousarray(A.colptr), np.ascontiguousarray(A.rowidx), int(source), parents,
                        levels.ctypes.data_as(C.c_void_p) if with_levels else None)
     return parents, levels, it
+
+
+def ref_multiway_merge(lists, m: int, n: int, sr: int):
+    """The reference's MultiwayMerge<SR> of CSC matrices of one shape;
+    returns (rows, cols, vals) in its column-major tuple order."""
+    lib = _ref()
+    dt = SR_DTYPE[sr]
+    keep = []
+    cps = (C.c_void_p * max(len(lists), 1))()
+    ris = (C.c_void_p * max(len(lists), 1))()
+    vls = (C.c_void_p * max(len(lists), 1))()
+    for k, M in enumerate(lists):
+        cp = np.ascontiguousarray(M.colptr, np.int64)
+        ri = np.ascontiguousarray(M.rowidx, np.int64)
+        v = np.ascontiguousarray(M.values, dt) if M.values is not None else np.ones(len(ri), dt)
+        keep += [cp, ri, v]
+        cps[k], ris[k], vls[k] = cp.ctypes.data, ri.ctypes.data, v.ctypes.data
+    nnz = lib.ref_multiway_merge(sr, len(lists), m, n, cps, ris, vls)
+    if nnz < 0:
+        raise ValueError("bad semiring")
+    return _fetch(lib, nnz, dt)
+
+
+def _sr_add(sr: int, a, b):
+    if sr in (SR_MINPLUS_F64, SR_MINPLUS_I64, SR_SELECT2NDMIN_I64):
+        return np.where(b < a, b, a)  # std::min(a, b)
+    if sr == SR_BOOL:
+        return np.logical_or(a, b)
+    return a + b  # IEEE / wrap-around, as the reference's add
+
+
+def port_multiway_merge(lists, m: int, n: int, sr: int):
+    """Restatement of MultiwayMerge (MultiwayMerge.h:193-240 SerialMerge):
+    entries of all lists in column-major order, equal (row, col) combined
+    by SR::add in list order.  Returns a CSC (colptr, rows, vals)."""
+    dt = SR_DTYPE[sr]
+    rows, cols, vals, src = [], [], [], []
+    for k, M in enumerate(lists):
+        cnt = np.diff(M.colptr)
+        rows.append(np.asarray(M.rowidx, np.int64))
+        cols.append(np.repeat(np.arange(n, dtype=np.int64), cnt))
+        vals.append(np.asarray(M.values, dt) if M.values is not None else np.ones(int(M.colptr[-1]), dt))
+        src.append(np.full(int(M.colptr[-1]), k, np.int64))
+    if not lists:
+        return np.zeros(n + 1, np.int64), np.zeros(0, np.int64), np.zeros(0, dt)
+    r, c, v, k = (np.concatenate(x) for x in (rows, cols, vals, src))
+    order = np.lexsort((k, r, c))
+    r, c, v = r[order], c[order], v[order]
+    key = c * m + r
+    start = np.ones(len(key), bool)
+    start[1:] = key[1:] != key[:-1]
+    head = np.nonzero(start)[0]
+    run = np.cumsum(start) - 1
+    occ = np.arange(len(key)) - head[run]
+    acc = v[head].copy()
+    for level in range(1, int(occ.max(initial=0)) + 1):
+        sel = occ == level
+        acc[run[sel]] = _sr_add(sr, acc[run[sel]], v[sel])
+    rr, cc = r[head], c[head]
+    colptr = np.zeros(n + 1, np.int64)
+    colptr[1:] = np.cumsum(np.bincount(cc, minlength=n))
+    return colptr, rr, acc.astype(dt)
 
 
 def msbfs_loop(A, roots, multiply):

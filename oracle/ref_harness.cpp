@@ -16,6 +16,7 @@
 //                           Applications/SpMSpV-IPDPS2017/SpMSpVBench.cpp:105-156
 //   ref_mcl_expand       -> MemEfficientSpGEMM + MCLPruneRecoverySelect
 //                           (ParFriends.h:452,185)
+//   ref_multiway_merge   -> MultiwayMerge (MultiwayMerge.h:428)
 #include "CombBLAS/CombBLAS.h"
 #include "CombBLAS/mtSpGEMM.h"
 
@@ -193,6 +194,27 @@ int64_t run_spgemm(int variant, int64_t m, int64_t k, int64_t n, const int64_t *
     return nnz;
 }
 
+template <typename SR, typename NT>
+int64_t run_merge(int nlists, int64_t m, int64_t n, const int64_t *const *cps, const int64_t *const *ris,
+                  const void *const *vals)
+{
+    std::vector<SpTuples<int64_t, NT> *> lists;
+    for (int k = 0; k < nlists; ++k) {
+        auto t = csc_to_tuples<NT>(n, cps[k], ris[k], vals[k]);
+        auto *arr = new std::tuple<int64_t, int64_t, NT>[t.size()];
+        std::copy(t.begin(), t.end(), arr);
+        lists.push_back(new SpTuples<int64_t, NT>((int64_t)t.size(), m, n, arr, true, false));
+    }
+    double t0 = now();
+    SpTuples<int64_t, NT> *C = MultiwayMerge<SR>(lists, m, n, false);
+    g_res.seconds = now() - t0;
+    store_tuples(C);
+    const int64_t nnz = C->getnnz();
+    if (nlists != 1 || C != lists[0]) delete C;
+    for (auto *L : lists) delete L;
+    return nnz;
+}
+
 }  // namespace
 
 extern "C" {
@@ -215,6 +237,23 @@ int64_t ref_spgemm(int variant, int sr, int64_t m, int64_t k, int64_t n, const i
         case 4: return run_spgemm<HarnessSelect2ndMinSR<int64_t, int64_t>, int64_t>(variant, m, k, n, Acp, Ari, Av, Bcp, Bri, Bv, reps);
         case 5: return run_spgemm<PlusTimesSRing<bool, bool>, bool>(variant, m, k, n, Acp, Ari, Av, Bcp, Bri, Bv, reps);
         case 6: return run_spgemm<MinPlusSRing<int64_t, int64_t>, int64_t>(variant, m, k, n, Acp, Ari, Av, Bcp, Bri, Bv, reps);
+        default: return -1;
+    }
+}
+
+// MultiwayMerge<SR> (MultiwayMerge.h:428) of nlists CSC matrices of one
+// shape; result (column-major tuples) in g_res.
+int64_t ref_multiway_merge(int sr, int nlists, int64_t m, int64_t n, const int64_t *const *cps,
+                           const int64_t *const *ris, const void *const *vals)
+{
+    switch (sr) {
+        case 0: return run_merge<PlusTimesSRing<double, double>, double>(nlists, m, n, cps, ris, vals);
+        case 1: return run_merge<PlusTimesSRing<float, float>, float>(nlists, m, n, cps, ris, vals);
+        case 2: return run_merge<PlusTimesSRing<int64_t, int64_t>, int64_t>(nlists, m, n, cps, ris, vals);
+        case 3: return run_merge<MinPlusSRing<double, double>, double>(nlists, m, n, cps, ris, vals);
+        case 4: return run_merge<HarnessSelect2ndMinSR<int64_t, int64_t>, int64_t>(nlists, m, n, cps, ris, vals);
+        case 5: return run_merge<PlusTimesSRing<bool, bool>, bool>(nlists, m, n, cps, ris, vals);
+        case 6: return run_merge<MinPlusSRing<int64_t, int64_t>, int64_t>(nlists, m, n, cps, ris, vals);
         default: return -1;
     }
 }

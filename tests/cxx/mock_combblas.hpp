@@ -103,8 +103,12 @@ class SpTuples {
     ~SpTuples()
     {
         if (tuples && opnew_) ::operator delete(tuples);
+        else delete[] tuples;
     }
     int64_t getnnz() const { return nnz; }
+    IT rowindex(int64_t i) const { return std::get<0>(tuples[i]); }
+    IT colindex(int64_t i) const { return std::get<1>(tuples[i]); }
+    NT numvalue(int64_t i) const { return std::get<2>(tuples[i]); }
     IT getnrow() const { return m_; }
     IT getncol() const { return n_; }
     int64_t nnz;
@@ -182,6 +186,27 @@ SpTuples<IT, NTO> *LocalHybridSpGEMM(const SpCCols<IT, NT1> &, const SpCCols<IT,
     ++fallback_calls();
     return nullptr;
 }
+// column-sorted merge with equal keys combined in list order
+template <class SR, class IT, class NT>
+SpTuples<IT, NT> *MultiwayMerge(std::vector<SpTuples<IT, NT> *> &L, IT mdim = 0, IT ndim = 0, bool delarrs = false)
+{
+    ++fallback_calls();
+    std::map<std::pair<IT, IT>, NT> acc;  // (col, row)
+    for (auto *T : L)
+        for (int64_t p = 0; p < T->getnnz(); ++p) {
+            const auto key = std::make_pair(T->colindex(p), T->rowindex(p));
+            auto it = acc.find(key);
+            if (it == acc.end()) acc[key] = T->numvalue(p);
+            else it->second = SR::add(it->second, T->numvalue(p));
+        }
+    auto *t = new std::tuple<IT, IT, NT>[acc.size() + 1];
+    int64_t q = 0;
+    for (auto &e : acc) t[q++] = std::tuple<IT, IT, NT>(e.first.second, e.first.first, e.second);
+    if (delarrs)
+        for (auto *T : L) delete T;
+    return new SpTuples<IT, NT>(q, mdim, ndim, t, true, false);
+}
+
 template <class SR, class IT, class NUM, class IVT, class OVT>
 void SpMXSpV(const Csc<IT, NUM> &, int32_t, const int32_t *, const IVT *, int32_t, std::vector<int32_t> &,
              std::vector<OVT> &, PreAllocatedSPA<OVT> &)

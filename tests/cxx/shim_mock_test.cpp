@@ -198,6 +198,32 @@ int main()
             ++k;
         }
     }
+    // 8. MultiwayMerge of three products of one shape (GPU) against the CPU merge
+    {
+        SpDCCols<I, double> *X = random_dcsc<double>(600, 300, 0.02, 0.1, 8);
+        std::vector<SpTuples<I, double> *> lists, lists_cpu;
+        for (unsigned k = 0; k < 3; ++k) {
+            SpDCCols<I, double> *Y = random_dcsc<double>(300, 200, 0.03, 0.2, 20 + k);
+            lists.push_back(combblas::LocalHybridSpGEMM<PT, double>(*X, *Y, false, false));
+            lists_cpu.push_back(combblas::LocalHybridSpGEMM<PT, double>(*X, *Y, false, false));
+            delete Y;
+        }
+        const int fb = fallback_calls();
+        SpTuples<I, double> *mg = gbcomb::MultiwayMerge<PT>(lists, (I)600, (I)200, true);
+        EXPECT(fallback_calls() == fb);
+        SpTuples<I, double> *mc = combblas::MultiwayMerge<PT>(lists_cpu, (I)600, (I)200, true);
+        EXPECT(mg->getnnz() > 0 && same(mg, mc) && !mg->opnew_);
+        std::vector<SpTuples<I, double> *> bad{new SpTuples<I, double>(0, 600, 200),
+                                              new SpTuples<I, double>(0, 601, 200)};
+        SpTuples<I, double> *mb = gbcomb::MultiwayMerge<PT>(bad, (I)600, (I)200, true);
+        EXPECT(mb->getnnz() == 0 && mb->getnrow() == 0);
+        delete mb;
+        delete bad[0];
+        delete bad[1];
+        delete mg;
+        delete mc;
+        delete X;
+    }
     delete B2;
     delete Bs;
     delete Ai;

@@ -51,4 +51,9 @@ template void gbcomb::SpMXSpV<S2M, int64_t, int64_t, int64_t, int64_t>(
     const Csc<int64_t, int64_t> &, int32_t, const int32_t *, const int64_t *, int32_t, std::vector<int32_t> &,
     std::vector<int64_t> &, PreAllocatedSPA<int64_t> &);
 
+template SpTuples<int64_t, double> *gbcomb::MultiwayMerge<PTD, int64_t, double>(
+    std::vector<SpTuples<int64_t, double> *> &, int64_t, int64_t, bool);
+template SpTuples<int32_t, double> *gbcomb::MultiwayMerge<PTD, int32_t, double>(
+    std::vector<SpTuples<int32_t, double> *> &, int32_t, int32_t, bool);
+
 int main() { return 0; }

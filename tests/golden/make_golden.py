@@ -164,6 +164,20 @@ def main(ref_root: str):
         d[f"msbfs/{name}/roots"] = roots
         d[f"msbfs/{name}/parents"] = par
         d[f"msbfs/{name}/levels"] = np.array(lv)
+    # MultiwayMerge of overlapping lists (several SUMMA stages of one block)
+    base = G.random_sparse(400, 250, 0.04, seed=21)
+    rng = np.random.default_rng(22)
+    lists = [G.random_sparse(400, 250, 0.02, seed=30 + k) for k in range(3)]
+    lists = [base.with_values((1.0 - rng.random(base.nnz)) * 10.0 ** rng.integers(-6, 6, base.nnz))] + \
+        [M.with_values(1.0 - rng.random(M.nnz)) for M in lists]
+    for k, M in enumerate(lists):
+        put_mat(d, f"in/merge{k}", M)
+    for K in (2, 4):
+        for sr in (O.SR_PLUSTIMES_F64, O.SR_SELECT2NDMIN_I64):
+            L = [with_type(M, sr, 40 + k) if sr != O.SR_PLUSTIMES_F64 else M for k, M in enumerate(lists[:K])]
+            r, c, v = O.ref_multiway_merge(L, 400, 250, sr)
+            key = f"merge/{K}/{sr}"
+            d[f"{key}/rows"], d[f"{key}/cols"], d[f"{key}/vals"] = r, c, v
     # MCL expansion + prune/select
     M = G.mcl_planted(4096, 256, 10, 3, seed=5)
     put_mat(d, "in/mcl4096", M)

@@ -164,3 +164,24 @@ def test_port_msbfs(oracle_lib, golden):
             other = np.arange(M.ncol) != s
             assert np.array_equal(par[r][other], single[other]), (name, s)
             assert par[r][s] == s
+
+
+def merge_lists(golden, K, sr, O):
+    lists = [golden_matrix(golden, f"merge{k}") for k in range(K)]
+    if sr != O.SR_PLUSTIMES_F64:
+        lists = [typed(M, sr, 40 + k, O) for k, M in enumerate(lists)]
+    return lists
+
+
+def test_port_multiway_merge(oracle_lib, golden):
+    """MultiwayMerge restated: exact against the reference for two lists and
+    for min-type semirings; with more lists the reference's heap decides the
+    order of equal keys, so fp64 sums agree within 1e-12."""
+    O = oracle_lib
+    for K in (2, 4):
+        for sr in (O.SR_PLUSTIMES_F64, O.SR_SELECT2NDMIN_I64):
+            lists = merge_lists(golden, K, sr, O)
+            cp, rows, vals = O.port_multiway_merge(lists, 400, 250, sr)
+            key = f"merge/{K}/{sr}"
+            check_csc(cp, rows, vals, golden, key, sr, O.V_HYBRID, 250, O,
+                      exact_values=(K == 2 or sr != O.SR_PLUSTIMES_F64))
