@@ -487,6 +487,40 @@ def bench_mcl(ctx):
 
 
 
+def bench_spmv(A, ctx, stream, hbm, peak_kind, reps: int = 20):
+    """y <- y + A x (PlusTimes fp64) through a plan; HBM roofline of k_spmv."""
+    import torch
+    from combblas_gb300 import local as LC
+
+    t0 = time.perf_counter()
+    plan = LC.SpMVPlan(LC.DeviceMatrix.from_host(A), np.float64, ctx)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    x = torch.rand(A.ncol, dtype=torch.float64, device="cuda")
+    y = torch.zeros(A.nrow, dtype=torch.float64, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # 256 MB > L2 between runs
+    for _ in range(3):
+        plan.multiply(x.data_ptr(), y.data_ptr())
+    times = []
+    for _ in range(reps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plan.multiply(x.data_ptr(), y.data_ptr())
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms = float(np.median(times))
+    nnz, m, n = A.nnz, A.nrow, A.ncol
+    bytes_alg = nnz * (4 + 8) + n * 8 + (m + 1) * 8 + 2 * m * 8
+    plan.close()
+    return {"op": "y <- y + A x, PlusTimes fp64, R-MAT matrix of this line", "ms": ms,
+            "gflops": 2 * nnz / ms / 1e6, "achieved_gbs": bytes_alg / ms / 1e6, "peak": hbm, "peak_kind": peak_kind,
+            "frac": bytes_alg / ms / 1e6 / hbm, "bytes_alg": bytes_alg, "plan_build_s": build_s,
+            "l2": "256 MB written between runs"}
+
+
+
 def bench_msbfs(args, world, A, ctx, stream, hbm, peak_kind, scale, ef):
     """Multi-source BFS from MS_ROOTS seeded roots at once (the masked
     Select2ndMin SpGEMM loop); a step is one whole traversal."""
@@ -731,6 +765,10 @@ def run_ours(args, world, rank, local):
     if args.workload == "msbfs22":
         result.update(bench_msbfs(args, world, A, ctx, stream, hbm, peak_kind, scale, ef))
 
+    # ---- dense-vector SpMV on the same matrix (dcsc_gespmv) ---------------
+    if args.workload.startswith("spgemm") and not args.no_bfs:
+        result["spmv"] = bench_spmv(A, ctx, stream, hbm, peak_kind)
+
     # ---- BFS: 64 roots, level loop as a replayed CUDA graph --------------
     if args.workload == "bfs20" or (args.workload.startswith("spgemm") and not args.no_bfs):
         g = B.Graph(A.with_values(None), ctx)
@@ -805,7 +843,7 @@ def run_ours(args, world, rank, local):
                    "parallelism": f"replicas x{world}", **({"b_columns": args.bcols} if args.bcols else {})},
     }
     for k in ("roofline", "cpu_baseline", "e2e", "gpu_launches", "clocks", "spgemm", "exact_two_phase", "mcl", "bfs",
-              "msbfs", "batch"):
+              "msbfs", "batch", "spmv"):
         if k in result:
             line[k] = result[k]
     if rank == 0:

@@ -140,6 +140,9 @@ _SIGS.update({
                           C.c_int]),
     "gbc_msbfs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int,
                             C.POINTER(gbc_msbfs_stats)]),
+    "gbc_spmv_plan_create": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(gbc_matrix), C.POINTER(C.c_void_p)]),
+    "gbc_spmv_plan_destroy": (C.c_int, [C.c_void_p]),
+    "gbc_spmv": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int]),
     "gbc_multiway_merge": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int64, C.c_int64,
                                      C.POINTER(C.c_void_p), C.POINTER(gbc_spgemm_stats)]),
 })

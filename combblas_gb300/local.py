@@ -11,6 +11,8 @@ Names and argument meaning follow the reference calls the C ABI replaces:
   mtSpGEMM.h:806
 * ``MultiwayMerge(lists, mdim, ndim)`` -- MultiwayMerge.h:428-708 (the sum of
   several stages' products, equal entries combined in list order)
+* ``dcsc_gespmv(A, x, y)`` / ``SpMVPlan`` -- Friends.h:63-175 (y (+)= A x with a
+  dense vector)
 
 The semiring is given by name (the reference's template argument ``SR``):
 ``"plustimes"`` (PlusTimesSRing), ``"minplus"`` (MinPlusSRing),
@@ -295,6 +297,54 @@ def spgemm_phased(A, B, sr: str = "plustimes", max_phase_nnz: int = 1 << 31, ctx
                                       int(max_phase_nnz), L.SIZING_LEARNED if sizing == "learned" else L.SIZING_EXACT,
                                       C.byref(st)))
     return st
+
+
+class SpMVPlan:
+    """A, prepared for y <- y (+) A x (gbc_spmv_plan): dcsc_gespmv
+    (Friends.h:63-175) with A's rows held row-major on the device."""
+
+    def __init__(self, A, dtype=np.float64, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.dtype = np.dtype(dtype)
+        keep: list = []
+        g = as_gbc_matrix(A, keep, self.dtype)
+        self.h = C.c_void_p()
+        L.check(L.lib().gbc_spmv_plan_create(self.ctx.h, VT_OF_DTYPE[self.dtype], C.byref(g), C.byref(self.h)))
+        self.nrow, self.ncol = int(A.nrow), int(A.ncol)
+
+    def multiply(self, x, y, sr: str = "plustimes"):
+        """y (+)= A x; numpy arrays (updated in place and returned) or device
+        addresses (ints)."""
+        if isinstance(x, int):
+            L.check(L.lib().gbc_spmv(self.ctx.h, self.h, SR_CODES[sr], C.c_void_p(x), C.c_void_p(y), L.GBC_DEVICE))
+            return y
+        x = np.ascontiguousarray(x, self.dtype)
+        assert y.dtype == self.dtype and y.flags.c_contiguous
+        L.check(L.lib().gbc_spmv(self.ctx.h, self.h, SR_CODES[sr], x.ctypes.data, y.ctypes.data, L.GBC_HOST))
+        return y
+
+    def close(self):
+        if self.h:
+            L.lib().gbc_spmv_plan_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        if sys.is_finalizing():
+            return
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def dcsc_gespmv(A, x, y, sr: str = "plustimes", dtype=None):
+    """y (+)= A x, the reference's dcsc_gespmv (one-shot plan)."""
+    dt = np.dtype(dtype) if dtype is not None else np.asarray(y).dtype
+    plan = SpMVPlan(A, dt)
+    try:
+        return plan.multiply(x, y, sr)
+    finally:
+        plan.close()
 
 
 def MultiwayMerge(lists, mdim: int, ndim: int, sr: str = "plustimes", dtype=None,

@@ -172,6 +172,19 @@ typedef struct {
 int gbc_spgemm_phased(gbc_context *ctx, int sr, int vt, const gbc_matrix *A, const gbc_matrix *B,
                       int64_t max_phase_nnz, int sizing, gbc_phased_stats *st);
 
+/* Sparse matrix x dense vector, y <- y (+) A x over semiring `sr`:
+ * replaces dcsc_gespmv / dcsc_gespmv_threaded (Friends.h:63-175), whose row
+ * update is SR::axpy(a, x[col], y[row]).  A plan holds A row-major on the
+ * device (built once by a stable device radix sort); x (ncol) and y (nrow)
+ * are where-located arrays of the plan's value type.  Rows without entries
+ * keep y.  Min-type, boolean and integer semirings give the reference's
+ * result exactly; PlusTimes on floating values sums each row in a fixed
+ * order (repeatable, within rounding of the reference's column order). */
+typedef struct gbc_spmv_plan gbc_spmv_plan;
+int gbc_spmv_plan_create(gbc_context *ctx, int vt, const gbc_matrix *A, gbc_spmv_plan **plan);
+int gbc_spmv_plan_destroy(gbc_spmv_plan *plan);
+int gbc_spmv(gbc_context *ctx, const gbc_spmv_plan *plan, int sr, const void *x, void *y, int where);
+
 /* Sum of nlists matrices of one shape (nrow x ncol), entries with the same
  * (row, column) combined with the semiring's add in list order: replaces
  * MultiwayMerge<SR>(vector<SpTuples*>&, mdim, ndim, delarrs)

@@ -10,6 +10,7 @@
  *   gbcomb::LocalHybridSpGEMM<SR, NTO>(SpCCols A, SpCCols B, ...)  mtSpGEMM.h:1142-1152
  *   gbcomb::SpMXSpV<SR>(Csc, mA, indx, numx, veclen, indy, numy, SPA)  SpImpl.h:115-124
  *   gbcomb::MultiwayMerge<SR>(ArrSpTups, mdim, ndim, delarrs)  MultiwayMerge.h:428-708
+ *   gbcomb::dcsc_gespmv<SR>(A, x, y)                           Friends.h:63-77
  *
  * Same arguments, same ownership (inputs borrowed; clearA / clearB delete
  * them; the returned SpTuples owns a tuple array from ::operator new with
@@ -338,6 +339,25 @@ combblas::SpTuples<IT, NT> *MultiwayMerge(std::vector<combblas::SpTuples<IT, NT>
         if (delarrs)
             for (int k = 0; k < nlists; ++k) delete ArrSpTups[k];
         return new combblas::SpTuples<IT, NT>(nnz, mdim, ndim, tuples, true, false);
+    }
+}
+
+// y <- y (+) A x with dense vectors.  A row-major plan is built and
+// dropped per call; callers that multiply the same matrix repeatedly keep a
+// gbc_spmv_plan instead.
+template <class SR, class IU, class NU, class RHS, class LHS>
+void dcsc_gespmv(const combblas::SpDCCols<IU, NU> &A, const RHS *x, LHS *y)
+{
+    if constexpr (!detail::offloaded<SR, NU, IU, RHS, LHS>()) {
+        combblas::dcsc_gespmv<SR>(A, x, y);
+    } else {
+        if (A.isZero()) return;
+        const gbc_matrix g = detail::view(A);
+        gbc_spmv_plan *p = nullptr;
+        detail::check(gbc_spmv_plan_create(detail::context(), semiring_of<SR>::vt, &g, &p), "gbc_spmv_plan_create");
+        const int rc = gbc_spmv(detail::context(), p, semiring_of<SR>::sr, x, y, GBC_HOST);
+        gbc_spmv_plan_destroy(p);
+        detail::check(rc, "gbc_spmv");
     }
 }
 

@@ -92,6 +92,8 @@ def _ref():
         lib.ref_mcl_expand.argtypes = [C.c_int64, _P64, _P64, np.ctypeslib.ndpointer(dtype=np.float32),
                                        C.c_float, C.c_int64, C.c_int64, C.c_float]
         lib.ref_num_threads.restype = C.c_int
+        lib.ref_spmv.restype = C.c_int
+        lib.ref_spmv.argtypes = [C.c_int, C.c_int64, C.c_int64, _P64, _P64, C.c_void_p, C.c_void_p, C.c_void_p]
         lib.ref_multiway_merge.restype = C.c_int64
         lib.ref_multiway_merge.argtypes = [C.c_int, C.c_int, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
                                            C.c_void_p]
@@ -315,6 +317,45 @@ def port_multiway_merge(lists, m: int, n: int, sr: int):
     colptr = np.zeros(n + 1, np.int64)
     colptr[1:] = np.cumsum(np.bincount(cc, minlength=n))
     return colptr, rr, acc.astype(dt)
+
+
+def ref_spmv(A, x, y, sr: int):
+    """The reference's dcsc_gespmv<SR>: returns y (+) A x (y is copied)."""
+    lib = _ref()
+    dt = SR_DTYPE[sr]
+    v = np.ascontiguousarray(A.values, dt) if A.values is not None else np.ones(A.nnz, dt)
+    x = np.ascontiguousarray(x, dt)
+    y = np.array(y, dt)
+    if lib.ref_spmv(sr, A.nrow, A.ncol, np.ascontiguousarray(A.colptr), np.ascontiguousarray(A.rowidx),
+                    v.ctypes.data, x.ctypes.data, y.ctypes.data) != 0:
+        raise ValueError("bad semiring")
+    return y
+
+
+def port_spmv(A, x, y, sr: int):
+    """Restatement of dcsc_gespmv (Friends.h:63-77): for every column in
+    order, for its entries, y[row] = axpy(a, x[col], y[row]); returns a copy."""
+    dt = SR_DTYPE[sr]
+    y = np.array(y, dt)
+    x = np.asarray(x, dt)
+    v = np.asarray(A.values, dt) if A.values is not None else np.ones(A.nnz, dt)
+    for j in range(A.ncol):
+        s0, s1 = int(A.colptr[j]), int(A.colptr[j + 1])
+        if s0 == s1:
+            continue
+        r = A.rowidx[s0:s1]
+        a = v[s0:s1]
+        if sr in (SR_PLUSTIMES_F64, SR_PLUSTIMES_F32, SR_PLUSTIMES_I64):
+            y[r] = y[r] + a * x[j]
+        elif sr == SR_BOOL:
+            y[r] = np.logical_or(y[r], np.logical_and(a, x[j]))
+        elif sr in (SR_MINPLUS_F64, SR_MINPLUS_I64):
+            inf = np.finfo(dt).max if dt == np.float64 else np.iinfo(dt).max
+            t = np.where((a == inf) | (x[j] == inf), inf, a + x[j])
+            y[r] = np.where(t < y[r], t, y[r])
+        else:  # Select2ndMin: multiply returns x
+            y[r] = np.where(x[j] < y[r], x[j], y[r])
+    return y
 
 
 def msbfs_loop(A, roots, multiply):

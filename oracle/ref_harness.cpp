@@ -17,6 +17,7 @@
 //   ref_mcl_expand       -> MemEfficientSpGEMM + MCLPruneRecoverySelect
 //                           (ParFriends.h:452,185)
 //   ref_multiway_merge   -> MultiwayMerge (MultiwayMerge.h:428)
+//   ref_spmv             -> dcsc_gespmv (Friends.h:63)
 #include "CombBLAS/CombBLAS.h"
 #include "CombBLAS/mtSpGEMM.h"
 
@@ -215,6 +216,16 @@ int64_t run_merge(int nlists, int64_t m, int64_t n, const int64_t *const *cps, c
     return nnz;
 }
 
+template <typename SR, typename NT>
+int run_spmv(int64_t m, int64_t n, const int64_t *cp, const int64_t *ri, const void *v, const void *x, void *y)
+{
+    std::unique_ptr<SpDCCols<int64_t, NT>> A(make_dcsc<NT>(m, n, cp, ri, v));
+    double t0 = now();
+    dcsc_gespmv<SR>(*A, static_cast<const NT *>(x), static_cast<NT *>(y));
+    g_res.seconds = now() - t0;
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -254,6 +265,22 @@ int64_t ref_multiway_merge(int sr, int nlists, int64_t m, int64_t n, const int64
         case 4: return run_merge<HarnessSelect2ndMinSR<int64_t, int64_t>, int64_t>(nlists, m, n, cps, ris, vals);
         case 5: return run_merge<PlusTimesSRing<bool, bool>, bool>(nlists, m, n, cps, ris, vals);
         case 6: return run_merge<MinPlusSRing<int64_t, int64_t>, int64_t>(nlists, m, n, cps, ris, vals);
+        default: return -1;
+    }
+}
+
+// dcsc_gespmv<SR> (Friends.h:63): y <- y (+) A x in place.
+int ref_spmv(int sr, int64_t m, int64_t n, const int64_t *cp, const int64_t *ri, const void *v, const void *x,
+             void *y)
+{
+    switch (sr) {
+        case 0: return run_spmv<PlusTimesSRing<double, double>, double>(m, n, cp, ri, v, x, y);
+        case 1: return run_spmv<PlusTimesSRing<float, float>, float>(m, n, cp, ri, v, x, y);
+        case 2: return run_spmv<PlusTimesSRing<int64_t, int64_t>, int64_t>(m, n, cp, ri, v, x, y);
+        case 3: return run_spmv<MinPlusSRing<double, double>, double>(m, n, cp, ri, v, x, y);
+        case 4: return run_spmv<HarnessSelect2ndMinSR<int64_t, int64_t>, int64_t>(m, n, cp, ri, v, x, y);
+        case 5: return run_spmv<PlusTimesSRing<bool, bool>, bool>(m, n, cp, ri, v, x, y);
+        case 6: return run_spmv<MinPlusSRing<int64_t, int64_t>, int64_t>(m, n, cp, ri, v, x, y);
         default: return -1;
     }
 }

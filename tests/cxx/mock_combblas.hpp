@@ -186,6 +186,17 @@ SpTuples<IT, NTO> *LocalHybridSpGEMM(const SpCCols<IT, NT1> &, const SpCCols<IT,
     ++fallback_calls();
     return nullptr;
 }
+// y <- y (+) A x, columns in order (the reference's dcsc_gespmv)
+template <class SR, class IU, class NU, class RHS, class LHS>
+void dcsc_gespmv(const SpDCCols<IU, NU> &A, const RHS *x, LHS *y)
+{
+    ++fallback_calls();
+    const Dcsc<IU, NU> *d = A.GetDCSC();
+    for (IU q = 0; q < d->nzc; ++q)
+        for (IU p = d->cp[q]; p < d->cp[q + 1]; ++p)
+            y[d->ir[p]] = SR::add(y[d->ir[p]], SR::multiply(d->numx[p], x[d->jc[q]]));
+}
+
 // column-sorted merge with equal keys combined in list order
 template <class SR, class IT, class NT>
 SpTuples<IT, NT> *MultiwayMerge(std::vector<SpTuples<IT, NT> *> &L, IT mdim = 0, IT ndim = 0, bool delarrs = false)

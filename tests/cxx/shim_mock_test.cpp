@@ -224,6 +224,20 @@ int main()
         delete mc;
         delete X;
     }
+    // 9. dcsc_gespmv over MinPlus int64 (order-free: bit-exact) on the GPU
+    {
+        typedef MinPlusSRing<int64_t, int64_t> MP;
+        SpDCCols<I, int64_t> *M = random_dcsc<int64_t>(900, 400, 0.01, 0.2, 9);
+        std::vector<int64_t> x(400), yg(900), yc(900);
+        for (int j = 0; j < 400; ++j) x[j] = (j * 37) % 101;
+        for (int r = 0; r < 900; ++r) yg[r] = yc[r] = 50 + (r * 13) % 77;
+        const int fb = fallback_calls();
+        gbcomb::dcsc_gespmv<MP>(*M, x.data(), yg.data());
+        EXPECT(fallback_calls() == fb);
+        combblas::dcsc_gespmv<MP>(*M, x.data(), yc.data());
+        EXPECT(yg == yc);
+        delete M;
+    }
     delete B2;
     delete Bs;
     delete Ai;

@@ -56,4 +56,9 @@ template SpTuples<int64_t, double> *gbcomb::MultiwayMerge<PTD, int64_t, double>(
 template SpTuples<int32_t, double> *gbcomb::MultiwayMerge<PTD, int32_t, double>(
     std::vector<SpTuples<int32_t, double> *> &, int32_t, int32_t, bool);
 
+template void gbcomb::dcsc_gespmv<PTD, int64_t, double, double, double>(const SpDCCols<int64_t, double> &,
+                                                                       const double *, double *);
+template void gbcomb::dcsc_gespmv<PTD, int32_t, double, double, double>(const SpDCCols<int32_t, double> &,
+                                                                       const double *, double *);
+
 int main() { return 0; }

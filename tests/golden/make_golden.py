@@ -178,6 +178,19 @@ def main(ref_root: str):
             r, c, v = O.ref_multiway_merge(L, 400, 250, sr)
             key = f"merge/{K}/{sr}"
             d[f"{key}/rows"], d[f"{key}/cols"], d[f"{key}/vals"] = r, c, v
+    # dcsc_gespmv: y <- y (+) A x on rmat8
+    rng = np.random.default_rng(23)
+    for sr in (O.SR_PLUSTIMES_F64, O.SR_MINPLUS_F64, O.SR_SELECT2NDMIN_I64, O.SR_BOOL):
+        Mt = with_type(rm, sr, 50 + sr)
+        dt = O.SR_DTYPE[sr]
+        if dt == np.bool_:
+            x, y = rng.random(rm.ncol) < 0.5, rng.random(rm.nrow) < 0.2
+        elif dt == np.int64:
+            x, y = rng.integers(0, 100, rm.ncol), rng.integers(0, 200, rm.nrow)
+        else:
+            x, y = rng.random(rm.ncol), rng.random(rm.nrow) * 3
+        d[f"spmv/{sr}/x"], d[f"spmv/{sr}/y0"] = x, y
+        d[f"spmv/{sr}/y"] = O.ref_spmv(Mt, x, y, sr)
     # MCL expansion + prune/select
     M = G.mcl_planted(4096, 256, 10, 3, seed=5)
     put_mat(d, "in/mcl4096", M)

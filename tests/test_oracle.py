@@ -185,3 +185,13 @@ def test_port_multiway_merge(oracle_lib, golden):
             key = f"merge/{K}/{sr}"
             check_csc(cp, rows, vals, golden, key, sr, O.V_HYBRID, 250, O,
                       exact_values=(K == 2 or sr != O.SR_PLUSTIMES_F64))
+
+
+def test_port_spmv(oracle_lib, golden):
+    """dcsc_gespmv restated (column order, SR::axpy per entry) reproduces the
+    reference's own multiply bit for bit."""
+    O = oracle_lib
+    M = golden_matrix(golden, "rmat8")
+    for sr in (O.SR_PLUSTIMES_F64, O.SR_MINPLUS_F64, O.SR_SELECT2NDMIN_I64, O.SR_BOOL):
+        y = O.port_spmv(typed(M, sr, 50 + sr, O), golden[f"spmv/{sr}/x"], golden[f"spmv/{sr}/y0"], sr)
+        assert np.array_equal(y, golden[f"spmv/{sr}/y"]), sr
