@@ -383,27 +383,28 @@ __global__ void __launch_bounds__(kThreads, SUB <= 1024 ? 3 : SUB <= 2048 ? 2 : 
                 for (int64_t cb = bs; cb < be; cb += kThreads) {
                     int nseg;
                     const int L = load_chunk_nz<V>(a, ch, cb, be, t, t + 1, bval, ch_bv, SR::one(), nseg);
-                    for (int q = 0; q < L; q += kSub) {
-                        const int n = min(kSub, L - q);
-                        // 1. first segment of every 32-product window of the sub-batch:
-                        //    one binary search per window, in parallel
-                        const int rounds = (n + kThreads - 1) / kThreads;  // block-uniform
-                        if (tid < (n + 31) >> 5) s_win[tid] = chunk_find_nz(ch, nseg, q + tid * 32);
-                        __syncthreads();
-                        // 2. load: round r covers products [r*kThreads, (r+1)*kThreads) of
-                        //    the sub-batch, warp w its window at r*kThreads + 32w
-                        //    (coalesced; the unrolled rounds keep all loads in flight);
-                        //    the lanes' segments come from window_seg
-                        int o_[kSubPerThread];
-                        V v_[kSubPerThread];
+                    // Sub-batches are software pipelined: the global loads of
+                    // sub-batch q + kSub are issued right after sub-batch q is
+                    // scattered, so their latency overlaps q's fold.
+                    int o_[kSubPerThread];
+                    V v_[kSubPerThread];
+                    // 1. first segment of every 32-product window of a sub-batch:
+                    //    one binary search per window, in parallel
+                    // 2. load: round r covers products [r*kThreads, (r+1)*kThreads)
+                    //    of the sub-batch, warp w its window at r*kThreads + 32w
+                    //    (coalesced; the unrolled rounds keep all loads in flight);
+                    //    the lanes' segments come from window_seg
+                    auto load_sub = [&](int q0) {
+                        const int n0 = min(kSub, L - q0);
+                        const int rounds0 = (n0 + kThreads - 1) / kThreads;
 #pragma unroll
                         for (int r = 0; r < kSubPerThread; ++r) {
                             o_[r] = -1;
-                            const int P = q + r * kThreads + warp * 32;
-                            if (r < rounds && P < q + n) {  // warp-uniform
+                            const int P = q0 + r * kThreads + warp * 32;
+                            if (r < rounds0 && P < q0 + n0) {  // warp-uniform
                                 const int p = P + lane;
                                 const int b = window_seg(ch, nseg, s_win[r * kWarps + warp], p);
-                                if (p < q + n) {
+                                if (p < q0 + n0) {
                                     const int64_t idx = (int64_t)ch.s[b] + (p - ch.off[b]);
                                     o_[r] = a.arow[idx] - row0;
                                     const V av = aval ? aval[idx] : SR::one();
@@ -411,6 +412,15 @@ __global__ void __launch_bounds__(kThreads, SUB <= 1024 ? 3 : SUB <= 2048 ? 2 : 
                                 }
                             }
                         }
+                    };
+                    if (L > 0) {
+                        if (tid < (min(kSub, L) + 31) >> 5) s_win[tid] = chunk_find_nz(ch, nseg, tid * 32);
+                        __syncthreads();
+                        load_sub(0);
+                    }
+                    for (int q = 0; q < L; q += kSub) {
+                        const int n = min(kSub, L - q);
+                        const int rounds = (n + kThreads - 1) / kThreads;  // block-uniform
                         // 3. stable partition by owner warp (row_owner): rank
                         //    within (round, warp) from 3 ballots; counts laid out
                         //    [owner][round][warp] so the scan follows product order
@@ -483,7 +493,13 @@ __global__ void __launch_bounds__(kThreads, SUB <= 1024 ? 3 : SUB <= 2048 ? 2 : 
                                 sval[pos] = v_[r];
                             }
                         }
+                        // windows of the next sub-batch (s_win was last read by its
+                        // own loads, issued before this sub-batch's barriers)
+                        const int qn = q + kSub;
+                        if (qn < L && tid < (min(kSub, L - qn) + 31) >> 5)
+                            s_win[tid] = chunk_find_nz(ch, nseg, qn + tid * 32);
                         __syncthreads();
+                        if (qn < L) load_sub(qn);  // o_/v_ of q were consumed by the scatter
                         // 6. each warp folds its bucket in staging (= k) order.  A window
                         //    whose rows are distinct (tag test: every lane stores its id
                         //    at its row's tag and reads it back) folds lane-parallel;
