@@ -14,7 +14,7 @@ constexpr int kBuckets = kWarps;         // one staging bucket per owner warp
 constexpr int kStage = 2048;             // products staged per sub-batch
 constexpr int kRounds = kStage / kThreads;
 constexpr int kTileRows = 8192;          // default rows of the dense accumulator tile (two blocks per SM at fp64)
-constexpr int kSymRows = 1 << 20;        // rows covered by one symbolic bitmap
+constexpr int kSymRows = 1 << 18;        // rows of one symbolic bitmap pass (32 KB: five blocks per SM)
 constexpr int kMaxMaskWords = 64;        // tile-mask words per column (64 tiles each)
 
 // Device view of the operands after preparation.  Rows of A are int32 and
