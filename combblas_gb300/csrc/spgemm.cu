@@ -325,7 +325,7 @@ static_assert(kWarps == 8, "row_owner returns 3 bits");
 __device__ __forceinline__ int row_owner(int o) { return (int)(((uint32_t)o * 0x9E3779B1u) >> 29); }
 
 template <class SR, int SUB>
-__global__ void __launch_bounds__(kThreads, SUB <= 1024 ? 3 : SUB <= 2048 ? 2 : 1) k_numeric(const SpgemmArgs *args, const int64_t *items, int64_t nitems,
+__global__ void __launch_bounds__(kThreads, SUB <= 1024 ? 4 : SUB <= 2048 ? 2 : 1) k_numeric(const SpgemmArgs *args, const int64_t *items, int64_t nitems,
                                                          const int64_t *ccp, int64_t ccp_base, const int64_t *cap,
                                                          int64_t *out_cnt, int32_t *overflow, int64_t *cir,
                                                          void *cval_v, unsigned long long *work)
@@ -660,7 +660,7 @@ int prepare_operands(Workspace &ws, const DevMatrix &A, const DevMatrix &B, Spge
     a.kdim = A.ncol;
     a.n = B.ncol;
     a.nb = B.nzc;
-    // default tile: 4096 rows (three blocks per SM) up to 2^18 rows, else
+    // default tile: 4096 rows (four blocks per SM) up to 2^18 rows, else
     // 8192 (two blocks per SM, half the tile passes per column)
     const int rows = (tile_rows == 4096 || tile_rows == 8192 || tile_rows == 16384) ? tile_rows
                      : (A.nrow <= (int64_t(1) << 18))                             ? 4096
@@ -955,7 +955,7 @@ static int run_numeric(Context *ctx, Plan &P, const Lists &L, const int64_t *ccp
             const size_t num_smem = numeric_smem_bytes(P.max_R, sizeof(V), 1024);
             GBC_TRY(set_smem(k_numeric<SR, 1024>, num_smem));
             int per_sm = std::max(1, (int)(ctx->smem_optin / (num_smem + 6144)));
-            k_numeric<SR, 1024><<<grid_for(ctx, L.n[2], std::min(per_sm, 3)), kThreads, num_smem, s>>>(
+            k_numeric<SR, 1024><<<grid_for(ctx, L.n[2], std::min(per_sm, 4)), kThreads, num_smem, s>>>(
                 P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir, cval, P.work + 1);
         } else {
             const size_t num_smem = numeric_smem_bytes(P.max_R, sizeof(V), 2048);

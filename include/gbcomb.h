@@ -78,7 +78,7 @@ typedef struct {
                         view); 0: drop empty output columns (SpDCCols view) */
     int tile_rows;   /* rows of the block kernel's accumulator tile: 0 = 4096
                         up to 2^18 rows of A and 8192 above, or 4096 / 8192 /
-                        16384; 4096-row tiles run three blocks per SM, 8192
+                        16384; 4096-row tiles run four blocks per SM, 8192
                         two, 16384 one */
     int64_t tiny_limit;  /* columns with <= this many multiplications use the
                             smallest warp kernel (<= 256; -1 = default 256) */
