@@ -321,30 +321,37 @@ __global__ void __launch_bounds__(kThreads) k_symbolic(const SpgemmArgs *args, c
 // bit of an R-MAT row id is skewed (set with probability c + d), so any
 // owner taken from a few row bits gets a fixed share far above 1/kWarps;
 // the hash spreads rows evenly and leaves only single hot rows.
-static_assert(kWarps == 8, "row_owner returns 3 bits");
-__device__ __forceinline__ int row_owner(int o) { return (int)(((uint32_t)o * 0x9E3779B1u) >> 29); }
+template <int LB>
+__device__ __forceinline__ int row_owner(int o) { return (int)(((uint32_t)o * 0x9E3779B1u) >> (32 - LB)); }
 
-template <class SR, int SUB>
-__global__ void __launch_bounds__(kThreads, SUB <= 1024 ? 4 : SUB <= 2048 ? 2 : 1) k_numeric(const SpgemmArgs *args, const int64_t *items, int64_t nitems,
+// NT threads per block (256 or 512), SUB products per sub-batch.
+template <int NT, int SUB>
+constexpr int numeric_min_blocks() { return NT == 512 ? 2 : SUB <= 1024 ? 4 : SUB <= 2048 ? 2 : 1; }
+
+template <class SR, int SUB, int NT>
+__global__ void __launch_bounds__(NT, numeric_min_blocks<NT, SUB>()) k_numeric(const SpgemmArgs *args, const int64_t *items, int64_t nitems,
                                                          const int64_t *ccp, int64_t ccp_base, const int64_t *cap,
                                                          int64_t *out_cnt, int32_t *overflow, int64_t *cir,
                                                          void *cval_v, unsigned long long *work)
 {
     typedef typename SR::V V;
     constexpr int kSub = SUB;
-    constexpr int kSubPerThread = SUB / kThreads;
+    constexpr int NW = NT / 32;                      // warps = owners
+    constexpr int LB = NW == 16 ? 4 : 3;             // owner bits
+    static_assert(NW == (1 << LB), "8 or 16 warps");
+    constexpr int kSubPerThread = SUB / NT;
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ ChunkSmem ch;
-    __shared__ V ch_bv[kThreads];
-    __shared__ int32_t s_cnt[kWarps * kSubPerThread * kWarps + 1];  // [owner][round][warp]
-    __shared__ int32_t s_wsum[kWarps];
+    __shared__ ChunkSmemN<NT> ch;
+    __shared__ V ch_bv[NT];
+    __shared__ int32_t s_cnt[NW * kSubPerThread * NW + 1];  // [owner][round][warp]
+    __shared__ int32_t s_wsum[NW];
     __shared__ int32_t s_win[SUB / 32];
     __shared__ int64_t s_col;
     __shared__ SpgemmArgs sa;
     V *cval = static_cast<V *>(cval_v);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned lt = (1u << lane) - 1;
-    constexpr int NC = kWarps * kSubPerThread * kWarps;
+    constexpr int NC = NW * kSubPerThread * NW;
 
     for (;;) {
         if (tid == 0) {
@@ -378,37 +385,43 @@ __global__ void __launch_bounds__(kThreads, SUB <= 1024 ? 4 : SUB <= 2048 ? 2 : 
                 const int t = mw * 64 + __ffsll((long long)msk) - 1;
                 msk &= msk - 1;
                 const int row0 = t * a.R;
-                for (int w = tid; w < words; w += kThreads) bm[w] = 0;
+                for (int w = tid; w < words; w += NT) bm[w] = 0;
                 __syncthreads();
-                for (int64_t cb = bs; cb < be; cb += kThreads) {
+                for (int64_t cb = bs; cb < be; cb += NT) {
                     int nseg;
                     const int L = load_chunk_nz<V>(a, ch, cb, be, t, t + 1, bval, ch_bv, SR::one(), nseg);
                     // Sub-batches are software pipelined: the global loads of
                     // sub-batch q + kSub are issued right after sub-batch q is
                     // scattered, so their latency overlaps q's fold.
-                    int o_[kSubPerThread];
-                    V v_[kSubPerThread];
+                    // Raw loads of a sub-batch, kept unconsumed until its
+                    // partition: row (-1: no product), A value, segment.
+                    int ar_[kSubPerThread];
+                    V av_[kSubPerThread];
+                    int sg_[kSubPerThread];
                     // 1. first segment of every 32-product window of a sub-batch:
                     //    one binary search per window, in parallel
-                    // 2. load: round r covers products [r*kThreads, (r+1)*kThreads)
-                    //    of the sub-batch, warp w its window at r*kThreads + 32w
+                    // 2. load: round r covers products [r*NT, (r+1)*NT) of the
+                    //    sub-batch, warp w its window at r*NT + 32w
                     //    (coalesced; the unrolled rounds keep all loads in flight);
-                    //    the lanes' segments come from window_seg
+                    //    the lanes' segments come from window_seg.  Nothing reads
+                    //    the loaded registers here, so the loads stay in flight
+                    //    through the fold that follows; the product with B(k,j)
+                    //    is formed at the scatter
                     auto load_sub = [&](int q0) {
                         const int n0 = min(kSub, L - q0);
-                        const int rounds0 = (n0 + kThreads - 1) / kThreads;
+                        const int rounds0 = (n0 + NT - 1) / NT;
 #pragma unroll
                         for (int r = 0; r < kSubPerThread; ++r) {
-                            o_[r] = -1;
-                            const int P = q0 + r * kThreads + warp * 32;
+                            ar_[r] = -1;
+                            const int P = q0 + r * NT + warp * 32;
                             if (r < rounds0 && P < q0 + n0) {  // warp-uniform
                                 const int p = P + lane;
-                                const int b = window_seg(ch, nseg, s_win[r * kWarps + warp], p);
+                                const int b = window_seg(ch, nseg, s_win[r * NW + warp], p);
                                 if (p < q0 + n0) {
                                     const int64_t idx = (int64_t)ch.s[b] + (p - ch.off[b]);
-                                    o_[r] = a.arow[idx] - row0;
-                                    const V av = aval ? aval[idx] : SR::one();
-                                    v_[r] = SR::mul(av, ch_bv[b]);
+                                    ar_[r] = a.arow[idx];
+                                    av_[r] = aval ? aval[idx] : SR::one();
+                                    sg_[r] = b;
                                 }
                             }
                         }
@@ -420,7 +433,7 @@ __global__ void __launch_bounds__(kThreads, SUB <= 1024 ? 4 : SUB <= 2048 ? 2 : 
                     }
                     for (int q = 0; q < L; q += kSub) {
                         const int n = min(kSub, L - q);
-                        const int rounds = (n + kThreads - 1) / kThreads;  // block-uniform
+                        const int rounds = (n + NT - 1) / NT;  // block-uniform
                         // 3. stable partition by owner warp (row_owner): rank
                         //    within (round, warp) from 3 ballots; counts laid out
                         //    [owner][round][warp] so the scan follows product order
@@ -428,23 +441,25 @@ __global__ void __launch_bounds__(kThreads, SUB <= 1024 ? 4 : SUB <= 2048 ? 2 : 
 #pragma unroll
                         for (int r = 0; r < kSubPerThread; ++r) {
                             if (r < rounds) {
-                                const bool act = o_[r] >= 0;
-                                const int w = row_owner(o_[r]);
+                                const bool act = ar_[r] >= 0;
+                                const int w = row_owner<LB>(ar_[r] - row0);
                                 const unsigned va = __ballot_sync(0xffffffffu, act);
-                                const unsigned b0 = __ballot_sync(0xffffffffu, act && (w & 1));
-                                const unsigned b1 = __ballot_sync(0xffffffffu, act && (w & 2));
-                                const unsigned b2 = __ballot_sync(0xffffffffu, act && (w & 4));
-                                const unsigned same =
-                                    va & ((w & 1) ? b0 : ~b0) & ((w & 2) ? b1 : ~b1) & ((w & 4) ? b2 : ~b2);
+                                unsigned bb[LB];
+#pragma unroll
+                                for (int i = 0; i < LB; ++i) bb[i] = __ballot_sync(0xffffffffu, act && ((w >> i) & 1));
+                                unsigned same = va;
+#pragma unroll
+                                for (int i = 0; i < LB; ++i) same &= ((w >> i) & 1) ? bb[i] : ~bb[i];
                                 rk_[r] = __popc(same & lt);
-                                // lanes 0..kWarps-1 publish the size of owner `lane`'s group
-                                if (lane < kWarps) {
-                                    const unsigned sl = va & ((lane & 1) ? b0 : ~b0) & ((lane & 2) ? b1 : ~b1) &
-                                                        ((lane & 4) ? b2 : ~b2);
-                                    s_cnt[(lane * kSubPerThread + r) * kWarps + warp] = __popc(sl);
+                                // lanes 0..NW-1 publish the size of owner `lane`'s group
+                                if (lane < NW) {
+                                    unsigned sl = va;
+#pragma unroll
+                                    for (int i = 0; i < LB; ++i) sl &= ((lane >> i) & 1) ? bb[i] : ~bb[i];
+                                    s_cnt[(lane * kSubPerThread + r) * NW + warp] = __popc(sl);
                                 }
-                            } else if (lane < kWarps) {
-                                s_cnt[(lane * kSubPerThread + r) * kWarps + warp] = 0;
+                            } else if (lane < NW) {
+                                s_cnt[(lane * kSubPerThread + r) * NW + warp] = 0;
                             }
                         }
                         __syncthreads();
@@ -452,7 +467,8 @@ __global__ void __launch_bounds__(kThreads, SUB <= 1024 ? 4 : SUB <= 2048 ? 2 : 
                         //    consecutive counts per thread, warp scan, one barrier for
                         //    the warp totals
                         {
-                            constexpr int PER = NC / kThreads;
+                            constexpr int PER = NC / NT;
+                            static_assert(PER * NT == NC, "counts split evenly over the threads");
                             int loc[PER];
                             int sum = 0;
 #pragma unroll
@@ -470,7 +486,7 @@ __global__ void __launch_bounds__(kThreads, SUB <= 1024 ? 4 : SUB <= 2048 ? 2 : 
                             __syncthreads();
                             int base = x - sum, tot = 0;
 #pragma unroll
-                            for (int u = 0; u < kWarps; ++u) {
+                            for (int u = 0; u < NW; ++u) {
                                 const int ws = s_wsum[u];
                                 base += u < warp ? ws : 0;
                                 tot += ws;
@@ -486,11 +502,12 @@ __global__ void __launch_bounds__(kThreads, SUB <= 1024 ? 4 : SUB <= 2048 ? 2 : 
                         // 5. scatter into owner buckets
 #pragma unroll
                         for (int r = 0; r < kSubPerThread; ++r) {
-                            if (r < rounds && o_[r] >= 0) {
-                                const int w = row_owner(o_[r]);
-                                const int pos = s_cnt[(w * kSubPerThread + r) * kWarps + warp] + rk_[r];
-                                srow[pos] = (uint16_t)o_[r];
-                                sval[pos] = v_[r];
+                            if (r < rounds && ar_[r] >= 0) {
+                                const int o = ar_[r] - row0;
+                                const int w = row_owner<LB>(o);
+                                const int pos = s_cnt[(w * kSubPerThread + r) * NW + warp] + rk_[r];
+                                srow[pos] = (uint16_t)o;
+                                sval[pos] = SR::mul(av_[r], ch_bv[sg_[r]]);
                             }
                         }
                         // windows of the next sub-batch (s_win was last read by its
@@ -499,15 +516,15 @@ __global__ void __launch_bounds__(kThreads, SUB <= 1024 ? 4 : SUB <= 2048 ? 2 : 
                         if (qn < L && tid < (min(kSub, L - qn) + 31) >> 5)
                             s_win[tid] = chunk_find_nz(ch, nseg, qn + tid * 32);
                         __syncthreads();
-                        if (qn < L) load_sub(qn);  // o_/v_ of q were consumed by the scatter
+                        if (qn < L) load_sub(qn);  // the registers of q were consumed by the scatter
                         // 6. each warp folds its bucket in staging (= k) order.  A window
                         //    whose rows are distinct (tag test: every lane stores its id
                         //    at its row's tag and reads it back) folds lane-parallel;
                         //    otherwise equal rows are grouped with __match_any_sync and
                         //    the lowest lane folds the group in lane order
                         {
-                            const int beg = s_cnt[warp * kWarps * kSubPerThread];
-                            const int end = s_cnt[(warp + 1) * kWarps * kSubPerThread];
+                            const int beg = s_cnt[warp * NW * kSubPerThread];
+                            const int end = s_cnt[(warp + 1) * NW * kSubPerThread];
                             for (int p0 = beg; p0 < end; p0 += 32) {
                                 const int p = p0 + lane;
                                 const bool act = p < end;
@@ -542,7 +559,7 @@ __global__ void __launch_bounds__(kThreads, SUB <= 1024 ? 4 : SUB <= 2048 ? 2 : 
                 // 32-word groups so stores stay contiguous
                 {
                     int wl = 0;
-                    const int wpt = (words + kThreads - 1) / kThreads;
+                    const int wpt = (words + NT - 1) / NT;
                     const int w0 = min(words, tid * wpt), w1 = min(words, (tid + 1) * wpt);
                     for (int w = w0; w < w1; ++w) wl += __popc(bm[w]);
                     int x = wl;
@@ -555,7 +572,7 @@ __global__ void __launch_bounds__(kThreads, SUB <= 1024 ? 4 : SUB <= 2048 ? 2 : 
                     __syncthreads();
                     int before = 0, tot = 0;
 #pragma unroll
-                    for (int u = 0; u < kWarps; ++u) {
+                    for (int u = 0; u < NW; ++u) {
                         const int ws = s_wsum[u];
                         before += u < warp ? ws : 0;
                         tot += ws;
@@ -576,7 +593,7 @@ __global__ void __launch_bounds__(kThreads, SUB <= 1024 ? 4 : SUB <= 2048 ? 2 : 
                             }
                         }
                         __syncthreads();
-                        for (int p = tid; p < tot; p += kThreads) {
+                        for (int p = tid; p < tot; p += NT) {
                             const int64_t pos = out + p;
                             if (pos < lim) {
                                 cir[pos] = (int64_t)row0 + srow[p];
@@ -947,21 +964,22 @@ static int run_numeric(Context *ctx, Plan &P, const Lists &L, const int64_t *ccp
         GBC_CUDA_TRY(cudaMemsetAsync(P.work + 1, 0, sizeof(unsigned long long), s));
         if (P.max_R > 8192) {
             const size_t num_smem = numeric_smem_bytes(P.max_R, sizeof(V), 4096);
-            GBC_TRY(set_smem(k_numeric<SR, 4096>, num_smem));
+            GBC_TRY(set_smem(k_numeric<SR, 4096, kThreads>, num_smem));
             int per_sm = std::max(1, (int)(ctx->smem_optin / (num_smem + 12288)));
-            k_numeric<SR, 4096><<<grid_for(ctx, L.n[2], std::min(per_sm, 8)), kThreads, num_smem, s>>>(
+            k_numeric<SR, 4096, kThreads><<<grid_for(ctx, L.n[2], std::min(per_sm, 8)), kThreads, num_smem, s>>>(
                 P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir, cval, P.work + 1);
         } else if (P.max_R <= 4096) {
             const size_t num_smem = numeric_smem_bytes(P.max_R, sizeof(V), 1024);
-            GBC_TRY(set_smem(k_numeric<SR, 1024>, num_smem));
+            GBC_TRY(set_smem(k_numeric<SR, 1024, kThreads>, num_smem));
             int per_sm = std::max(1, (int)(ctx->smem_optin / (num_smem + 6144)));
-            k_numeric<SR, 1024><<<grid_for(ctx, L.n[2], std::min(per_sm, 4)), kThreads, num_smem, s>>>(
+            k_numeric<SR, 1024, kThreads><<<grid_for(ctx, L.n[2], std::min(per_sm, 4)), kThreads, num_smem, s>>>(
                 P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir, cval, P.work + 1);
         } else {
+            // 8192-row tiles: 512-thread blocks, two per SM (64 registers)
             const size_t num_smem = numeric_smem_bytes(P.max_R, sizeof(V), 2048);
-            GBC_TRY(set_smem(k_numeric<SR, 2048>, num_smem));
-            int per_sm = std::max(1, (int)(ctx->smem_optin / (num_smem + 8192)));
-            k_numeric<SR, 2048><<<grid_for(ctx, L.n[2], std::min(per_sm, 8)), kThreads, num_smem, s>>>(
+            GBC_TRY(set_smem(k_numeric<SR, 2048, 512>, num_smem));
+            int per_sm = std::max(1, (int)(ctx->smem_optin / (num_smem + 14336)));
+            k_numeric<SR, 2048, 512><<<grid_for(ctx, L.n[2], std::min(per_sm, 2)), 512, num_smem, s>>>(
                 P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir, cval, P.work + 1);
         }
         note_launch();

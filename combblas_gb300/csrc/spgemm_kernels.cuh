@@ -43,10 +43,13 @@ __host__ __device__ __forceinline__ int64_t make_item(int pid, int64_t col) { re
 __host__ __device__ __forceinline__ int item_pid(int64_t it) { return (int)(it >> 32); }
 __host__ __device__ __forceinline__ int64_t item_col(int64_t it) { return it & 0xffffffffll; }
 
-// Block-wide exclusive sum (kThreads threads); *total gets the block total.
+// Block-wide exclusive sum (NT threads); *total gets the block total.
+template <int NT = kThreads>
 __device__ __forceinline__ int64_t block_exclusive_sum64(int64_t v, int64_t *total)
 {
-    __shared__ int64_t ws[kWarps];
+    constexpr int NW = NT / 32;
+    static_assert(NW <= 32, "one warp scans the warp totals");
+    __shared__ int64_t ws[NW];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     int64_t x = v;
 #pragma unroll
@@ -57,36 +60,39 @@ __device__ __forceinline__ int64_t block_exclusive_sum64(int64_t v, int64_t *tot
     if (lane == 31) ws[wid] = x;
     __syncthreads();
     if (wid == 0) {
-        int64_t s = lane < kWarps ? ws[lane] : 0;
+        int64_t s = lane < NW ? ws[lane] : 0;
 #pragma unroll
-        for (int o = 1; o < kWarps; o <<= 1) {
+        for (int o = 1; o < NW; o <<= 1) {
             int64_t y = __shfl_up_sync(0xffffffffu, s, o);
             if (lane >= o) s += y;
         }
-        if (lane < kWarps) ws[lane] = s;
+        if (lane < NW) ws[lane] = s;
     }
     __syncthreads();
     int64_t base = wid ? ws[wid - 1] : 0;
-    if (total) *total = ws[kWarps - 1];
+    if (total) *total = ws[NW - 1];
     __syncthreads();
     return base + x - v;
 }
 
-// One chunk of up to kThreads consecutive entries of a B column: for entry
-// b, the A segment [s[b], s[b] + len) restricted to row tiles [t0, t1), and
-// off[] the exclusive prefix of the segment lengths (off[kThreads] = total).
-struct ChunkSmem {
-    uint32_t s[kThreads];
-    int32_t off[kThreads + 1];
+// One chunk of up to NT consecutive entries of a B column (NT = threads of
+// the block): for entry b, the A segment [s[b], s[b] + len) restricted to
+// row tiles [t0, t1), and off[] the exclusive prefix of the segment lengths
+// (off[NT] = total).
+template <int NT>
+struct ChunkSmemN {
+    uint32_t s[NT];
+    int32_t off[NT + 1];
 };
+typedef ChunkSmemN<kThreads> ChunkSmem;
 
 // Load one chunk, keeping only the non-empty segments: ch.s / ch.off (and
 // ch_bv) hold the nseg non-empty segments in entry order, ch.off[nseg] =
 // total.
 // One block scan packs the segment length (high word) with a non-empty
 // flag (low word), giving offsets and compacted positions together.
-template <typename V>
-__device__ __forceinline__ int load_chunk_nz(const SpgemmArgs &a, ChunkSmem &ch, int64_t cb, int64_t be, int t0,
+template <typename V, int NT>
+__device__ __forceinline__ int load_chunk_nz(const SpgemmArgs &a, ChunkSmemN<NT> &ch, int64_t cb, int64_t be, int t0,
                                              int t1, const V *bval, V *ch_bv, V one, int &nseg)
 {
     const int tid = threadIdx.x;
@@ -102,7 +108,7 @@ __device__ __forceinline__ int load_chunk_nz(const SpgemmArgs &a, ChunkSmem &ch,
         if (ch_bv && bval) bv = bval[b];
     }
     int64_t tot;
-    const int64_t ex = block_exclusive_sum64(((int64_t)len << 32) | (len > 0 ? 1 : 0), &tot);
+    const int64_t ex = block_exclusive_sum64<NT>(((int64_t)len << 32) | (len > 0 ? 1 : 0), &tot);
     if (len > 0) {
         const int c = (int)(ex & 0xffffffff);
         ch.s[c] = s;
@@ -116,7 +122,8 @@ __device__ __forceinline__ int load_chunk_nz(const SpgemmArgs &a, ChunkSmem &ch,
 }
 
 // Largest segment b < nseg with ch.off[b] <= p (warp-uniform p: broadcast reads).
-__device__ __forceinline__ int chunk_find_nz(const ChunkSmem &ch, int nseg, int p)
+template <int NT>
+__device__ __forceinline__ int chunk_find_nz(const ChunkSmemN<NT> &ch, int nseg, int p)
 {
     int lo = 0, hi = nseg;
     while (hi - lo > 1) {
@@ -134,7 +141,8 @@ __device__ __forceinline__ int chunk_find_nz(const ChunkSmem &ch, int nseg, int 
 // window start within it): lane k holds the boundary ch.off[bcur+1+k] and a
 // five-step binary search over the lanes counts the boundaries <= p.  All
 // lanes of the warp must call it.
-__device__ __forceinline__ int window_seg(const ChunkSmem &ch, int nseg, int bcur, int p)
+template <int NT>
+__device__ __forceinline__ int window_seg(const ChunkSmemN<NT> &ch, int nseg, int bcur, int p)
 {
     const int lane = threadIdx.x & 31;
     const int o = ch.off[min(bcur + 1 + lane, nseg)];
