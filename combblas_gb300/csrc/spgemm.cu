@@ -314,8 +314,8 @@ __global__ void __launch_bounds__(kThreads) k_symbolic(const SpgemmArgs *args, c
 //    writes each product into its owner's bucket in shared memory, keeping
 //    k order inside every bucket;
 //  * folding: each warp walks its bucket in 32-product windows.  Equal rows
-//    in a window are grouped with __match_any_sync and the lowest lane folds
-//    the group in lane order.  Each output entry is thus the left fold
+//    in a window are grouped (row tag winner + shared-memory group masks) and
+//    the lowest lane folds the group in lane order.  Each output entry is thus the left fold
 //    acc = add(mrhs, acc) over k ascending, with no atomics on values.
 // Owner warp of tile row o: the top bits of a multiplicative hash.  Every
 // bit of an R-MAT row id is skewed (set with probability c + d), so any
@@ -346,6 +346,7 @@ __global__ void __launch_bounds__(NT, numeric_min_blocks<NT, SUB>()) k_numeric(c
     __shared__ int32_t s_cnt[NW * kSubPerThread * NW + 1];  // [owner][round][warp]
     __shared__ int32_t s_wsum[NW];
     __shared__ int32_t s_win[SUB / 32];
+    __shared__ uint32_t s_grp[NT];  // per warp: group mask of each winner lane
     __shared__ int64_t s_col;
     __shared__ SpgemmArgs sa;
     V *cval = static_cast<V *>(cval_v);
@@ -517,24 +518,33 @@ __global__ void __launch_bounds__(NT, numeric_min_blocks<NT, SUB>()) k_numeric(c
                             s_win[tid] = chunk_find_nz(ch, nseg, qn + tid * 32);
                         __syncthreads();
                         if (qn < L) load_sub(qn);  // the registers of q were consumed by the scatter
-                        // 6. each warp folds its bucket in staging (= k) order.  A window
-                        //    whose rows are distinct (tag test: every lane stores its id
-                        //    at its row's tag and reads it back) folds lane-parallel;
-                        //    otherwise equal rows are grouped with __match_any_sync and
-                        //    the lowest lane folds the group in lane order
+                        // 6. each warp folds its bucket in staging (= k) order.  Every
+                        //    lane stores its id at its row's tag and reads back the
+                        //    row's winner; a window whose rows are distinct folds
+                        //    lane-parallel.  Otherwise each lane ORs its bit into the
+                        //    winner's group mask (shared memory, one word per lane),
+                        //    and the lowest lane of each group folds it in lane
+                        //    order.  (The atomic group masks cost far less than
+                        //    __match_any_sync, whose throughput falls to about one per
+                        //    64 SM cycles on windows of distinct rows.)
                         {
                             const int beg = s_cnt[warp * NW * kSubPerThread];
                             const int end = s_cnt[(warp + 1) * NW * kSubPerThread];
+                            uint32_t *gm = s_grp + warp * 32;
                             for (int p0 = beg; p0 < end; p0 += 32) {
                                 const int p = p0 + lane;
                                 const bool act = p < end;
-                                const int o = act ? (int)srow[p] : (0x10000 + lane);
+                                const int o = act ? (int)srow[p] : 0;
                                 if (act) tag[o] = (uint8_t)lane;
+                                gm[lane] = 0;
                                 __syncwarp();
-                                const bool clash = act && tag[o] != (uint8_t)lane;
-                                const unsigned grp = __ballot_sync(0xffffffffu, clash)
-                                                         ? __match_any_sync(0xffffffffu, o)
-                                                         : (1u << lane);
+                                const int wl = act ? (int)tag[o] : lane;
+                                unsigned grp = 1u << lane;
+                                if (__ballot_sync(0xffffffffu, wl != lane)) {
+                                    if (act) atomicOr(&gm[wl], 1u << lane);
+                                    __syncwarp();
+                                    if (act) grp = gm[wl];
+                                }
                                 if (act && (grp & lt) == 0) {
                                     const uint32_t bit = 1u << (o & 31);
                                     const bool touched = (bm[o >> 5] & bit) != 0;
@@ -978,7 +988,7 @@ static int run_numeric(Context *ctx, Plan &P, const Lists &L, const int64_t *ccp
             // 8192-row tiles: 512-thread blocks, two per SM (64 registers)
             const size_t num_smem = numeric_smem_bytes(P.max_R, sizeof(V), 2048);
             GBC_TRY(set_smem(k_numeric<SR, 2048, 512>, num_smem));
-            int per_sm = std::max(1, (int)(ctx->smem_optin / (num_smem + 14336)));
+            int per_sm = std::max(1, (int)(ctx->smem_optin / (num_smem + 16384)));
             k_numeric<SR, 2048, 512><<<grid_for(ctx, L.n[2], std::min(per_sm, 2)), 512, num_smem, s>>>(
                 P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir, cval, P.work + 1);
         }
