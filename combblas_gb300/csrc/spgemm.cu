@@ -380,259 +380,302 @@ __global__ void __launch_bounds__(NT, numeric_min_blocks<NT, SUB>()) k_numeric(c
         int64_t out = out0;
         const int64_t lim = cap ? out0 + cap[g] : ccp[g - ccp_base + 1];
         bool over = false;
-        for (int mw = 0; mw < a.mask_words; ++mw) {
-            uint64_t msk = a.tmask[i * a.mask_words + mw];
-            while (msk) {
-                const int t = mw * 64 + __ffsll((long long)msk) - 1;
-                msk &= msk - 1;
-                const int row0 = t * a.R;
-                for (int w = tid; w < words; w += NT) bm[w] = 0;
-                __syncthreads();
-                for (int64_t cb = bs; cb < be; cb += NT) {
-                    int nseg;
-                    const int L = load_chunk_nz<V>(a, ch, cb, be, t, t + 1, bval, ch_bv, SR::one(), nseg);
-                    // Sub-batches are software pipelined: the global loads of
-                    // sub-batch q + kSub are issued right after sub-batch q is
-                    // scattered, so their latency overlaps q's fold.
-                    // Raw loads of a sub-batch, kept unconsumed until its
-                    // partition: row (-1: no product), A value, segment.
-                    int ar_[kSubPerThread];
-                    V av_[kSubPerThread];
-                    int sg_[kSubPerThread];
-                    // 1. first segment of every 32-product window of a sub-batch:
-                    //    one binary search per window, in parallel
-                    // 2. load: round r covers products [r*NT, (r+1)*NT) of the
-                    //    sub-batch, warp w its window at r*NT + 32w
-                    //    (coalesced; the unrolled rounds keep all loads in flight);
-                    //    the lanes' segments come from window_seg.  Nothing reads
-                    //    the loaded registers here, so the loads stay in flight
-                    //    through the fold that follows; the product with B(k,j)
-                    //    is formed at the scatter
-                    auto load_sub = [&](int q0) {
-                        const int n0 = min(kSub, L - q0);
-                        const int rounds0 = (n0 + NT - 1) / NT;
-#pragma unroll
-                        for (int r = 0; r < kSubPerThread; ++r) {
-                            ar_[r] = -1;
-                            const int P = q0 + r * NT + warp * 32;
-                            if (r < rounds0 && P < q0 + n0) {  // warp-uniform
-                                const int p = P + lane;
-                                const int b = window_seg(ch, nseg, s_win[r * NW + warp], p);
-                                if (p < q0 + n0) {
-                                    const int64_t idx = (int64_t)ch.s[b] + (p - ch.off[b]);
-                                    ar_[r] = a.arow[idx];
-                                    av_[r] = aval ? aval[idx] : SR::one();
-                                    sg_[r] = b;
-                                }
-                            }
-                        }
-                    };
-                    if (L > 0) {
-                        if (tid < (min(kSub, L) + 31) >> 5) s_win[tid] = chunk_find_nz(ch, nseg, tid * 32);
-                        __syncthreads();
-                        load_sub(0);
-                    }
-                    for (int q = 0; q < L; q += kSub) {
-                        const int n = min(kSub, L - q);
-                        const int rounds = (n + NT - 1) / NT;  // block-uniform
-                        // 3. stable partition by owner warp (row_owner): rank
-                        //    within (round, warp) from 3 ballots; counts laid out
-                        //    [owner][round][warp] so the scan follows product order
-                        int rk_[kSubPerThread];
-#pragma unroll
-                        for (int r = 0; r < kSubPerThread; ++r) {
-                            if (r < rounds) {
-                                const bool act = ar_[r] >= 0;
-                                const int w = row_owner<LB>(ar_[r] - row0);
-                                const unsigned va = __ballot_sync(0xffffffffu, act);
-                                unsigned bb[LB];
-#pragma unroll
-                                for (int i = 0; i < LB; ++i) bb[i] = __ballot_sync(0xffffffffu, act && ((w >> i) & 1));
-                                unsigned same = va;
-#pragma unroll
-                                for (int i = 0; i < LB; ++i) same &= ((w >> i) & 1) ? bb[i] : ~bb[i];
-                                rk_[r] = __popc(same & lt);
-                                // lanes 0..NW-1 publish the size of owner `lane`'s group
-                                if (lane < NW) {
-                                    unsigned sl = va;
-#pragma unroll
-                                    for (int i = 0; i < LB; ++i) sl &= ((lane >> i) & 1) ? bb[i] : ~bb[i];
-                                    s_cnt[(lane * kSubPerThread + r) * NW + warp] = __popc(sl);
-                                }
-                            } else if (lane < NW) {
-                                s_cnt[(lane * kSubPerThread + r) * NW + warp] = 0;
-                            }
-                        }
-                        __syncthreads();
-                        // 4. exclusive scan of the (owner, round, warp) counts: PER
-                        //    consecutive counts per thread, warp scan, one barrier for
-                        //    the warp totals
-                        {
-                            constexpr int PER = NC / NT;
-                            static_assert(PER * NT == NC, "counts split evenly over the threads");
-                            int loc[PER];
-                            int sum = 0;
-#pragma unroll
-                            for (int u = 0; u < PER; ++u) {
-                                loc[u] = s_cnt[tid * PER + u];
-                                sum += loc[u];
-                            }
-                            int x = sum;
-#pragma unroll
-                            for (int o = 1; o < 32; o <<= 1) {
-                                const int y = __shfl_up_sync(0xffffffffu, x, o);
-                                if (lane >= o) x += y;
-                            }
-                            if (lane == 31) s_wsum[warp] = x;
-                            __syncthreads();
-                            int base = x - sum, tot = 0;
-#pragma unroll
-                            for (int u = 0; u < NW; ++u) {
-                                const int ws = s_wsum[u];
-                                base += u < warp ? ws : 0;
-                                tot += ws;
-                            }
-#pragma unroll
-                            for (int u = 0; u < PER; ++u) {
-                                s_cnt[tid * PER + u] = base;
-                                base += loc[u];
-                            }
-                            if (tid == 0) s_cnt[NC] = tot;
-                        }
-                        __syncthreads();
-                        // 5. scatter into owner buckets
-#pragma unroll
-                        for (int r = 0; r < kSubPerThread; ++r) {
-                            if (r < rounds && ar_[r] >= 0) {
-                                const int o = ar_[r] - row0;
-                                const int w = row_owner<LB>(o);
-                                const int pos = s_cnt[(w * kSubPerThread + r) * NW + warp] + rk_[r];
-                                srow[pos] = (uint16_t)o;
-                                sval[pos] = SR::mul(av_[r], ch_bv[sg_[r]]);
-                            }
-                        }
-                        // windows of the next sub-batch (s_win was last read by its
-                        // own loads, issued before this sub-batch's barriers)
-                        const int qn = q + kSub;
-                        if (qn < L && tid < (min(kSub, L - qn) + 31) >> 5)
-                            s_win[tid] = chunk_find_nz(ch, nseg, qn + tid * 32);
-                        __syncthreads();
-                        if (qn < L) load_sub(qn);  // the registers of q were consumed by the scatter
-                        // 6. each warp folds its bucket in staging (= k) order.  Every
-                        //    lane stores its id at its row's tag and reads back the
-                        //    row's winner; a window whose rows are distinct folds
-                        //    lane-parallel.  Otherwise each lane ORs its bit into the
-                        //    winner's group mask (shared memory, one word per lane),
-                        //    and the lowest lane of each group folds it in lane
-                        //    order.  (The atomic group masks cost far less than
-                        //    __match_any_sync, whose throughput falls to about one per
-                        //    64 SM cycles on windows of distinct rows.)
-                        {
-                            const int beg = s_cnt[warp * NW * kSubPerThread];
-                            const int end = s_cnt[(warp + 1) * NW * kSubPerThread];
-                            uint32_t *gm = s_grp + warp * 32;
-                            for (int p0 = beg; p0 < end; p0 += 32) {
-                                const int p = p0 + lane;
-                                const bool act = p < end;
-                                const int o = act ? (int)srow[p] : 0;
-                                if (act) tag[o] = (uint8_t)lane;
-                                gm[lane] = 0;
-                                __syncwarp();
-                                const int wl = act ? (int)tag[o] : lane;
-                                unsigned grp = 1u << lane;
-                                if (__ballot_sync(0xffffffffu, wl != lane)) {
-                                    if (act) atomicOr(&gm[wl], 1u << lane);
-                                    __syncwarp();
-                                    if (act) grp = gm[wl];
-                                }
-                                if (act && (grp & lt) == 0) {
-                                    const uint32_t bit = 1u << (o & 31);
-                                    const bool touched = (bm[o >> 5] & bit) != 0;
-                                    V *ap = acc + o;
-                                    V cur = touched ? SR::add(sval[p], *ap) : sval[p];
-                                    unsigned rest = grp & ~(1u << lane);
-                                    while (rest) {
-                                        const int m = __ffs(rest) - 1;
-                                        rest &= rest - 1;
-                                        cur = SR::add(sval[p0 + m], cur);
-                                    }
-                                    *ap = cur;
-                                    if (!touched) atomicOr(&bm[o >> 5], bit);
-                                }
-                                __syncwarp();
-                            }
-                        }
-                        __syncthreads();
-                    }
-                }
-                // write the tile's entries in row order: warp-cooperative over
-                // 32-word groups so stores stay contiguous
-                {
-                    int wl = 0;
-                    const int wpt = (words + NT - 1) / NT;
-                    const int w0 = min(words, tid * wpt), w1 = min(words, (tid + 1) * wpt);
-                    for (int w = w0; w < w1; ++w) wl += __popc(bm[w]);
-                    int x = wl;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const int y = __shfl_up_sync(0xffffffffu, x, o);
-                        if (lane >= o) x += y;
-                    }
-                    if (lane == 31) s_wsum[warp] = x;
-                    __syncthreads();
-                    int before = 0, tot = 0;
-#pragma unroll
-                    for (int u = 0; u < NW; ++u) {
-                        const int ws = s_wsum[u];
-                        before += u < warp ? ws : 0;
-                        tot += ws;
-                    }
-                    if (tot <= kSub) {
-                        // stage the tile's entries in row order in shared memory,
-                        // then store them with consecutive threads on
-                        // consecutive positions
-                        int q = before + x - wl;
-                        for (int w = w0; w < w1; ++w) {
-                            uint32_t bits = bm[w];
-                            while (bits) {
-                                const int o = w * 32 + __ffs(bits) - 1;
-                                bits &= bits - 1;
-                                srow[q] = (uint16_t)o;
-                                sval[q] = acc[o];
-                                ++q;
-                            }
-                        }
-                        __syncthreads();
-                        for (int p = tid; p < tot; p += NT) {
-                            const int64_t pos = out + p;
-                            if (pos < lim) {
-                                cir[pos] = (int64_t)row0 + srow[p];
-                                cval[pos] = sval[p];
-                            } else {
-                                over = true;  // never write past the column's range
-                            }
-                        }
-                    } else {
-                        int64_t pos = out + before + x - wl;
-                        for (int w = w0; w < w1; ++w) {
-                            uint32_t bits = bm[w];
-                            while (bits) {
-                                const int o = w * 32 + __ffs(bits) - 1;
-                                bits &= bits - 1;
-                                if (pos < lim) {
-                                    cir[pos] = (int64_t)row0 + o;
-                                    cval[pos] = acc[o];
-                                } else {
-                                    over = true;
-                                }
-                                ++pos;
-                            }
-                        }
-                    }
-                    out += tot;
-                }
-                __syncthreads();
+        // the touched bitmap starts clear (its place depends on this
+        // product's R); every tile's write-out clears it again.  The barriers
+        // of the first chunk load order this before any fold.
+        for (int w = tid; w < words; w += NT) bm[w] = 0;
+        // Touched row tiles in order; next_tile() gives the next one, or -1.
+        int mwi = 0;
+        uint64_t msk = a.tmask[i * a.mask_words];
+        auto next_tile = [&]() -> int {
+            while (msk == 0) {
+                if (++mwi >= a.mask_words) return -1;
+                msk = a.tmask[i * a.mask_words + mwi];
             }
+            const int tt = mwi * 64 + __ffsll((long long)msk) - 1;
+            msk &= msk - 1;
+            return tt;
+        };
+        // A column of at most NT entries is one chunk: thread tid keeps its
+        // entry's A column in bk, and the segment bounds of the next touched
+        // tile are loaded one tile ahead (ps, pe), so the chunk of a tile
+        // waits on no dependent global loads.
+        const bool single = be - bs <= NT;
+        int bk = -1;
+        uint32_t ps = 0, pe = 0;
+        int t = next_tile();
+        if (single && tid < be - bs) {
+            bk = a.brow[bs + tid];
+            if (t >= 0) {
+                const uint32_t *tp = a.tptr + (int64_t)bk * (a.T + 1);
+                ps = tp[t];
+                pe = tp[t + 1];
+            }
+        }
+        while (t >= 0) {
+            const int tn = next_tile();
+            const int row0 = t * a.R;
+            for (int64_t cb = bs; cb < be; cb += NT) {
+                int nseg, L;
+                if (single) {
+                    const uint32_t s0 = ps;
+                    const int len0 = bk >= 0 ? (int)(pe - ps) : 0;
+                    const V bv = (bk >= 0 && bval) ? bval[bs + tid] : SR::one();
+                    if (bk >= 0 && tn >= 0) {
+                        const uint32_t *tp = a.tptr + (int64_t)bk * (a.T + 1);
+                        ps = tp[tn];
+                        pe = tp[tn + 1];
+                    }
+                    L = compact_chunk<V, NT>(ch, s0, len0, bv, ch_bv, nseg);
+                } else {
+                    L = load_chunk_nz<V>(a, ch, cb, be, t, t + 1, bval, ch_bv, SR::one(), nseg);
+                }
+                // Sub-batches are software pipelined: the global loads of
+                // sub-batch q + kSub are issued right after sub-batch q is
+                // scattered, so their latency overlaps q's fold.
+                // Raw loads of a sub-batch, kept unconsumed until its
+                // partition: row (-1: no product), A value, segment.
+                int ar_[kSubPerThread];
+                V av_[kSubPerThread];
+                int sg_[kSubPerThread];
+                // 1. first segment of every 32-product window of a sub-batch:
+                //    one binary search per window, in parallel
+                // 2. load: round r covers products [r*NT, (r+1)*NT) of the
+                //    sub-batch, warp w its window at r*NT + 32w
+                //    (coalesced; the unrolled rounds keep all loads in flight);
+                //    the lanes' segments come from window_seg.  Nothing reads
+                //    the loaded registers here, so the loads stay in flight
+                //    through the fold that follows; the product with B(k,j)
+                //    is formed at the scatter
+                auto load_sub = [&](int q0) {
+                    const int n0 = min(kSub, L - q0);
+                    const int rounds0 = (n0 + NT - 1) / NT;
+#pragma unroll
+                    for (int r = 0; r < kSubPerThread; ++r) {
+                        ar_[r] = -1;
+                        const int P = q0 + r * NT + warp * 32;
+                        if (r < rounds0 && P < q0 + n0) {  // warp-uniform
+                            const int p = P + lane;
+                            const int b = window_seg(ch, nseg, s_win[r * NW + warp], p);
+                            if (p < q0 + n0) {
+                                const int64_t idx = (int64_t)ch.s[b] + (p - ch.off[b]);
+                                ar_[r] = a.arow[idx];
+                                av_[r] = aval ? aval[idx] : SR::one();
+                                sg_[r] = b;
+                            }
+                        }
+                    }
+                };
+                if (L > 0) {
+                    if (tid < (min(kSub, L) + 31) >> 5) s_win[tid] = chunk_find_nz(ch, nseg, tid * 32);
+                    __syncthreads();
+                    load_sub(0);
+                }
+                for (int q = 0; q < L; q += kSub) {
+                    const int n = min(kSub, L - q);
+                    const int rounds = (n + NT - 1) / NT;  // block-uniform
+                    // 3. stable partition by owner warp (row_owner): rank
+                    //    within (round, warp) from 3 ballots; counts laid out
+                    //    [owner][round][warp] so the scan follows product order
+                    int rk_[kSubPerThread];
+#pragma unroll
+                    for (int r = 0; r < kSubPerThread; ++r) {
+                        if (r < rounds) {
+                            const bool act = ar_[r] >= 0;
+                            const int w = row_owner<LB>(ar_[r] - row0);
+                            const unsigned va = __ballot_sync(0xffffffffu, act);
+                            unsigned bb[LB];
+#pragma unroll
+                            for (int i = 0; i < LB; ++i) bb[i] = __ballot_sync(0xffffffffu, act && ((w >> i) & 1));
+                            unsigned same = va;
+#pragma unroll
+                            for (int i = 0; i < LB; ++i) same &= ((w >> i) & 1) ? bb[i] : ~bb[i];
+                            rk_[r] = __popc(same & lt);
+                            // lanes 0..NW-1 publish the size of owner `lane`'s group
+                            if (lane < NW) {
+                                unsigned sl = va;
+#pragma unroll
+                                for (int i = 0; i < LB; ++i) sl &= ((lane >> i) & 1) ? bb[i] : ~bb[i];
+                                s_cnt[(lane * kSubPerThread + r) * NW + warp] = __popc(sl);
+                            }
+                        } else if (lane < NW) {
+                            s_cnt[(lane * kSubPerThread + r) * NW + warp] = 0;
+                        }
+                    }
+                    __syncthreads();
+                    // 4. exclusive scan of the (owner, round, warp) counts: PER
+                    //    consecutive counts per thread, warp scan, one barrier for
+                    //    the warp totals
+                    {
+                        constexpr int PER = NC / NT;
+                        static_assert(PER * NT == NC, "counts split evenly over the threads");
+                        int loc[PER];
+                        int sum = 0;
+#pragma unroll
+                        for (int u = 0; u < PER; ++u) {
+                            loc[u] = s_cnt[tid * PER + u];
+                            sum += loc[u];
+                        }
+                        int x = sum;
+#pragma unroll
+                        for (int o = 1; o < 32; o <<= 1) {
+                            const int y = __shfl_up_sync(0xffffffffu, x, o);
+                            if (lane >= o) x += y;
+                        }
+                        if (lane == 31) s_wsum[warp] = x;
+                        __syncthreads();
+                        int base = x - sum, tot = 0;
+#pragma unroll
+                        for (int u = 0; u < NW; ++u) {
+                            const int ws = s_wsum[u];
+                            base += u < warp ? ws : 0;
+                            tot += ws;
+                        }
+#pragma unroll
+                        for (int u = 0; u < PER; ++u) {
+                            s_cnt[tid * PER + u] = base;
+                            base += loc[u];
+                        }
+                        if (tid == 0) s_cnt[NC] = tot;
+                    }
+                    __syncthreads();
+                    // 5. scatter into owner buckets
+#pragma unroll
+                    for (int r = 0; r < kSubPerThread; ++r) {
+                        if (r < rounds && ar_[r] >= 0) {
+                            const int o = ar_[r] - row0;
+                            const int w = row_owner<LB>(o);
+                            const int pos = s_cnt[(w * kSubPerThread + r) * NW + warp] + rk_[r];
+                            srow[pos] = (uint16_t)o;
+                            sval[pos] = SR::mul(av_[r], ch_bv[sg_[r]]);
+                        }
+                    }
+                    // windows of the next sub-batch (s_win was last read by its
+                    // own loads, issued before this sub-batch's barriers)
+                    const int qn = q + kSub;
+                    if (qn < L && tid < (min(kSub, L - qn) + 31) >> 5)
+                        s_win[tid] = chunk_find_nz(ch, nseg, qn + tid * 32);
+                    __syncthreads();
+                    if (qn < L) load_sub(qn);  // the registers of q were consumed by the scatter
+                    // 6. each warp folds its bucket in staging (= k) order.  Every
+                    //    lane stores its id at its row's tag and reads back the
+                    //    row's winner; a window whose rows are distinct folds
+                    //    lane-parallel.  Otherwise each lane ORs its bit into the
+                    //    winner's group mask (shared memory, one word per lane),
+                    //    and the lowest lane of each group folds it in lane
+                    //    order.  (The atomic group masks cost far less than
+                    //    __match_any_sync, whose throughput falls to about one per
+                    //    64 SM cycles on windows of distinct rows.)
+                    {
+                        const int beg = s_cnt[warp * NW * kSubPerThread];
+                        const int end = s_cnt[(warp + 1) * NW * kSubPerThread];
+                        uint32_t *gm = s_grp + warp * 32;
+                        for (int p0 = beg; p0 < end; p0 += 32) {
+                            const int p = p0 + lane;
+                            const bool act = p < end;
+                            const int o = act ? (int)srow[p] : 0;
+                            if (act) tag[o] = (uint8_t)lane;
+                            gm[lane] = 0;
+                            __syncwarp();
+                            const int wl = act ? (int)tag[o] : lane;
+                            unsigned grp = 1u << lane;
+                            if (__ballot_sync(0xffffffffu, wl != lane)) {
+                                if (act) atomicOr(&gm[wl], 1u << lane);
+                                __syncwarp();
+                                if (act) grp = gm[wl];
+                            }
+                            if (act && (grp & lt) == 0) {
+                                const uint32_t bit = 1u << (o & 31);
+                                const bool touched = (bm[o >> 5] & bit) != 0;
+                                V *ap = acc + o;
+                                V cur = touched ? SR::add(sval[p], *ap) : sval[p];
+                                unsigned rest = grp & ~(1u << lane);
+                                while (rest) {
+                                    const int m = __ffs(rest) - 1;
+                                    rest &= rest - 1;
+                                    cur = SR::add(sval[p0 + m], cur);
+                                }
+                                *ap = cur;
+                                if (!touched) atomicOr(&bm[o >> 5], bit);
+                            }
+                            __syncwarp();
+                        }
+                    }
+                    __syncthreads();
+                }
+            }
+            // write the tile's entries in row order: each thread takes its
+            // words of the touched bitmap (clearing them for the next
+            // tile), entries are staged in row order in shared memory and
+            // stored by consecutive threads
+            {
+                int wl = 0;
+                const int wpt = (words + NT - 1) / NT;
+                const int w0 = min(words, tid * wpt), w1 = min(words, (tid + 1) * wpt);
+                for (int w = w0; w < w1; ++w) wl += __popc(bm[w]);
+                int x = wl;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, x, o);
+                    if (lane >= o) x += y;
+                }
+                if (lane == 31) s_wsum[warp] = x;
+                __syncthreads();
+                int before = 0, tot = 0;
+#pragma unroll
+                for (int u = 0; u < NW; ++u) {
+                    const int ws = s_wsum[u];
+                    before += u < warp ? ws : 0;
+                    tot += ws;
+                }
+                if (tot <= kSub) {
+                    // stage the tile's entries in row order in shared memory,
+                    // then store them with consecutive threads on
+                    // consecutive positions
+                    int q = before + x - wl;
+                    for (int w = w0; w < w1; ++w) {
+                        uint32_t bits = bm[w];
+                        bm[w] = 0;  // clear for the next tile
+                        while (bits) {
+                            const int o = w * 32 + __ffs(bits) - 1;
+                            bits &= bits - 1;
+                            srow[q] = (uint16_t)o;
+                            sval[q] = acc[o];
+                            ++q;
+                        }
+                    }
+                    __syncthreads();
+                    for (int p = tid; p < tot; p += NT) {
+                        const int64_t pos = out + p;
+                        if (pos < lim) {
+                            cir[pos] = (int64_t)row0 + srow[p];
+                            cval[pos] = sval[p];
+                        } else {
+                            over = true;  // never write past the column's range
+                        }
+                    }
+                } else {
+                    int64_t pos = out + before + x - wl;
+                    for (int w = w0; w < w1; ++w) {
+                        uint32_t bits = bm[w];
+                        bm[w] = 0;  // clear for the next tile
+                        while (bits) {
+                            const int o = w * 32 + __ffs(bits) - 1;
+                            bits &= bits - 1;
+                            if (pos < lim) {
+                                cir[pos] = (int64_t)row0 + o;
+                                cval[pos] = acc[o];
+                            } else {
+                                over = true;
+                            }
+                            ++pos;
+                        }
+                    }
+                }
+                out += tot;
+            }
+            __syncthreads();
+            t = tn;
         }
         over = __syncthreads_or(over);
         if (tid == 0) {

@@ -86,27 +86,16 @@ struct ChunkSmemN {
 };
 typedef ChunkSmemN<kThreads> ChunkSmem;
 
-// Load one chunk, keeping only the non-empty segments: ch.s / ch.off (and
-// ch_bv) hold the nseg non-empty segments in entry order, ch.off[nseg] =
-// total.
-// One block scan packs the segment length (high word) with a non-empty
-// flag (low word), giving offsets and compacted positions together.
+// Compact one chunk whose segments are already known per thread (start s,
+// length len, B value bv; len 0 for threads past the chunk), keeping only
+// the non-empty segments: ch.s / ch.off (and ch_bv) hold the nseg non-empty
+// segments in entry order, ch.off[nseg] = total.  One block scan packs the
+// segment length (high word) with a non-empty flag (low word), giving
+// offsets and compacted positions together.  Returns the total.
 template <typename V, int NT>
-__device__ __forceinline__ int load_chunk_nz(const SpgemmArgs &a, ChunkSmemN<NT> &ch, int64_t cb, int64_t be, int t0,
-                                             int t1, const V *bval, V *ch_bv, V one, int &nseg)
+__device__ __forceinline__ int compact_chunk(ChunkSmemN<NT> &ch, uint32_t s, int len, V bv, V *ch_bv, int &nseg)
 {
     const int tid = threadIdx.x;
-    const int64_t b = cb + tid;
-    int len = 0;
-    uint32_t s = 0;
-    V bv = one;
-    if (b < be) {
-        const int k = a.brow[b];
-        const uint32_t *tp = a.tptr + (int64_t)k * (a.T + 1);
-        s = tp[t0];
-        len = (int)(tp[t1] - s);
-        if (ch_bv && bval) bv = bval[b];
-    }
     int64_t tot;
     const int64_t ex = block_exclusive_sum64<NT>(((int64_t)len << 32) | (len > 0 ? 1 : 0), &tot);
     if (len > 0) {
@@ -119,6 +108,26 @@ __device__ __forceinline__ int load_chunk_nz(const SpgemmArgs &a, ChunkSmemN<NT>
     if (tid == 0) ch.off[nseg] = (int)(tot >> 32);
     __syncthreads();
     return (int)(tot >> 32);
+}
+
+// Load one chunk of B entries [cb, min(cb + NT, be)) restricted to row tiles
+// [t0, t1) and compact it (compact_chunk).
+template <typename V, int NT>
+__device__ __forceinline__ int load_chunk_nz(const SpgemmArgs &a, ChunkSmemN<NT> &ch, int64_t cb, int64_t be, int t0,
+                                             int t1, const V *bval, V *ch_bv, V one, int &nseg)
+{
+    const int64_t b = cb + threadIdx.x;
+    int len = 0;
+    uint32_t s = 0;
+    V bv = one;
+    if (b < be) {
+        const int k = a.brow[b];
+        const uint32_t *tp = a.tptr + (int64_t)k * (a.T + 1);
+        s = tp[t0];
+        len = (int)(tp[t1] - s);
+        if (ch_bv && bval) bv = bval[b];
+    }
+    return compact_chunk<V, NT>(ch, s, len, bv, ch_bv, nseg);
 }
 
 // Largest segment b < nseg with ch.off[b] <= p (warp-uniform p: broadcast reads).
