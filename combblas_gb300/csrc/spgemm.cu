@@ -187,9 +187,15 @@ __global__ void k_flop_mask(int64_t nb, const int64_t *bcp, const int32_t *brow,
 constexpr int kSmall1 = 256;
 constexpr int kSmall2 = 4096;
 
+// Big columns are binned by flop (> 2^23, > 2^21, > 2^19, the rest) and
+// listed heaviest bin first, so the longest columns start early and do not
+// run alone at the end of a launch (a scale-20 R-MAT hub column holds up to
+// 2*10^7 products, most of one block's share of a phase).
+constexpr int kBigBins = 4;
+
 __global__ void k_classify(const int64_t *flop, int pid, int64_t col_base, int64_t j0, int64_t j1, int64_t s1,
-                           int64_t s2, int64_t *l1, int64_t *l2, int64_t *lb, unsigned long long *counts,
-                           int64_t *cnt_zero, const int32_t *only_flagged)
+                           int64_t s2, int64_t *l1, int64_t *l2, int64_t *lb, int64_t lb_stride,
+                           unsigned long long *counts, int64_t *cnt_zero, const int32_t *only_flagged)
 {
     const int64_t i = j0 + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
@@ -198,20 +204,24 @@ __global__ void k_classify(const int64_t *flop, int pid, int64_t col_base, int64
         const int64_t f = flop[i];
         if (f == 0) {
             if (cnt_zero) cnt_zero[col_base + i] = 0;
+        } else if (f <= s1) {
+            cls = 0;
+        } else if (f <= s2) {
+            cls = 1;
         } else {
-            cls = f <= s1 ? 0 : (f <= s2 ? 1 : 2);
+            cls = f > (1ll << 23) ? 2 : f > (1ll << 21) ? 3 : f > (1ll << 19) ? 4 : 5;
         }
     }
-    int64_t *lists[3] = {l1, l2, lb};
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
+    for (int c = 0; c < 2 + kBigBins; ++c) {
         const unsigned m = __ballot_sync(0xffffffffu, cls == c);
         if (!m) continue;
         const int leader = __ffs(m) - 1;
         unsigned long long base = 0;
         if (lane == leader) base = atomicAdd(&counts[c], (unsigned long long)__popc(m));
         base = __shfl_sync(0xffffffffu, base, leader);
-        if (cls == c) lists[c][base + __popc(m & ((1u << lane) - 1))] = make_item(pid, i);
+        int64_t *list = c == 0 ? l1 : c == 1 ? l2 : lb + (c - 2) * lb_stride;
+        if (cls == c) list[base + __popc(m & ((1u << lane) - 1))] = make_item(pid, i);
     }
 }
 
@@ -810,7 +820,7 @@ struct Plan {
     int64_t s1 = kSmall1, s2 = kSmall2;  // flop thresholds of the column classes
     int tile_rows = 0;                   // accumulator tile height (0: default)
     unsigned long long *work = nullptr;  // kernel work counters
-    int64_t *lbuf = nullptr;             // column lists (3 x (total_cols + 1))
+    int64_t *lbuf = nullptr;             // column lists ((2 + kBigBins) x (total_cols + 1))
     unsigned long long *lcnt = nullptr;  // list lengths
     SpgemmArgs &a() { return h[0]; }
 };
@@ -869,8 +879,8 @@ static int plan_finalize(Workspace &ws, Plan &P)
 {
     GBC_TRY(ws.alloc_n(&P.d, P.h.size() + 1));
     GBC_TRY(ws.alloc_n(&P.work, 16));
-    GBC_TRY(ws.alloc_n(&P.lbuf, 3 * ((size_t)P.total_cols + 1)));
-    GBC_TRY(ws.alloc_n(&P.lcnt, 4));
+    GBC_TRY(ws.alloc_n(&P.lbuf, (2 + kBigBins) * ((size_t)P.total_cols + 1)));
+    GBC_TRY(ws.alloc_n(&P.lcnt, 2 + kBigBins));
     GBC_CUDA_TRY(cudaMemcpyAsync(P.d, P.h.data(), P.h.size() * sizeof(SpgemmArgs), cudaMemcpyHostToDevice,
                                  ws.ctx->stream));
     return GBC_OK;
@@ -895,7 +905,8 @@ static int plan_build(Workspace &ws, const DevMatrix &A, const DevMatrix &B, Pla
 static int plan_classify(Plan &P, cudaStream_t s, int pid, int64_t j0, int64_t j1, Lists &L, int64_t *cnt_zero,
                          const int32_t *flagged = nullptr)
 {
-    GBC_CUDA_TRY(cudaMemsetAsync(P.lcnt, 0, 4 * sizeof(unsigned long long), s));
+    constexpr int NL = 2 + kBigBins;
+    GBC_CUDA_TRY(cudaMemsetAsync(P.lcnt, 0, NL * sizeof(unsigned long long), s));
     const int64_t stride = P.total_cols + 1;
     int64_t *l0 = P.lbuf, *l1 = P.lbuf + stride, *l2 = P.lbuf + 2 * stride;
     for (int q = 0; q < (int)P.h.size(); ++q) {
@@ -904,18 +915,29 @@ static int plan_classify(Plan &P, cudaStream_t s, int pid, int64_t j0, int64_t j
         const int64_t lo = pid >= 0 ? j0 : 0, hi = (pid >= 0 && j1 >= 0) ? j1 : a.nb;
         if (hi > lo) {
             k_classify<<<(unsigned)((hi - lo + 255) / 256), 256, 0, s>>>(a.flop, q, a.col_base, lo, hi, P.s1, P.s2,
-                                                                         l0, l1, l2, P.lcnt, cnt_zero, flagged);
+                                                                         l0, l1, l2, stride, P.lcnt, cnt_zero,
+                                                                         flagged);
             note_launch();
         }
     }
     GBC_CUDA_TRY(cudaGetLastError());
-    unsigned long long h[4];
+    unsigned long long h[NL];
     GBC_CUDA_TRY(cudaMemcpyAsync(h, P.lcnt, sizeof(h), cudaMemcpyDeviceToHost, s));
     GBC_CUDA_TRY(cudaStreamSynchronize(s));
+    // the big list: bin 0 (heaviest) in place, the other bins appended
+    int64_t nbig = (int64_t)h[2];
+    for (int c = 1; c < kBigBins; ++c) {
+        const int64_t nc = (int64_t)h[2 + c];
+        if (nc > 0)
+            GBC_CUDA_TRY(cudaMemcpyAsync(l2 + nbig, l2 + c * stride, nc * sizeof(int64_t), cudaMemcpyDeviceToDevice, s));
+        nbig += nc;
+    }
     L.l[0] = l0;
     L.l[1] = l1;
     L.l[2] = l2;
-    for (int c = 0; c < 3; ++c) L.n[c] = (int64_t)h[c];
+    L.n[0] = (int64_t)h[0];
+    L.n[1] = (int64_t)h[1];
+    L.n[2] = nbig;
     return GBC_OK;
 }
 
