@@ -273,7 +273,7 @@ __global__ void __launch_bounds__(kThreads) k_symbolic(const SpgemmArgs *args, c
                             const int p = P + lane;
                             const int b = window_seg(ch, nseg, bcur, p);
                             if (p < we) {
-                                const int64_t idx = (int64_t)ch.s[b] + (p - ch.off[b]);
+                                const int64_t idx = (uint32_t)(ch.base[b] + (uint32_t)p);
                                 const int r = a.arow[idx] - (int)row0;
                                 atomicOr(&bm[r >> 5], 1u << (r & 31));
                             }
@@ -468,7 +468,7 @@ __global__ void __launch_bounds__(NT, numeric_min_blocks<NT, SUB>()) k_numeric(c
                             const int p = P + lane;
                             const int b = window_seg(ch, nseg, s_win[r * NW + warp], p);
                             if (p < q0 + n0) {
-                                const int64_t idx = (int64_t)ch.s[b] + (p - ch.off[b]);
+                                const int64_t idx = (uint32_t)(ch.base[b] + (uint32_t)p);
                                 ar_[r] = a.arow[idx];
                                 av_[r] = aval ? aval[idx] : SR::one();
                                 sg_[r] = b;

@@ -76,20 +76,21 @@ __device__ __forceinline__ int64_t block_exclusive_sum64(int64_t v, int64_t *tot
 }
 
 // One chunk of up to NT consecutive entries of a B column (NT = threads of
-// the block): for entry b, the A segment [s[b], s[b] + len) restricted to
-// row tiles [t0, t1), and off[] the exclusive prefix of the segment lengths
-// (off[NT] = total).
+// the block), as its non-empty A segments restricted to row tiles [t0, t1):
+// off[] is the exclusive prefix of the segment lengths (off[nseg] = total),
+// and product p of segment b (off[b] <= p < off[b+1]) sits at position
+// base[b] + p of A's arrays (base = segment start - off, modulo 2^32).
 template <int NT>
 struct ChunkSmemN {
-    uint32_t s[NT];
+    uint32_t base[NT];
     int32_t off[NT + 1];
 };
 typedef ChunkSmemN<kThreads> ChunkSmem;
 
 // Compact one chunk whose segments are already known per thread (start s,
 // length len, B value bv; len 0 for threads past the chunk), keeping only
-// the non-empty segments: ch.s / ch.off (and ch_bv) hold the nseg non-empty
-// segments in entry order, ch.off[nseg] = total.  One block scan packs the
+// the non-empty segments: ch.base / ch.off (and ch_bv) hold the nseg
+// non-empty segments in entry order, ch.off[nseg] = total.  One block scan packs the
 // segment length (high word) with a non-empty flag (low word), giving
 // offsets and compacted positions together.  Returns the total.
 template <typename V, int NT>
@@ -100,8 +101,8 @@ __device__ __forceinline__ int compact_chunk(ChunkSmemN<NT> &ch, uint32_t s, int
     const int64_t ex = block_exclusive_sum64<NT>(((int64_t)len << 32) | (len > 0 ? 1 : 0), &tot);
     if (len > 0) {
         const int c = (int)(ex & 0xffffffff);
-        ch.s[c] = s;
         ch.off[c] = (int)(ex >> 32);
+        ch.base[c] = s - (uint32_t)(ex >> 32);
         if (ch_bv) ch_bv[c] = bv;
     }
     nseg = (int)(tot & 0xffffffff);
@@ -145,16 +146,18 @@ __device__ __forceinline__ int chunk_find_nz(const ChunkSmemN<NT> &ch, int nseg,
     return lo;
 }
 
-// Segment of product p for a warp whose 32-product window starts inside
-// segment bcur (segments non-empty, so at most 31 boundaries follow the
-// window start within it): lane k holds the boundary ch.off[bcur+1+k] and a
-// five-step binary search over the lanes counts the boundaries <= p.  All
-// lanes of the warp must call it.
+// Segment of product p for a warp whose 32-product window [p - lane,
+// p - lane + 32) starts inside segment bcur (segments non-empty, so at most
+// 31 boundaries follow the window start within it): lane k holds the
+// boundary ch.off[bcur+1+k]; a window that ends before the first boundary
+// lies in bcur, otherwise a five-step binary search over the lanes counts
+// the boundaries <= p.  All lanes of the warp must call it.
 template <int NT>
 __device__ __forceinline__ int window_seg(const ChunkSmemN<NT> &ch, int nseg, int bcur, int p)
 {
     const int lane = threadIdx.x & 31;
     const int o = ch.off[min(bcur + 1 + lane, nseg)];
+    if (__shfl_sync(0xffffffffu, o, 0) > p - lane + 31) return bcur;  // warp-uniform
     int c = 0;
 #pragma unroll
     for (int step = 16; step; step >>= 1) {
