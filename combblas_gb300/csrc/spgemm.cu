@@ -193,6 +193,18 @@ constexpr int kSmall2 = 4096;
 // 2*10^7 products, most of one block's share of a phase).
 constexpr int kBigBins = 4;
 
+// Next work item of a persistent block: its own index first (consecutive
+// blocks sit on different SMs, so the heaviest items, listed first, start
+// on different SMs), then the items handed out by the counter.
+__device__ __forceinline__ int64_t next_item(unsigned long long *work, bool &first)
+{
+    if (first) {
+        first = false;
+        return (int64_t)blockIdx.x;
+    }
+    return (int64_t)gridDim.x + (int64_t)atomicAdd(work, 1ull);
+}
+
 __global__ void k_classify(const int64_t *flop, int pid, int64_t col_base, int64_t j0, int64_t j1, int64_t s1,
                            int64_t s2, int64_t *l1, int64_t *l2, int64_t *lb, int64_t lb_stride,
                            unsigned long long *counts, int64_t *cnt_zero, const int32_t *only_flagged)
@@ -238,9 +250,10 @@ __global__ void __launch_bounds__(kThreads) k_symbolic(const SpgemmArgs *args, c
     __shared__ int64_t s_red[kThreads / 32];
     __shared__ SpgemmArgs sa;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    bool first_item = true;
     for (;;) {
         if (tid == 0) {
-            s_col = (int64_t)atomicAdd(work, 1ull);
+            s_col = next_item(work, first_item);
             if (s_col < nitems) sa = args[item_pid(items[s_col])];
         }
         __syncthreads();
@@ -364,9 +377,10 @@ __global__ void __launch_bounds__(NT, numeric_min_blocks<NT, SUB>()) k_numeric(c
     const unsigned lt = (1u << lane) - 1;
     constexpr int NC = NW * kSubPerThread * NW;
 
+    bool first_item = true;
     for (;;) {
         if (tid == 0) {
-            s_col = (int64_t)atomicAdd(work, 1ull);
+            s_col = next_item(work, first_item);
             if (s_col < nitems) sa = args[item_pid(items[s_col])];
         }
         __syncthreads();
