@@ -12,10 +12,9 @@
 //                 a shared-memory bitmap over the rows, plus the mask of row
 //                 tiles the column touches.
 //   k_numeric     per column, per touched row tile: products staged in
-//                 shared memory, stably partitioned to owner warps (rows are
-//                 striped over warps in 32-row groups), and folded by the
-//                 owner into a dense shared-memory accumulator in B-entry
-//                 order.  Each output entry is therefore the left fold
+//                 shared memory, stably partitioned to owner warps (owner =
+//                 a hash of the row), and folded by the owner into a dense
+//                 shared-memory accumulator in B-entry order.  Each output entry is therefore the left fold
 //                 acc = add(mrhs, acc) over k ascending -- exactly the order
 //                 of the reference's hash path (mtSpGEMM.h:385-400) -- so
 //                 repeated runs are bit-identical.  Rows come out ascending
