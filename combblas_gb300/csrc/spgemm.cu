@@ -24,6 +24,7 @@
 #include <functional>
 #include <map>
 #include <mutex>
+#include <tuple>
 
 #include "gbc_internal.cuh"
 #include "semiring.cuh"
@@ -744,6 +745,33 @@ static int grid_for(Context *c, int64_t work, int per_sm)
     return (int)std::max<int64_t>(1, std::min<int64_t>(g, work));
 }
 
+// Blocks of `kernel` that fit on one SM at once (registers, shared memory,
+// threads), at most cap.  Persistent kernels launch exactly this many per
+// SM: every block then starts at once and takes its first item (the
+// heaviest first) without waiting for another block to exit.  Memoized per
+// device, kernel, block size and shared memory, so a stream capture that
+// repeats an earlier launch makes no query.
+template <class K>
+static int resident_blocks(K kernel, int threads, size_t dyn_smem, int cap)
+{
+    static std::mutex mu;
+    static std::map<std::tuple<int, const void *, int, size_t>, int> known;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    const auto key = std::make_tuple(dev, (const void *)kernel, threads, dyn_smem);
+    auto it = known.find(key);
+    if (it == known.end()) {
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, dyn_smem) != cudaSuccess || n < 1) {
+            cudaGetLastError();
+            n = 1;
+        }
+        it = known.emplace(key, n).first;
+    }
+    return std::min(it->second, cap);
+}
+
 int prepare_operands(Workspace &ws, const DevMatrix &A, const DevMatrix &B, SpgemmArgs &a, int64_t **acp_out,
                      int tile_rows)
 {
@@ -996,9 +1024,9 @@ static int run_symbolic(Context *ctx, Plan &P, const Lists &L, int64_t *cnt)
     if (L.n[2] > 0) {
         const size_t sym_smem = P.max_sym_smem;
         GBC_TRY(set_smem(k_symbolic, sym_smem));
-        int per_sm = std::max(1, (int)(ctx->smem_optin / (sym_smem + 8192)));
+        const int per_sm = resident_blocks(k_symbolic, kThreads, sym_smem, 8);
         GBC_CUDA_TRY(cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), s));
-        k_symbolic<<<grid_for(ctx, L.n[2], std::min(per_sm, 8)), kThreads, sym_smem, s>>>(P.d, L.l[2], L.n[2], cnt,
+        k_symbolic<<<grid_for(ctx, L.n[2], per_sm), kThreads, sym_smem, s>>>(P.d, L.l[2], L.n[2], cnt,
                                                                                              P.work);
         note_launch();
     }
@@ -1053,21 +1081,21 @@ static int run_numeric(Context *ctx, Plan &P, const Lists &L, const int64_t *ccp
         if (P.max_R > 8192) {
             const size_t num_smem = numeric_smem_bytes(P.max_R, sizeof(V), 4096);
             GBC_TRY(set_smem(k_numeric<SR, 4096, kThreads>, num_smem));
-            int per_sm = std::max(1, (int)(ctx->smem_optin / (num_smem + 12288)));
-            k_numeric<SR, 4096, kThreads><<<grid_for(ctx, L.n[2], std::min(per_sm, 8)), kThreads, num_smem, s>>>(
+            const int per_sm = resident_blocks(k_numeric<SR, 4096, kThreads>, kThreads, num_smem, 8);
+            k_numeric<SR, 4096, kThreads><<<grid_for(ctx, L.n[2], per_sm), kThreads, num_smem, s>>>(
                 P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir, cval, P.work + 1);
         } else if (P.max_R <= 4096) {
             const size_t num_smem = numeric_smem_bytes(P.max_R, sizeof(V), 1024);
             GBC_TRY(set_smem(k_numeric<SR, 1024, kThreads>, num_smem));
-            int per_sm = std::max(1, (int)(ctx->smem_optin / (num_smem + 6144)));
-            k_numeric<SR, 1024, kThreads><<<grid_for(ctx, L.n[2], std::min(per_sm, 4)), kThreads, num_smem, s>>>(
+            const int per_sm = resident_blocks(k_numeric<SR, 1024, kThreads>, kThreads, num_smem, 4);
+            k_numeric<SR, 1024, kThreads><<<grid_for(ctx, L.n[2], per_sm), kThreads, num_smem, s>>>(
                 P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir, cval, P.work + 1);
         } else {
             // 8192-row tiles: 512-thread blocks, two per SM (64 registers)
             const size_t num_smem = numeric_smem_bytes(P.max_R, sizeof(V), 2048);
             GBC_TRY(set_smem(k_numeric<SR, 2048, 512>, num_smem));
-            int per_sm = std::max(1, (int)(ctx->smem_optin / (num_smem + 16384)));
-            k_numeric<SR, 2048, 512><<<grid_for(ctx, L.n[2], std::min(per_sm, 2)), 512, num_smem, s>>>(
+            const int per_sm = resident_blocks(k_numeric<SR, 2048, 512>, 512, num_smem, 2);
+            k_numeric<SR, 2048, 512><<<grid_for(ctx, L.n[2], per_sm), 512, num_smem, s>>>(
                 P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir, cval, P.work + 1);
         }
         note_launch();
