@@ -42,8 +42,8 @@ SEED = 1
 BFS_ROOTS = 64
 # DRAM bytes of k_numeric measured by ncu on a scale-20 column sample
 # (profiles/k_numeric_s20_cols4096.txt), used to scale roofline.traffic
-NUMERIC_DRAM_READ_PER_MULT = 5.81
-NUMERIC_DRAM_WRITE_PER_ENTRY = 15.68
+NUMERIC_DRAM_READ_PER_MULT = 5.57
+NUMERIC_DRAM_WRITE_PER_ENTRY = 15.66
 # DRAM bytes of the multi-source BFS kernels per scanned edge (expand +
 # finalize, profiles/launches_msbfs22.txt)
 MSBFS_DRAM_PER_SCANNED_EDGE = 19.5
