@@ -499,7 +499,7 @@ __global__ void __launch_bounds__(NT, numeric_min_blocks<NT, SUB>()) k_numeric(c
                     const int n = min(kSub, L - q);
                     const int rounds = (n + NT - 1) / NT;  // block-uniform
                     // 3. stable partition by owner warp (row_owner): rank
-                    //    within (round, warp) from 3 ballots; counts laid out
+                    //    within (round, warp) from LB + 1 ballots; counts laid out
                     //    [owner][round][warp] so the scan follows product order
                     int rk_[kSubPerThread];
 #pragma unroll
