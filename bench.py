@@ -278,13 +278,21 @@ def run_reference(args, world, rank):
         "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.workload.startswith("spgemm") or args.workload == "batch256" else "int64",
         "data": "synthetic (seeded R-MAT)",
-        "config": {"workload": args.workload, "scale": scale, "edge_factor": ef, "seed": SEED},
+        "config": workload_config(args, scale, ef, world),
         "cpu_baseline": {"value": val, "unit": unit, "cores": threads, "kind": "port",
                          "sample": desc + " per step; the reference's CPU algorithm as restated in oracle/oracle.c "
                                           "(the reference sources are not on this machine)"},
         "e2e": {"value": val, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def workload_config(args, scale, ef, world):
+    """The `config` object of both arms' JSON lines (the same workload)."""
+    return {"workload": args.workload, "scale": scale, "edge_factor": ef, "seed": SEED,
+            "rmat_abcd": [0.57, 0.19, 0.19, 0.05], "index": "int64",
+            "phase_budget_nnz": args.phase_nnz, "l2": "inputs and outputs larger than L2 (129 MB)",
+            "parallelism": f"replicas x{world}", **({"b_columns": args.bcols} if args.bcols else {})}
 
 
 def metric_name(workload, scale, ef):
@@ -746,7 +754,6 @@ def run_ours(args, world, rank, local):
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
     hbm, peak_kind = peaks()
-    budget = args.phase_nnz
     result: dict = {}
     if args.workload == "batch256":
         A, scale, ef = None, 0, 0
@@ -837,10 +844,7 @@ def run_ours(args, world, rank, local):
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.workload.startswith("spgemm") or args.workload == "batch256" else "int64",
         "data": "synthetic (seeded R-MAT, numpy generator)",
-        "config": {"workload": args.workload, "scale": scale, "edge_factor": ef, "seed": SEED,
-                   "rmat_abcd": [0.57, 0.19, 0.19, 0.05], "index": "int64",
-                   "phase_budget_nnz": budget, "l2": "inputs and outputs larger than L2 (129 MB)",
-                   "parallelism": f"replicas x{world}", **({"b_columns": args.bcols} if args.bcols else {})},
+        "config": workload_config(args, scale, ef, world),
     }
     for k in ("roofline", "cpu_baseline", "e2e", "gpu_launches", "clocks", "spgemm", "exact_two_phase", "mcl", "bfs",
               "msbfs", "batch", "spmv"):

@@ -56,3 +56,20 @@ def test_reference_arm_rank_nonzero_does_no_work():
             "bench.run_reference(a, 2, 1); print('done')").format(root=ROOT)
     r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=120)
     assert r.returncode == 0 and r.stdout.strip() == "done", r.stdout + r.stderr
+
+
+def test_reference_arm_line_matches_our_config():
+    """Rank 0 of the reference arm times the oracle on the same workload and
+    prints the same metric and config as the GPU arm (tiny scale-10 graph)."""
+    code = ("import sys, json, io, contextlib; sys.path.insert(0, {root!r}); import bench, argparse; "
+            "a = argparse.Namespace(impl='reference', workload='spgemm14', scale=10, steps=1, warmup=0, "
+            "phase_nnz=3 << 30, bcols=0); buf = io.StringIO()\n"
+            "with contextlib.redirect_stdout(buf): bench.run_reference(a, 1, 0)\n"
+            "line = json.loads(buf.getvalue().strip().splitlines()[-1])\n"
+            "assert line['impl'] == 'reference' and line['value'] > 0, line\n"
+            "assert line['config'] == bench.workload_config(a, 10, 8, 1), line['config']\n"
+            "assert line['metric'] == bench.metric_name('spgemm14', 10, 8)\n"
+            "assert line['e2e']['h2d_bytes_per_step'] == 0 and line['cpu_baseline']['value'] == line['value']\n"
+            "print('ok')").format(root=ROOT)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stdout + r.stderr
