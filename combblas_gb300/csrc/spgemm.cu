@@ -370,12 +370,19 @@ __global__ void __launch_bounds__(NT, numeric_min_blocks<NT, SUB>()) k_numeric(c
     __shared__ int32_t s_wsum[NW];
     __shared__ int32_t s_win[SUB / 32];
     __shared__ uint32_t s_grp[NT];  // per warp: group mask of each winner lane
+    __shared__ int32_t s_hist[256];  // range visits: products per row tile
     __shared__ int64_t s_col;
     __shared__ SpgemmArgs sa;
     V *cval = static_cast<V *>(cval_v);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned lt = (1u << lane) - 1;
     constexpr int NC = NW * kSubPerThread * NW;
+    // Range visits (see below): a hash table of HS slots in the accumulator
+    // area, keys shifted by 13 bits in the sort.
+    constexpr int HS = 2 * SUB;
+    constexpr int HSB = SUB == 1024 ? 11 : SUB == 2048 ? 12 : 13;
+    static_assert((1 << HSB) == HS && HS <= 8192, "hash slots");
+    constexpr bool kRanges = sizeof(V) == 8;
 
     bool first_item = true;
     for (;;) {
@@ -436,14 +443,70 @@ __global__ void __launch_bounds__(NT, numeric_min_blocks<NT, SUB>()) k_numeric(c
                 pe = tp[t + 1];
             }
         }
+        // Range visits.  A sparse column visits most of its row tiles with a
+        // few hundred products each, and a tile visit costs about the same
+        // whatever its size.  So a single-chunk column of at most 2^18
+        // products first counts its products per tile (hist), and a run of
+        // consecutive touched tiles holding at most SUB products together is
+        // visited once: its products are folded (same owner partition and
+        // ordered fold) into a hash table of HS slots keyed by the row and
+        // held in the accumulator area (hval, hkey, plus hrow, the rows of the
+        // staged products), then the occupied slots are sorted by row
+        // (bitonic, in the staging area) and written in row order.  Tiles with
+        // more products keep the dense visit.
+        const bool ranges = kRanges && single && a.T > 1 && a.T <= 256 && a.R >= HS &&
+                            (size_t)HS * (sizeof(V) + 4) + (size_t)SUB * 4 <= (size_t)a.R * sizeof(V) &&
+                            a.flop[i] <= (1 << 18);
+        V *hval = acc;                                                 // [HS]
+        int32_t *hkey = reinterpret_cast<int32_t *>(acc + HS);         // [HS] row, -1 empty
+        int32_t *hrow = hkey + HS;                                     // [SUB]
+        uint64_t *skey = reinterpret_cast<uint64_t *>(sval);           // [SUB] sort keys
+        int32_t *hist = s_hist;                                        // [T]
+        if (ranges) {
+            for (int tt = tid; tt < a.T; tt += NT) hist[tt] = 0;
+            ch.base[tid] = (uint32_t)bk;  // the column's A columns, for all threads
+            __syncthreads();
+            const int nb = (int)(be - bs), npairs = nb * a.T;
+            for (int p0 = tid; p0 < npairs; p0 += 4 * NT) {
+                int len[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int pp = p0 + u * NT;
+                    len[u] = 0;
+                    if (pp < npairs) {
+                        const int e = pp / a.T, tt = pp - e * a.T;
+                        const uint32_t *tp = a.tptr + (int64_t)(int)ch.base[e] * (a.T + 1);
+                        len[u] = (int)(tp[tt + 1] - tp[tt]);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (len[u] > 0) atomicAdd(&hist[(p0 + u * NT) % a.T], len[u]);
+            }
+            __syncthreads();
+        }
         while (t >= 0) {
-            const int tn = next_tile();
+            int tn = next_tile();
+            int tlast = t;
+            if (ranges && hist[t] <= SUB) {
+                int rsum = hist[t];
+                while (tn >= 0 && hist[tn] <= SUB - rsum) {
+                    rsum += hist[tn];
+                    tlast = tn;
+                    tn = next_tile();
+                }
+            }
+            const bool hashed = tlast > t;  // block-uniform
+            if (hashed)
+                for (int u = tid; u < HS; u += NT) hkey[u] = -1;
             const int row0 = t * a.R;
             for (int64_t cb = bs; cb < be; cb += NT) {
                 int nseg, L;
                 if (single) {
                     const uint32_t s0 = ps;
-                    const int len0 = bk >= 0 ? (int)(pe - ps) : 0;
+                    uint32_t e0 = pe;
+                    if (hashed && bk >= 0) e0 = a.tptr[(int64_t)bk * (a.T + 1) + tlast + 1];
+                    const int len0 = bk >= 0 ? (int)(e0 - s0) : 0;
                     const V bv = (bk >= 0 && bval) ? bval[bs + tid] : SR::one();
                     if (bk >= 0 && tn >= 0) {
                         const uint32_t *tp = a.tptr + (int64_t)bk * (a.T + 1);
@@ -451,6 +514,10 @@ __global__ void __launch_bounds__(NT, numeric_min_blocks<NT, SUB>()) k_numeric(c
                         pe = tp[tn + 1];
                     }
                     L = compact_chunk<V, NT>(ch, s0, len0, bv, ch_bv, nseg);
+                    if (hashed && L > kSub) {  // cannot happen: the run was cut at SUB products
+                        if (tid == 0) atomicOr(a.err, 256);
+                        L = 0;
+                    }
                 } else {
                     L = load_chunk_nz<V>(a, ch, cb, be, t, t + 1, bval, ch_bv, SR::one(), nseg);
                 }
@@ -570,7 +637,10 @@ __global__ void __launch_bounds__(NT, numeric_min_blocks<NT, SUB>()) k_numeric(c
                             const int o = ar_[r] - row0;
                             const int w = row_owner<LB>(o);
                             const int pos = s_cnt[(w * kSubPerThread + r) * NW + warp] + rk_[r];
-                            srow[pos] = (uint16_t)o;
+                            if (hashed)
+                                hrow[pos] = o;
+                            else
+                                srow[pos] = (uint16_t)o;
                             sval[pos] = SR::mul(av_[r], ch_bv[sg_[r]]);
                         }
                     }
@@ -597,7 +667,24 @@ __global__ void __launch_bounds__(NT, numeric_min_blocks<NT, SUB>()) k_numeric(c
                         for (int p0 = beg; p0 < end; p0 += 32) {
                             const int p = p0 + lane;
                             const bool act = p < end;
-                            const int o = act ? (int)srow[p] : 0;
+                            int o = 0;  // accumulator index: the tile row, or the row's hash slot
+                            if (act && !hashed) {
+                                o = srow[p];
+                            } else if (act) {
+                                // linear probing; the table holds at most SUB rows of HS slots
+                                const int row = hrow[p];
+                                int h = (int)(((uint32_t)row * 0x85EBCA6Bu) >> (32 - HSB));
+                                for (;;) {
+                                    const int k = ((volatile int32_t *)hkey)[h];
+                                    if (k == row) break;
+                                    if (k < 0) {
+                                        const int old = atomicCAS(&hkey[h], -1, row);
+                                        if (old < 0 || old == row) break;
+                                    }
+                                    h = (h + 1) & (HS - 1);
+                                }
+                                o = h;
+                            }
                             if (act) tag[o] = (uint8_t)lane;
                             gm[lane] = 0;
                             __syncwarp();
@@ -628,6 +715,65 @@ __global__ void __launch_bounds__(NT, numeric_min_blocks<NT, SUB>()) k_numeric(c
                     __syncthreads();
                 }
             }
+            if (hashed) {
+                // range visit: the occupied slots, as (row << 13 | slot) keys,
+                // are sorted (bitonic, in the staging area: at most SUB of
+                // them) and written in row order; the slot bits are cleared
+                constexpr int SPT = HS / NT;
+                int c = 0;
+#pragma unroll
+                for (int u = 0; u < SPT; ++u) c += hkey[tid * SPT + u] >= 0;
+                int x = c;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, x, o);
+                    if (lane >= o) x += y;
+                }
+                if (lane == 31) s_wsum[warp] = x;
+                __syncthreads();
+                int q = x - c, tot = 0;
+#pragma unroll
+                for (int u = 0; u < NW; ++u) {
+                    const int ws = s_wsum[u];
+                    q += u < warp ? ws : 0;
+                    tot += ws;
+                }
+#pragma unroll
+                for (int u = 0; u < SPT; ++u) {
+                    const int sl = tid * SPT + u;
+                    const int k = hkey[sl];
+                    if (k >= 0) skey[q++] = ((uint64_t)(uint32_t)k << 13) | (uint64_t)sl;
+                }
+                int N = 1;
+                while (N < tot) N <<= 1;
+                for (int u = tot + tid; u < N; u += NT) skey[u] = ~0ull;
+                __syncthreads();
+                for (int k2 = 2; k2 <= N; k2 <<= 1) {
+                    for (int j = k2 >> 1; j > 0; j >>= 1) {
+                        for (int u = tid; u < (N >> 1); u += NT) {
+                            const int lo = ((u & ~(j - 1)) << 1) | (u & (j - 1)), hi = lo + j;
+                            const uint64_t x0 = skey[lo], x1 = skey[hi];
+                            if ((x0 > x1) == ((lo & k2) == 0)) {
+                                skey[lo] = x1;
+                                skey[hi] = x0;
+                            }
+                        }
+                        __syncthreads();
+                    }
+                }
+                for (int u = tid; u < tot; u += NT) {
+                    const uint64_t key = skey[u];
+                    const int64_t pos = out + u;
+                    if (pos < lim) {
+                        cir[pos] = (int64_t)row0 + (int64_t)(key >> 13);
+                        cval[pos] = hval[key & (HS - 1)];
+                    } else {
+                        over = true;
+                    }
+                }
+                for (int w = tid; w < (HS >> 5); w += NT) bm[w] = 0;
+                out += tot;
+            } else
             // write the tile's entries in row order: each thread takes its
             // words of the touched bitmap (clearing them for the next
             // tile), entries are staged in row order in shared memory and
