@@ -14,11 +14,14 @@
 //   k_numeric     per column, per touched row tile: products staged in
 //                 shared memory, stably partitioned to owner warps (owner =
 //                 a hash of the row), and folded by the owner into a dense
-//                 shared-memory accumulator in B-entry order.  Each output entry is therefore the left fold
-//                 acc = add(mrhs, acc) over k ascending -- exactly the order
-//                 of the reference's hash path (mtSpGEMM.h:385-400) -- so
-//                 repeated runs are bit-identical.  Rows come out ascending
-//                 (tile order, then bitmap order): no sort is needed.
+//                 shared-memory accumulator in B-entry order.  Each output
+//                 entry is therefore the left fold acc = add(mrhs, acc) over
+//                 k ascending -- exactly the order of the reference's hash
+//                 path (mtSpGEMM.h:385-400) -- so repeated runs are
+//                 bit-identical.  Rows come out ascending (tile order, then
+//                 bitmap order).  Runs of sparse tiles of one column are
+//                 folded the same way into a shared-memory hash table and
+//                 sorted by row on write-out.
 #include <algorithm>
 #include <cstdio>
 #include <functional>
