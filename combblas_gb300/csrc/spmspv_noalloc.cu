@@ -8,8 +8,13 @@
 // the implicit device-wide synchronisation of cudaMalloc/cudaFree, or code
 // whose environment forbids driver allocations after start-up.  This entry
 // point therefore takes every input and output as caller-provided device
-// memory and keeps its working storage in one file-scope __device__ array
-// that the driver reserves when the library is loaded.
+// memory and keeps its working storage in one file-scope __device__ array.
+// The CUDA runtime reserves that array when it loads this file's device
+// code on a device; with lazy module loading (the runtime's default) that
+// happens at the first use on each device, i.e. inside the first call of
+// this entry point, which then needs the array's ~8.4 MB to be free.
+// Callers should therefore make one warm-up call per device at start-up
+// (nrow = 0 and veclen = 0 is enough), while memory is still available.
 //
 // Limits and rules (also stated in include/gbcomb.h):
 //  * the matrix may have at most kNoAllocMaxRows rows; larger inputs are
@@ -22,7 +27,11 @@
 //    and must be serialised by the caller;
 //  * the first call on a device looks up the array's device address with
 //    cudaGetSymbolAddress (with that device current) and caches it; make
-//    that first call before any stream capture begins.
+//    that first call before any stream capture begins.  If the lookup
+//    reports an error the cache entry stays empty and the next call tries
+//    again;
+//  * every call reads its error flag and output count back to the host and
+//    waits for `stream` to finish before it returns.
 #include <mutex>
 
 #include "gbc_internal.cuh"
@@ -59,8 +68,10 @@ int scratch_address(int device, NoAllocScratch **out)
     if (!g_addr[device]) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess)
+        if (e != cudaSuccess) {
+            cudaGetLastError();  // nothing is cached: the next call looks the address up again
             return fail(GBC_ECUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+        }
         g_addr[device] = static_cast<NoAllocScratch *>(p);
     }
     *out = g_addr[device];

@@ -329,13 +329,17 @@ int gbc_msbfs(gbc_context *ctx, gbc_graph *g, const int64_t *roots, int64_t nroo
  * memory on the current device (A as CSC: cp[ncol+1], ir[nnz]; x: indx,
  * numx[veclen]; y: indy, numy with room for nrow entries); *nnzy (host) gets
  * the output count after the call synchronises `stream` (a cudaStream_t,
- * NULL for the default stream).  Working storage is one fixed __device__
- * array of about 8.4 MB that every GPU loading the library holds until the
- * process exits; nrow above 1048576 is rejected with GBC_EOVERFLOW.  All
- * calls share that array: calls that overlap on the GPU race and must be
- * serialised by the caller.  The first call on a device looks up the
- * array's address (cudaGetSymbolAddress) -- make it before any stream
- * capture. */
+ * NULL for the default stream); every call waits for `stream` before it
+ * returns.  Working storage is one fixed __device__ array of about 8.4 MB,
+ * held until the process exits by every GPU on which it was used; nrow
+ * above 1048576 is rejected with GBC_EOVERFLOW.  The CUDA runtime reserves
+ * the array when it loads the library's device code on a device -- under
+ * lazy module loading (the default) during the first call on that device --
+ * so make one warm-up call per device at start-up (nrow = 0, veclen = 0),
+ * while the 8.4 MB are still free.  All calls share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller.  The first
+ * call on a device looks up the array's address (cudaGetSymbolAddress) --
+ * make it before any stream capture. */
 int gbc_spmspv_select2ndmin_noalloc(int64_t nrow, int64_t ncol, int64_t nnz, const int64_t *cp, const int64_t *ir,
                                     const int32_t *indx, const int64_t *numx, int32_t veclen, int32_t *indy,
                                     int64_t *numy, int32_t *nnzy, void *stream);

@@ -51,6 +51,54 @@ def test_noalloc_matches_allocating_entry_point_twice():
         assert np.array_equal(yi[:ny], ei) and np.array_equal(yv[:ny], ev)
 
 
+def test_noalloc_allocates_nothing_and_reports_bad_input():
+    """After a warm-up call, further calls leave the device's free memory
+    unchanged; an out-of-range vector index is reported as GBC_EINVAL (the
+    kernel's own bounds check), and the next valid call still gives the right
+    answer (every call clears the error flag)."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from combblas_gb300 import _lib
+    from combblas_gb300 import bfs as B
+    from combblas_gb300 import generators as G
+
+    lib = _lib.lib()
+    A = G.rmat(12, 8, seed=5, values=None)
+    A_dev = (torch.from_numpy(A.colptr).cuda(), torch.from_numpy(A.rowidx).cuda())
+    g = B.Graph(A)
+    rng = np.random.default_rng(9)
+    x = np.sort(rng.choice(A.ncol, 200, replace=False)).astype(np.int32)
+    xv = rng.integers(0, 10**6, 200).astype(np.int64)
+    dx, dv = torch.from_numpy(x).cuda(), torch.from_numpy(xv).cuda()
+    yi = torch.empty(A.nrow, dtype=torch.int32, device="cuda")
+    yv = torch.empty(A.nrow, dtype=torch.int64, device="cuda")
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    ny = C.c_int32(-1)
+
+    def call(xp, n):
+        return lib.gbc_spmspv_select2ndmin_noalloc(A.nrow, A.ncol, A.nnz, A_dev[0].data_ptr(), A_dev[1].data_ptr(),
+                                                   xp, dv.data_ptr(), n, yi.data_ptr(), yv.data_ptr(),
+                                                   C.byref(ny), stream)
+
+    assert call(dx.data_ptr(), len(x)) == 0  # warm-up: loads the module on this device
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        assert call(dx.data_ptr(), len(x)) == 0
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    bad = dx.clone()
+    bad[7] = A.ncol + 5  # index >= ncol
+    torch.cuda.synchronize()
+    assert call(bad.data_ptr(), len(x)) == _lib.GBC_OK - 1  # GBC_EINVAL
+    assert b"out of range" in lib.gbc_last_error()
+    assert call(dx.data_ptr(), len(x)) == 0
+    ei, ev = B.SpMXSpV(g, x, xv)
+    assert ny.value == len(ei)
+    assert np.array_equal(yi.cpu().numpy()[:ny.value], ei) and np.array_equal(yv.cpu().numpy()[:ny.value], ev)
+
+
 def test_noalloc_rejects_oversized_matrix():
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
