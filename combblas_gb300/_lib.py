@@ -28,6 +28,9 @@ VT_BOOL = 3
 SIZING_EXACT = 0
 SIZING_LEARNED = 1
 
+FOLD_EXACT = 0    # PlusTimes fp64: exact sum of the rounded products, rounded once
+FOLD_ORDERED = 1  # PlusTimes fp64: left fold in B-entry order (the reference's hash path)
+
 
 class GbcError(RuntimeError):
     def __init__(self, code: int, msg: str):
@@ -86,6 +89,7 @@ _SIGS = {
     "gbc_context_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int]),
     "gbc_context_destroy": (C.c_int, [C.c_void_p]),
     "gbc_context_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gbc_context_set_fold": (C.c_int, [C.c_void_p, C.c_int]),
     "gbc_context_synchronize": (C.c_int, [C.c_void_p]),
     "gbc_result_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                   C.POINTER(C.c_int64), C.POINTER(C.c_int)]),

@@ -314,6 +314,15 @@ int gbc_context_destroy(gbc_context *c)
     return GBC_OK;
 }
 
+int gbc_context_set_fold(gbc_context *c, int fold)
+{
+    if (!c) return fail(GBC_EINVAL, "null context");
+    if (fold != GBC_FOLD_EXACT && fold != GBC_FOLD_ORDERED)
+        return fail(GBC_EINVAL, "fold must be GBC_FOLD_EXACT or GBC_FOLD_ORDERED");
+    c->fold = fold;
+    return GBC_OK;
+}
+
 int gbc_context_set_stream(gbc_context *c, void *stream)
 {
     if (!c) return fail(GBC_EINVAL, "null context");

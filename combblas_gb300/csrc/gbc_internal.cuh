@@ -49,6 +49,7 @@ struct Context {
     int32_t *d_flag = nullptr;  // device error/overflow flags (8 ints)
     void *mlp = nullptr;        // sizing model used by GBC_SIZING_LEARNED (gbc_mlp*)
     void *pinned = nullptr;     // small pinned staging for scalar reads
+    int fold = GBC_FOLD_EXACT;  // PlusTimes fp64 accumulation (gbc_context_set_fold)
 };
 
 // Stream-ordered device allocations; everything taken through a Workspace

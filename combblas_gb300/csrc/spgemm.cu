@@ -28,11 +28,13 @@
 #include <map>
 #include <mutex>
 #include <tuple>
+#include <type_traits>
 
 #include "gbc_internal.cuh"
 #include "semiring.cuh"
 #include "spgemm_kernels.cuh"
 #include "spgemm_small.cuh"
+#include "spgemm_exact.cuh"
 #include "mlp.cuh"
 
 namespace gbc {
@@ -196,18 +198,6 @@ constexpr int kSmall2 = 4096;
 // 2*10^7 products, most of one block's share of a phase).
 constexpr int kBigBins = 4;
 
-// Next work item of a persistent block: its own index first (consecutive
-// blocks sit on different SMs, so the heaviest items, listed first, start
-// on different SMs), then the items handed out by the counter.
-__device__ __forceinline__ int64_t next_item(unsigned long long *work, bool &first)
-{
-    if (first) {
-        first = false;
-        return (int64_t)blockIdx.x;
-    }
-    return (int64_t)gridDim.x + (int64_t)atomicAdd(work, 1ull);
-}
-
 __global__ void k_classify(const int64_t *flop, int pid, int64_t col_base, int64_t j0, int64_t j1, int64_t s1,
                            int64_t s2, int64_t *l1, int64_t *l2, int64_t *lb, int64_t lb_stride,
                            unsigned long long *counts, int64_t *cnt_zero, const int32_t *only_flagged)
@@ -358,8 +348,11 @@ template <class SR, int SUB, int NT>
 __global__ void __launch_bounds__(NT, numeric_min_blocks<NT, SUB>()) k_numeric(const SpgemmArgs *args, const int64_t *items, int64_t nitems,
                                                          const int64_t *ccp, int64_t ccp_base, const int64_t *cap,
                                                          int64_t *out_cnt, int32_t *overflow, int64_t *cir,
-                                                         void *cval_v, unsigned long long *work)
+                                                         void *cval_v, unsigned long long *work,
+                                                         const unsigned long long *dyn_n)
 {
+    // a device-side item count (columns handed over by another kernel)
+    if (dyn_n) nitems = min(nitems, (int64_t)*dyn_n);
     typedef typename SR::V V;
     constexpr int kSub = SUB;
     constexpr int NW = NT / 32;                      // warps = owners
@@ -921,6 +914,23 @@ static int resident_blocks(K kernel, int threads, size_t dyn_smem, int cap)
     return std::min(it->second, cap);
 }
 
+// Raise a kernel's dynamic shared-memory limit once (per device and kernel,
+// only upwards), so replays and graph captures make no attribute calls.
+template <class K>
+static int set_smem(K kernel, size_t bytes)
+{
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, size_t> done;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    size_t &cur = done[{dev, (const void *)kernel}];
+    if (cur >= bytes) return GBC_OK;
+    GBC_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    cur = bytes;
+    return GBC_OK;
+}
+
 int prepare_operands(Workspace &ws, const DevMatrix &A, const DevMatrix &B, SpgemmArgs &a, int64_t **acp_out,
                      int tile_rows)
 {
@@ -1012,8 +1022,31 @@ struct Plan {
     unsigned long long *work = nullptr;  // kernel work counters
     int64_t *lbuf = nullptr;             // column lists ((2 + kBigBins) x (total_cols + 1))
     unsigned long long *lcnt = nullptr;  // list lengths
+    bool want_aexp = false;              // PlusTimes fp64, exact accumulation (k_numeric_x)
+    int64_t *fb_items = nullptr;         // big columns the exact kernel hands to the ordered one
+    unsigned long long *fb_cnt = nullptr;
+    XSeg *xscratch = nullptr;            // exact kernel: bucketing scratch, kXScap segments per block
+    int x_blocks = 0;                    // exact kernel: its grid (resident blocks)
     SpgemmArgs &a() { return h[0]; }
 };
+
+// PlusTimes fp64 under GBC_FOLD_EXACT: every admitted column is summed
+// exactly (big columns by k_numeric_x, whose accumulator tile is kXRows
+// high; the tile height is a tuning knob only, so it is fixed here).
+template <class SR>
+static void plan_fold(Context *ctx, Plan &P)
+{
+    if (std::is_same<SR, PlusTimes<double>>::value && ctx->fold == GBC_FOLD_EXACT) {
+        P.want_aexp = true;
+        P.tile_rows = kXRows;
+    }
+}
+
+template <class SR>
+static bool use_exact(const Plan &P)
+{
+    return std::is_same<SR, PlusTimes<double>>::value && P.want_aexp && P.max_R <= kXRows;
+}
 
 struct Lists {
     const int64_t *l[3] = {nullptr, nullptr, nullptr};  // small1, small2, big
@@ -1052,6 +1085,40 @@ static int plan_add(Workspace &ws, Plan &P, const DevMatrix &A, const DevMatrix 
     GBC_CUDA_TRY(cudaGetLastError());
     a.flop = flop;
     a.tmask = tmask;
+    a.aexp = nullptr;
+    a.ktl_ptr = nullptr;
+    a.ktl_start = nullptr;
+    a.ktl_tile = nullptr;
+    if (P.want_aexp) {
+        int32_t *aexp = nullptr;
+        GBC_TRY(ws.alloc_n(&aexp, (size_t)A.ncol + 1));
+        if (A.ncol > 0) {
+            k_aexp_f64<<<grid_for(ctx, (A.ncol + 7) / 8, 8), 256, 0, s>>>(A.ncol, acp,
+                                                                         static_cast<const double *>(A.num), aexp);
+            note_launch();
+        }
+        a.aexp = aexp;
+        if (a.T <= kXTMax && A.ncol > 0) {
+            // per-column tile lists of A (bucketing in the exact kernel)
+            int64_t *kptr = nullptr;
+            GBC_TRY(ws.alloc_n(&kptr, (size_t)A.ncol + 1));
+            k_ktl_count<<<(unsigned)((A.ncol + 255) / 256), 256, 0, s>>>(A.ncol, amask, a.mask_words, kptr);
+            note_launch();
+            GBC_TRY(exclusive_scan_i64(ws, kptr, kptr, A.ncol, s));
+            int64_t nent = 0;
+            GBC_TRY(read_i64(ctx, kptr + A.ncol, &nent));
+            uint32_t *kst = nullptr;
+            uint16_t *ktt = nullptr;
+            GBC_TRY(ws.alloc_n(&kst, (size_t)nent + 1));
+            GBC_TRY(ws.alloc_n(&ktt, (size_t)nent + 1));
+            k_ktl_fill<<<grid_for(ctx, (A.ncol + 7) / 8, 8), 256, 0, s>>>(A.ncol, a.tptr, a.T, kptr, kst, ktt);
+            note_launch();
+            GBC_CUDA_TRY(cudaGetLastError());
+            a.ktl_ptr = kptr;
+            a.ktl_start = kst;
+            a.ktl_tile = ktt;
+        }
+    }
     a.aval = A.num;
     a.bval = B.num;
     a.col_base = P.total_cols;
@@ -1071,6 +1138,15 @@ static int plan_finalize(Workspace &ws, Plan &P)
     GBC_TRY(ws.alloc_n(&P.work, 16));
     GBC_TRY(ws.alloc_n(&P.lbuf, (2 + kBigBins) * ((size_t)P.total_cols + 1)));
     GBC_TRY(ws.alloc_n(&P.lcnt, 2 + kBigBins));
+    if (P.want_aexp) {
+        GBC_TRY(ws.alloc_n(&P.fb_items, (size_t)P.total_cols + 1));
+        GBC_TRY(ws.alloc_n(&P.fb_cnt, 1));
+        // bucketing scratch of the exact kernel: kXScap segments per resident block
+        const size_t smem = (size_t)kXW * kXRows * 4 + kXRows;
+        GBC_TRY(set_smem(k_numeric_x<kXThreads>, smem));
+        P.x_blocks = ws.ctx->num_sms * resident_blocks(k_numeric_x<kXThreads>, kXThreads, smem, 2);
+        GBC_TRY(ws.alloc_n(&P.xscratch, (size_t)P.x_blocks * kXScap));
+    }
     GBC_CUDA_TRY(cudaMemcpyAsync(P.d, P.h.data(), P.h.size() * sizeof(SpgemmArgs), cudaMemcpyHostToDevice,
                                  ws.ctx->stream));
     return GBC_OK;
@@ -1131,23 +1207,6 @@ static int plan_classify(Plan &P, cudaStream_t s, int pid, int64_t j0, int64_t j
     return GBC_OK;
 }
 
-// Raise a kernel's dynamic shared-memory limit once (per device and kernel,
-// only upwards), so replays and graph captures make no attribute calls.
-template <class K>
-static int set_smem(K kernel, size_t bytes)
-{
-    static std::mutex mu;
-    static std::map<std::pair<int, const void *>, size_t> done;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    std::lock_guard<std::mutex> lk(mu);
-    size_t &cur = done[{dev, (const void *)kernel}];
-    if (cur >= bytes) return GBC_OK;
-    GBC_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    cur = bytes;
-    return GBC_OK;
-}
-
 // Exact nnz per listed column (estimateNNZ_Hash's result), into the
 // batch-wide array cnt.
 static int run_symbolic(Context *ctx, Plan &P, const Lists &L, int64_t *cnt)
@@ -1198,6 +1257,63 @@ static int launch_small(Context *ctx, Plan &P, const int64_t *items, int64_t n, 
     return GBC_OK;
 }
 
+// The ordered (k-order fold) block kernel over `items`; with dyn_n the
+// item count is read on the device (at most nitems).
+template <class SR>
+static int launch_big_ordered(Context *ctx, Plan &P, const int64_t *items, int64_t nitems,
+                              const unsigned long long *dyn_n, const int64_t *ccp, int64_t ccp_base,
+                              const int64_t *cap, int64_t *out_cnt, int32_t *overflow, int64_t *cir, void *cval)
+{
+    typedef typename SR::V V;
+    cudaStream_t s = ctx->stream;
+    GBC_CUDA_TRY(cudaMemsetAsync(P.work + 1, 0, sizeof(unsigned long long), s));
+    if (P.max_R > 8192) {
+        const size_t num_smem = numeric_smem_bytes(P.max_R, sizeof(V), 4096);
+        GBC_TRY(set_smem(k_numeric<SR, 4096, kThreads>, num_smem));
+        const int per_sm = resident_blocks(k_numeric<SR, 4096, kThreads>, kThreads, num_smem, 8);
+        k_numeric<SR, 4096, kThreads><<<grid_for(ctx, nitems, per_sm), kThreads, num_smem, s>>>(
+            P.d, items, nitems, ccp, ccp_base, cap, out_cnt, overflow, cir, cval, P.work + 1, dyn_n);
+    } else if (P.max_R <= 4096) {
+        const size_t num_smem = numeric_smem_bytes(P.max_R, sizeof(V), 1024);
+        GBC_TRY(set_smem(k_numeric<SR, 1024, kThreads>, num_smem));
+        const int per_sm = resident_blocks(k_numeric<SR, 1024, kThreads>, kThreads, num_smem, 4);
+        k_numeric<SR, 1024, kThreads><<<grid_for(ctx, nitems, per_sm), kThreads, num_smem, s>>>(
+            P.d, items, nitems, ccp, ccp_base, cap, out_cnt, overflow, cir, cval, P.work + 1, dyn_n);
+    } else {
+        // 8192-row tiles: 512-thread blocks, two per SM (64 registers)
+        const size_t num_smem = numeric_smem_bytes(P.max_R, sizeof(V), 2048);
+        GBC_TRY(set_smem(k_numeric<SR, 2048, 512>, num_smem));
+        const int per_sm = resident_blocks(k_numeric<SR, 2048, 512>, 512, num_smem, 2);
+        k_numeric<SR, 2048, 512><<<grid_for(ctx, nitems, per_sm), 512, num_smem, s>>>(
+            P.d, items, nitems, ccp, ccp_base, cap, out_cnt, overflow, cir, cval, P.work + 1, dyn_n);
+    }
+    note_launch();
+    GBC_CUDA_TRY(cudaGetLastError());
+    return GBC_OK;
+}
+
+// Exact (order-free) block kernel for PlusTimes fp64 over the big list;
+// the columns it does not admit go to the ordered kernel afterwards
+// (device-side count, no host synchronisation: graph capture stays valid).
+template <class SR>
+static int launch_big_exact(Context *ctx, Plan &P, const Lists &L, const int64_t *ccp, int64_t ccp_base,
+                            const int64_t *cap, int64_t *out_cnt, int32_t *overflow, int64_t *cir, void *cval)
+{
+    cudaStream_t s = ctx->stream;
+    constexpr int NT = kXThreads;
+    const size_t smem = (size_t)kXW * kXRows * 4 + kXRows;
+    const int grid = (int)std::min<int64_t>(P.x_blocks, L.n[2]);  // the scratch holds P.x_blocks blocks
+    GBC_CUDA_TRY(cudaMemsetAsync(P.work + 1, 0, 2 * sizeof(unsigned long long), s));
+    GBC_CUDA_TRY(cudaMemsetAsync(P.fb_cnt, 0, sizeof(unsigned long long), s));
+    k_numeric_x<NT><<<grid, NT, smem, s>>>(P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir,
+                                           static_cast<double *>(cval), P.work + 1, P.fb_items, P.fb_cnt,
+                                           P.xscratch);
+    note_launch();
+    GBC_CUDA_TRY(cudaGetLastError());
+    return launch_big_ordered<SR>(ctx, P, P.fb_items, L.n[2], P.fb_cnt, ccp, ccp_base, cap, out_cnt, overflow, cir,
+                                  cval);
+}
+
 // Numeric pass over the listed columns.  Exact sizing: cap == nullptr and
 // ccp holds the exact offsets.  Learned sizing: cap gives each column's room
 // at ccp[g - ccp_base]; out_cnt/overflow receive actual counts and flags.
@@ -1206,8 +1322,6 @@ template <class SR>
 static int run_numeric(Context *ctx, Plan &P, const Lists &L, const int64_t *ccp, int64_t ccp_base, const int64_t *cap,
                        int64_t *out_cnt, int32_t *overflow, int64_t *cir, void *cval)
 {
-    typedef typename SR::V V;
-    cudaStream_t s = ctx->stream;
     const bool pack = P.max_key_bits <= 20;
     if (L.n[0] > 0) {
         if (pack)
@@ -1226,28 +1340,11 @@ static int run_numeric(Context *ctx, Plan &P, const Lists &L, const int64_t *ccp
                                                           overflow, cir, cval)));
     }
     if (L.n[2] > 0) {
-        GBC_CUDA_TRY(cudaMemsetAsync(P.work + 1, 0, sizeof(unsigned long long), s));
-        if (P.max_R > 8192) {
-            const size_t num_smem = numeric_smem_bytes(P.max_R, sizeof(V), 4096);
-            GBC_TRY(set_smem(k_numeric<SR, 4096, kThreads>, num_smem));
-            const int per_sm = resident_blocks(k_numeric<SR, 4096, kThreads>, kThreads, num_smem, 8);
-            k_numeric<SR, 4096, kThreads><<<grid_for(ctx, L.n[2], per_sm), kThreads, num_smem, s>>>(
-                P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir, cval, P.work + 1);
-        } else if (P.max_R <= 4096) {
-            const size_t num_smem = numeric_smem_bytes(P.max_R, sizeof(V), 1024);
-            GBC_TRY(set_smem(k_numeric<SR, 1024, kThreads>, num_smem));
-            const int per_sm = resident_blocks(k_numeric<SR, 1024, kThreads>, kThreads, num_smem, 4);
-            k_numeric<SR, 1024, kThreads><<<grid_for(ctx, L.n[2], per_sm), kThreads, num_smem, s>>>(
-                P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir, cval, P.work + 1);
-        } else {
-            // 8192-row tiles: 512-thread blocks, two per SM (64 registers)
-            const size_t num_smem = numeric_smem_bytes(P.max_R, sizeof(V), 2048);
-            GBC_TRY(set_smem(k_numeric<SR, 2048, 512>, num_smem));
-            const int per_sm = resident_blocks(k_numeric<SR, 2048, 512>, 512, num_smem, 2);
-            k_numeric<SR, 2048, 512><<<grid_for(ctx, L.n[2], per_sm), 512, num_smem, s>>>(
-                P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir, cval, P.work + 1);
-        }
-        note_launch();
+        if (use_exact<SR>(P))
+            GBC_TRY(launch_big_exact<SR>(ctx, P, L, ccp, ccp_base, cap, out_cnt, overflow, cir, cval));
+        else
+            GBC_TRY(launch_big_ordered<SR>(ctx, P, L.l[2], L.n[2], nullptr, ccp, ccp_base, cap, out_cnt, overflow,
+                                           cir, cval));
     }
     GBC_CUDA_TRY(cudaGetLastError());
     return GBC_OK;
@@ -1323,6 +1420,7 @@ static int spgemm_exact(Context *ctx, const DevMatrix &A, const DevMatrix &B, co
     cudaEventRecord(ctx->ev[0], s);
     Plan P;
     plan_options(P, opt);
+    plan_fold<SR>(ctx, P);
     GBC_TRY(plan_build(ws, A, B, P));
     const int64_t nb = B.nzc;
     int64_t *cnt = nullptr, *ccp = nullptr;
@@ -1635,6 +1733,7 @@ static int spgemm_phased(Context *ctx, const DevMatrix &A, const DevMatrix &B, i
     Workspace ws(ctx);
     cudaEventRecord(ctx->ev[0], s);
     Plan P;
+    plan_fold<SR>(ctx, P);
     GBC_TRY(plan_build(ws, A, B, P));
     const int64_t nb = B.nzc;
     int64_t *size = nullptr;  // exact counts, or capacities when learned
@@ -1901,6 +2000,7 @@ int spgemm_learned(Context *ctx, const DevMatrix &A, const DevMatrix &B, const g
     cudaEventRecord(ctx->ev[0], s);
     Plan P;
     plan_options(P, opt);
+    plan_fold<SR>(ctx, P);
     LearnedOut O;
     GBC_TRY(learned_into_slots<SR>(ctx, ws, A, B, P, O));
     const int64_t nb = O.nb;
@@ -2087,6 +2187,7 @@ static int batch_build(Batch &b, const std::vector<DevMatrix> &A, const std::vec
     Context *ctx = b.ctx;
     cudaStream_t s = ctx->stream;
     Workspace &ws = *b.ws;
+    plan_fold<SR>(ctx, b.P);
     for (int p = 0; p < b.np; ++p) GBC_TRY(plan_add(ws, b.P, A[p], B[p]));
     GBC_TRY(plan_finalize(ws, b.P));
     const int64_t tc = b.P.total_cols;

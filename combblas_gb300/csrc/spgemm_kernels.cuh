@@ -36,12 +36,28 @@ struct SpgemmArgs {
     const uint64_t *tmask;       // [nb][mask_words] row tiles each output column touches
     int64_t col_base;            // this product's first column in batch-wide per-column arrays
     int key_bits;                // bits needed for a row id
+    const int32_t *aexp;         // fp64 A: per-column exponent range of the values (exact accumulation), or nullptr
+    const int64_t *ktl_ptr;      // exact accumulation: per column of A, its touched row tiles (or nullptr)
+    const uint32_t *ktl_start;   //   ... first position of the column inside each listed tile, then the column end
+    const uint16_t *ktl_tile;    //   ... the tiles (0xFFFF: end marker)
 };
 
 // A work item names one output column of one product of a batch.
 __host__ __device__ __forceinline__ int64_t make_item(int pid, int64_t col) { return ((int64_t)pid << 32) | col; }
 __host__ __device__ __forceinline__ int item_pid(int64_t it) { return (int)(it >> 32); }
 __host__ __device__ __forceinline__ int64_t item_col(int64_t it) { return it & 0xffffffffll; }
+
+// Next work item of a persistent block: its own index first (consecutive
+// blocks sit on different SMs, so the heaviest items, listed first, start
+// on different SMs), then the items handed out by the counter.
+__device__ __forceinline__ int64_t next_item(unsigned long long *work, bool &first)
+{
+    if (first) {
+        first = false;
+        return (int64_t)blockIdx.x;
+    }
+    return (int64_t)gridDim.x + (int64_t)atomicAdd(work, 1ull);
+}
 
 // Block-wide exclusive sum (NT threads); *total gets the block total.
 template <int NT = kThreads>

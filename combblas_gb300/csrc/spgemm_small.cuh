@@ -15,6 +15,9 @@
 //                   ascending.
 #pragma once
 
+#include <type_traits>
+
+#include "spgemm_exact.cuh"
 #include "spgemm_kernels.cuh"
 
 namespace gbc {
@@ -268,6 +271,20 @@ __global__ void __launch_bounds__(WPB * 32) k_small_numeric(const SpgemmArgs *ar
                 vd = tv;
             }
         }
+        // PlusTimes fp64 with exact accumulation: the column's exponent
+        // window (the same admission as the block kernel's)
+        int ebase = 0;
+        bool xact = false;
+        if constexpr (std::is_same<SR, PlusTimes<double>>::value) {
+            if (a.aexp) {
+                int emin = 1 << 30, emax = -(1 << 30);
+                for (int64_t b = a.bcp[i] + lane; b < a.bcp[i + 1]; b += 32)
+                    x_window(a.aexp[a.brow[b]], bval ? (double)bval[b] : 1.0, bval != nullptr, emin, emax);
+                ebase = __reduce_min_sync(0xffffffffu, emin);
+                emax = __reduce_max_sync(0xffffffffu, emax);
+                xact = x_admit(ebase, emax, a.bcp[i + 1] - a.bcp[i]);
+            }
+        }
         // 3. fold runs of equal rows in order and write them
         const int64_t out0 = ccp[g - ccp_base];
         const int64_t room = cap ? cap[g] : (ccp[g - ccp_base + 1] - out0);
@@ -282,10 +299,24 @@ __global__ void __launch_bounds__(WPB * 32) k_small_numeric(const SpgemmArgs *ar
             const unsigned hm = __ballot_sync(0xffffffffu, head);
             if (head) {
                 V v = PACK ? vs[kk & 4095] : vs[p];
-                for (int q = p + 1; q < n; ++q) {
-                    const uint32_t kq = ks[q];
-                    if ((int)(PACK ? (kq >> 12) : kq) != row) break;
-                    v = SR::add(PACK ? vs[kq & 4095] : vs[q], v);
+                if (xact) {
+                    // exact sum of the run, rounded once (PlusTimes fp64)
+                    uint64_t hi = 0, lo = 0;
+                    uint32_t fl = 0;
+                    bool ok = true;
+                    for (int q = p; q < n; ++q) {
+                        const uint32_t kq = ks[q];
+                        if ((int)(PACK ? (kq >> 12) : kq) != row) break;
+                        ok &= x_acc128(hi, lo, fl, (double)(PACK ? vs[kq & 4095] : vs[q]), ebase);
+                    }
+                    v = (V)x_round(hi, lo, fl, ebase);
+                    if (!ok) atomicOr(a.err, 512);
+                } else {
+                    for (int q = p + 1; q < n; ++q) {
+                        const uint32_t kq = ks[q];
+                        if ((int)(PACK ? (kq >> 12) : kq) != row) break;
+                        v = SR::add(PACK ? vs[kq & 4095] : vs[q], v);
+                    }
                 }
                 const int64_t pos = heads + __popc(hm & lt);
                 if (pos < room) {

@@ -26,6 +26,7 @@ from __future__ import annotations
 
 import ctypes as C
 import sys
+from contextlib import contextmanager
 from dataclasses import dataclass
 
 import numpy as np
@@ -52,6 +53,30 @@ class Context:
 
     def set_stream(self, stream_handle: int | None):
         L.check(L.lib().gbc_context_set_stream(self.h, C.c_void_p(stream_handle or 0)))
+
+    fold = "exact"
+
+    def set_fold(self, fold: str):
+        """How PlusTimes fp64 products are summed (gbc_context_set_fold):
+        "exact" (default) -- the exact sum of the rounded products, rounded
+        once; "ordered" -- the reference's hash-path left fold in B-entry
+        order, bit for bit."""
+        code = {"exact": L.FOLD_EXACT, "ordered": L.FOLD_ORDERED}[fold]
+        L.check(L.lib().gbc_context_set_fold(self.h, code))
+        self.fold = fold
+
+    @contextmanager
+    def folding(self, fold: str | None):
+        """Temporarily use `fold` (None: leave the context as it is)."""
+        if fold is None or fold == self.fold:
+            yield self
+            return
+        old = self.fold
+        self.set_fold(fold)
+        try:
+            yield self
+        finally:
+            self.set_fold(old)
 
     def close(self):
         if self.h:
@@ -262,10 +287,11 @@ def _value_dtype(A, B, sr: str):
 
 def spgemm(A, B, sr: str = "plustimes", sizing: str = "exact", sorted: bool = True, keep_empty: bool = True,
            ctx: Context | None = None, dtype=None, tile_rows: int = 0, tiny_limit: int = -1,
-           small_limit: int = -1) -> SpResult:
+           small_limit: int = -1, fold: str | None = None) -> SpResult:
     """C = A * B over ``sr`` on the GPU.  tile_rows / tiny_limit /
     small_limit are tuning knobs (see gbc_spgemm_opts); results do not
-    depend on them."""
+    depend on them.  ``fold`` ("exact" / "ordered", None: the context's)
+    selects how PlusTimes fp64 products are summed (Context.set_fold)."""
     ctx = ctx or default_context()
     dt = np.dtype(dtype) if dtype is not None else _value_dtype(A, B, sr)
     vt = VT_OF_DTYPE[dt]
@@ -276,13 +302,14 @@ def spgemm(A, B, sr: str = "plustimes", sizing: str = "exact", sorted: bool = Tr
                              int(bool(keep_empty)), int(tile_rows), int(tiny_limit), int(small_limit))
     out = C.c_void_p()
     st = L.gbc_spgemm_stats()
-    L.check(L.lib().gbc_spgemm(ctx.h, SR_CODES[sr], vt, C.byref(ga), C.byref(gb), C.byref(opts), C.byref(out),
-                               C.byref(st)))
+    with ctx.folding(fold):
+        L.check(L.lib().gbc_spgemm(ctx.h, SR_CODES[sr], vt, C.byref(ga), C.byref(gb), C.byref(opts), C.byref(out),
+                                   C.byref(st)))
     return SpResult(out, st)
 
 
 def spgemm_phased(A, B, sr: str = "plustimes", max_phase_nnz: int = 1 << 31, ctx: Context | None = None,
-                  dtype=None, sizing: str = "exact") -> L.gbc_phased_stats:
+                  dtype=None, sizing: str = "exact", fold: str | None = None) -> L.gbc_phased_stats:
     """C = A * B in column phases of at most ``max_phase_nnz`` output entries;
     returns the statistics and checksums (the product is not kept).
     ``sizing="learned"`` sizes the phases with the context's sizing model
@@ -293,9 +320,10 @@ def spgemm_phased(A, B, sr: str = "plustimes", max_phase_nnz: int = 1 << 31, ctx
     ga = as_gbc_matrix(A, keep, dt)
     gb = as_gbc_matrix(B, keep, dt)
     st = L.gbc_phased_stats()
-    L.check(L.lib().gbc_spgemm_phased(ctx.h, SR_CODES[sr], VT_OF_DTYPE[dt], C.byref(ga), C.byref(gb),
-                                      int(max_phase_nnz), L.SIZING_LEARNED if sizing == "learned" else L.SIZING_EXACT,
-                                      C.byref(st)))
+    with ctx.folding(fold):
+        L.check(L.lib().gbc_spgemm_phased(ctx.h, SR_CODES[sr], VT_OF_DTYPE[dt], C.byref(ga), C.byref(gb),
+                                          int(max_phase_nnz),
+                                          L.SIZING_LEARNED if sizing == "learned" else L.SIZING_EXACT, C.byref(st)))
     return st
 
 

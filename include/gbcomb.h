@@ -57,6 +57,10 @@ extern "C" {
 #define GBC_SIZING_EXACT 0   /* symbolic pass + numeric pass (two-phase) */
 #define GBC_SIZING_LEARNED 1 /* MLP-predicted capacities, overflow re-run exactly */
 
+/* accumulation of PlusTimes fp64 products (gbc_context_set_fold) */
+#define GBC_FOLD_EXACT 0   /* exact sum of the rounded products, rounded once (default) */
+#define GBC_FOLD_ORDERED 1 /* left fold in B-entry order, the reference's hash path bit for bit */
+
 typedef struct gbc_context gbc_context;
 typedef struct gbc_result gbc_result;
 
@@ -102,6 +106,16 @@ int gbc_context_destroy(gbc_context *ctx);
 /* Use an existing cudaStream_t (passed as void*); NULL selects the
  * context's own stream. */
 int gbc_context_set_stream(gbc_context *ctx, void *stream);
+/* How PlusTimes fp64 products are summed into an output entry.  The
+ * reference folds them as acc = add(product, acc) over the B column's entries
+ * in order (mtSpGEMM.h:396-412).  GBC_FOLD_ORDERED reproduces that fold bit
+ * for bit.  GBC_FOLD_EXACT (the default) adds the same rounded products
+ * exactly and rounds the sum once to the nearest double: independent of any
+ * order, identical on every run, and within the reference's own rounding
+ * error of its result.  A column whose products span more than 61 binades,
+ * or whose values include subnormal, infinite or NaN entries, keeps the
+ * ordered fold. */
+int gbc_context_set_fold(gbc_context *ctx, int fold);
 int gbc_context_synchronize(gbc_context *ctx);
 const char *gbc_last_error(void);
 int gbc_version(void);

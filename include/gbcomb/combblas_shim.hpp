@@ -225,6 +225,12 @@ auto run(const M1 &A, const M2 &B, bool clearA, bool clearB, int sorted)
 
 inline void set_device(int device) { detail::device_slot() = device; }
 
+// PlusTimes fp64 accumulation of the offloaded products: GBC_FOLD_EXACT (the
+// library default: exact sum of the rounded products, rounded once) or
+// GBC_FOLD_ORDERED (the reference's hash-path fold, mtSpGEMM.h:396-412, bit
+// for bit).
+inline void set_fold(int fold) { detail::check(gbc_context_set_fold(detail::context(), fold), "gbc_context_set_fold"); }
+
 template <class SR, class NTO, class IT, class NT1, class NT2>
 combblas::SpTuples<IT, NTO> *LocalHybridSpGEMM(const combblas::SpDCCols<IT, NT1> &A,
                                                const combblas::SpDCCols<IT, NT2> &B, bool clearA, bool clearB,

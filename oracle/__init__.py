@@ -185,6 +185,9 @@ def _port():
         lib.gbc_o_spgemm.restype = C.c_int64
         lib.gbc_o_spgemm.argtypes = [C.c_int, C.c_int, C.c_int64, C.c_int64, C.c_int64, _P64, _P64, C.c_void_p,
                                      _P64, _P64, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.gbc_o_spgemm_exact.restype = C.c_int64
+        lib.gbc_o_spgemm_exact.argtypes = [C.c_int64, C.c_int64, C.c_int64, _P64, _P64, C.c_void_p, _P64, _P64,
+                                           C.c_void_p, C.c_void_p, C.c_void_p]
         lib.gbc_o_result.restype = None
         lib.gbc_o_result.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         lib.gbc_o_spmspv.restype = C.c_int64
@@ -208,9 +211,11 @@ def _port_csc(lib, ncol, nnz, dtype):
     return cp, rows, vals
 
 
-def port_spgemm(A, B, sr: int, sorted: bool = True, want_counts: bool = False):
+def port_spgemm(A, B, sr: int, sorted: bool = True, want_counts: bool = False, fold: str = "ordered"):
     """C = A*B by the C restatement.  Returns a CSC (generators.CSC-like
-    tuple: colptr, rowidx, values) and optionally (flop, nnz) per column."""
+    tuple: colptr, rowidx, values) and optionally (flop, nnz) per column.
+    fold="exact" (PlusTimes fp64 only): the library's exact fold -- each
+    entry the exact sum of the rounded products, rounded once (rows sorted)."""
     lib = _port()
     dt = SR_DTYPE[sr]
     av, ap = _vals_ptr(A, dt)
@@ -223,10 +228,18 @@ def port_spgemm(A, B, sr: int, sorted: bool = True, want_counts: bool = False):
         bp = bv.ctypes.data_as(C.c_void_p)
     flop = np.empty(B.ncol, np.int64)
     cnt = np.empty(B.ncol, np.int64)
-    nnz = lib.gbc_o_spgemm(sr, int(sorted), A.nrow, A.ncol, B.ncol, np.ascontiguousarray(A.colptr),
-                           np.ascontiguousarray(A.rowidx), ap, np.ascontiguousarray(B.colptr),
-                           np.ascontiguousarray(B.rowidx), bp, flop.ctypes.data_as(C.c_void_p),
-                           cnt.ctypes.data_as(C.c_void_p))
+    if fold == "exact":
+        if sr != SR_PLUSTIMES_F64:
+            raise ValueError("the exact fold is defined for PlusTimes fp64")
+        nnz = lib.gbc_o_spgemm_exact(A.nrow, A.ncol, B.ncol, np.ascontiguousarray(A.colptr),
+                                     np.ascontiguousarray(A.rowidx), ap, np.ascontiguousarray(B.colptr),
+                                     np.ascontiguousarray(B.rowidx), bp, flop.ctypes.data_as(C.c_void_p),
+                                     cnt.ctypes.data_as(C.c_void_p))
+    else:
+        nnz = lib.gbc_o_spgemm(sr, int(sorted), A.nrow, A.ncol, B.ncol, np.ascontiguousarray(A.colptr),
+                               np.ascontiguousarray(A.rowidx), ap, np.ascontiguousarray(B.colptr),
+                               np.ascontiguousarray(B.rowidx), bp, flop.ctypes.data_as(C.c_void_p),
+                               cnt.ctypes.data_as(C.c_void_p))
     if nnz < 0:
         raise ValueError("bad semiring")
     cp, rows, vals = _port_csc(lib, B.ncol, nnz, dt)

@@ -12,6 +12,8 @@
  *                     mtSpGEMM.h:206-210) or hash-slot order when unsorted.
  *                     Every column takes the hash path, so PlusTimes sums are
  *                     accumulated in B-entry order: val = add(mrhs, val).
+ *   gbc_o_spgemm_exact  PlusTimes<double> with the library's exact fold
+ *                     (sum of the same rounded products, rounded once).
  *   gbc_o_spmspv      SpMXSpV_Bucket (SpImpl.cpp:389-699): per-bucket row
  *                     split, SPA merge with the semiring add, sort of the
  *                     touched rows, output sorted by row.
@@ -261,6 +263,142 @@ int64_t gbc_o_spgemm(int sr, int sorted, int64_t m, int64_t k, int64_t n, const 
 }
 
 /* ----------------------------------------------------------------- SpMSpV */
+/* ------------------------------------------- exact PlusTimes fp64 fold */
+/* The library's GBC_FOLD_EXACT semantics, restated on the host: every
+ * product fl(a*b) is formed as the reference forms it, the products of one
+ * output entry are added exactly (a signed 128-bit integer in units of
+ * 2^(ebase-1075)), and the sum is rounded once to the nearest double, ties
+ * to even.  A column takes this fold when its products are normal, finite
+ * and span at most 61 binades, with the exact sum below 2^125 and the
+ * rounded result finite (the window is bounded from each A column's
+ * exponent range and each B value's exponent); other columns keep the hash
+ * path's left fold.  Output rows are sorted. */
+static void exp_range(int64_t ncol, const int64_t *Acp, const double *Av, int *amin, int *amax)
+{
+    _Pragma("omp parallel for schedule(static)")
+    for (int64_t c = 0; c < ncol; ++c) {
+        int lo = 32767, hi = -32768;
+        for (int64_t q = Acp[c]; q < Acp[c + 1]; ++q) {
+            uint64_t bits;
+            memcpy(&bits, &Av[q], 8);
+            if ((bits << 1) == 0) continue;
+            int e = (int)((bits >> 52) & 0x7ff);
+            if (e == 0) e = -64;
+            if (e < lo) lo = e;
+            if (e > hi) hi = e;
+        }
+        amin[c] = lo;
+        amax[c] = hi;
+    }
+}
+
+static int bit_length_i64(int64_t x)
+{
+    int b = 0;
+    while (x > 0) {
+        ++b;
+        x >>= 1;
+    }
+    return b;
+}
+
+static double round_exact(__int128 M, int nonnegzero, int ebase)
+{
+    if (M == 0) return nonnegzero ? 0.0 : -0.0;
+    const int neg = M < 0;
+    unsigned __int128 u = neg ? (unsigned __int128)(-M) : (unsigned __int128)M;
+    double d;
+    if (u < ((unsigned __int128)1 << 53)) {
+        d = ldexp((double)(uint64_t)u, ebase - 1075);
+    } else {
+        int top = 127;
+        while (!((u >> top) & 1)) --top;
+        int sh = top > 63 ? top - 63 : 0;
+        uint64_t w = (uint64_t)(u >> sh);
+        if (sh && (u & (((unsigned __int128)1 << sh) - 1))) w |= 1; /* sticky */
+        d = ldexp((double)w, sh + ebase - 1075); /* (double)w rounds to nearest even */
+    }
+    return neg ? -d : d;
+}
+
+/* C = A*B over PlusTimes<double> with the exact fold; result as gbc_o_spgemm
+ * (sorted rows).  Returns nnz(C). */
+int64_t gbc_o_spgemm_exact(int64_t m, int64_t k, int64_t n, const int64_t *Acp, const int64_t *Ari,
+                           const double *Av, const int64_t *Bcp, const int64_t *Bri, const double *Bv,
+                           int64_t *flop_out, int64_t *nnz_out)
+{
+    const int64_t tot = gbc_o_spgemm(SR_PT_F64, 1, m, k, n, Acp, Ari, Av, Bcp, Bri, Bv, flop_out, nnz_out);
+    int *amin = (int *)malloc((size_t)(k > 0 ? k : 1) * sizeof(int));
+    int *amax = (int *)malloc((size_t)(k > 0 ? k : 1) * sizeof(int));
+    exp_range(k, Acp, Av, amin, amax);
+    double *Cv = (double *)g_vals;
+    _Pragma("omp parallel")
+    {
+        int64_t cap = 0;
+        __int128 *acc = NULL;
+        unsigned char *nz = NULL;
+        _Pragma("omp for schedule(dynamic, 64)") for (int64_t j = 0; j < n; ++j)
+        {
+            int ebase = 1 << 30, etop = -(1 << 30);
+            for (int64_t p = Bcp[j]; p < Bcp[j + 1]; ++p) {
+                const int64_t c = Bri[p];
+                uint64_t bb;
+                memcpy(&bb, &Bv[p], 8);
+                if (amin[c] > amax[c] || (bb << 1) == 0) continue;
+                int eb = (int)((bb >> 52) & 0x7ff);
+                if (eb == 0) eb = -64;
+                if (amin[c] + eb - 1023 < ebase) ebase = amin[c] + eb - 1023;
+                if (amax[c] + eb - 1022 > etop) etop = amax[c] + eb - 1022;
+            }
+            const int lg = bit_length_i64(Bcp[j + 1] - Bcp[j]);
+            if (ebase > etop) {
+                ebase = 1;
+            } else if (!(ebase >= 1 && etop <= 2046 - lg - 2 && etop - ebase <= 61 && etop - ebase + 53 + lg <= 125)) {
+                continue; /* keeps the hash path's left fold */
+            }
+            const int64_t c0 = g_colptr[j], c1 = g_colptr[j + 1];
+            if (c1 - c0 > cap) {
+                free(acc);
+                free(nz);
+                cap = c1 - c0;
+                acc = (__int128 *)malloc((size_t)cap * sizeof(__int128));
+                nz = (unsigned char *)malloc((size_t)cap);
+            }
+            memset(acc, 0, (size_t)(c1 - c0) * sizeof(__int128));
+            memset(nz, 0, (size_t)(c1 - c0));
+            for (int64_t p = Bcp[j]; p < Bcp[j + 1]; ++p) {
+                const int64_t c = Bri[p];
+                const double b = Bv[p];
+                for (int64_t q = Acp[c]; q < Acp[c + 1]; ++q) {
+                    const double prod = Av[q] * b;
+                    int64_t lo = c0, hi = c1;
+                    while (lo < hi) {
+                        const int64_t mid = (lo + hi) >> 1;
+                        if (g_rows[mid] < Ari[q])
+                            lo = mid + 1;
+                        else
+                            hi = mid;
+                    }
+                    const int64_t o = lo - c0;
+                    uint64_t bits;
+                    memcpy(&bits, &prod, 8);
+                    if (bits != (1ull << 63)) nz[o] = 1;
+                    const int e = (int)((bits >> 52) & 0x7ff);
+                    if (e == 0) continue; /* zero: admitted columns have no subnormal products */
+                    const __int128 mag = (__int128)((bits & 0xFFFFFFFFFFFFFull) | (1ull << 52)) << (e - ebase);
+                    acc[o] += (bits >> 63) ? -mag : mag;
+                }
+            }
+            for (int64_t o = c0; o < c1; ++o) Cv[o] = round_exact(acc[o - c0], nz[o - c0], ebase);
+        }
+        free(acc);
+        free(nz);
+    }
+    free(amin);
+    free(amax);
+    return tot;
+}
+
 static int cmp_i32(const void *x, const void *y)
 {
     int32_t a = *(const int32_t *)x, b = *(const int32_t *)y;

@@ -4,6 +4,7 @@
 #include "mock_combblas.hpp"
 
 #include <cstdio>
+#include <cmath>
 #include <cstring>
 #include <random>
 
@@ -78,7 +79,9 @@ bool same(const SpTuples<I, NT> *a, const SpTuples<I, NT> *b)
 int main()
 {
     typedef PlusTimesSRing<double, double> PT;
-    // 1. PlusTimes fp64 over DCSC, bit-exact against the CPU product
+    // 1. PlusTimes fp64 over DCSC with the ordered fold, bit-exact against
+    //    the CPU product (the exact fold is checked within 1e-12 at the end)
+    gbcomb::set_fold(GBC_FOLD_ORDERED);
     SpDCCols<I, double> *A = random_dcsc<double>(700, 500, 0.02, 0.3, 1);
     SpDCCols<I, double> *B = random_dcsc<double>(500, 400, 0.03, 0.3, 2);
     const int fb0 = fallback_calls();
@@ -241,6 +244,26 @@ int main()
     delete B2;
     delete Bs;
     delete Ai;
+    // 10. the default exact fold: same pattern, every value within 1e-12
+    {
+        gbcomb::set_fold(GBC_FOLD_EXACT);
+        SpDCCols<I, double> *X = random_dcsc<double>(700, 500, 0.02, 0.3, 11);
+        SpDCCols<I, double> *Y = random_dcsc<double>(500, 400, 0.03, 0.3, 12);
+        SpTuples<I, double> *gx = gbcomb::LocalHybridSpGEMM<PT, double>(*X, *Y, false, false);
+        SpTuples<I, double> *cx = combblas::LocalHybridSpGEMM<PT, double>(*X, *Y, false, false);
+        bool ok = gx->getnnz() == cx->getnnz() && gx->getnnz() > 0;
+        for (int64_t p = 0; ok && p < gx->getnnz(); ++p) {
+            ok = std::get<0>(gx->tuples[p]) == std::get<0>(cx->tuples[p]) &&
+                 std::get<1>(gx->tuples[p]) == std::get<1>(cx->tuples[p]);
+            const double x = std::get<2>(gx->tuples[p]), y = std::get<2>(cx->tuples[p]);
+            ok = ok && std::fabs(x - y) <= 1e-12 * std::fabs(y);
+        }
+        EXPECT(ok);
+        delete gx;
+        delete cx;
+        delete X;
+        delete Y;
+    }
     if (failures == 0) std::printf("OK\n");
     return failures == 0 ? 0 : 1;
 }

@@ -26,7 +26,7 @@ def test_batch_matches_one_by_one_and_oracle(gpu_ctx, oracle_lib):
         cp, ir, num = b.result(p)
         ecp, eir, enum = local.spgemm(A, B).to_csc()
         assert np.array_equal(cp, ecp) and np.array_equal(ir, eir) and np.array_equal(num, enum), p
-        pcp, pir, pnum = O.port_spgemm(A, B, O.SR_PLUSTIMES_F64)
+        pcp, pir, pnum = O.port_spgemm(A, B, O.SR_PLUSTIMES_F64, fold="exact")  # the default fold
         assert np.array_equal(cp, pcp) and np.array_equal(ir, pir) and np.array_equal(num, pnum), p
     b.close()
 

@@ -11,7 +11,14 @@ pytestmark = pytest.mark.gpu
 
 
 def test_merge_golden(gpu_ctx, oracle_lib, golden):
+    """Under the ordered fold the lists are folded in list order (the
+    oracle's restatement); the exact fold is checked in the next test."""
     O = oracle_lib
+    with gpu_ctx.folding("ordered"):
+        _merge_golden(O, golden)
+
+
+def _merge_golden(O, golden):
     for K in (2, 4):
         for sr, name, dt in ((O.SR_PLUSTIMES_F64, "plustimes", np.float64), (O.SR_SELECT2NDMIN_I64, "select2ndmin",
                                                                              np.int64)):
@@ -31,9 +38,18 @@ def test_merge_semirings_and_dcsc(gpu_ctx, oracle_lib, sr):
     name, dt = SR_NAME[sr]
     lists = [typed(G.random_sparse(700, 500, 0.01, seed=60 + k, empty_cols=0.3), sr, 70 + k, O) for k in range(3)]
     ins = [local.DCSC.from_csc(M) if k % 2 else M for k, M in enumerate(lists)]  # mixed CSC / DCSC inputs
-    cp, rows, vals = local.MultiwayMerge(ins, 700, 500, sr=name, dtype=dt).to_csc()
     pcp, prow, pval = O.port_multiway_merge(lists, 700, 500, sr)
+    with gpu_ctx.folding("ordered"):
+        cp, rows, vals = local.MultiwayMerge(ins, 700, 500, sr=name, dtype=dt).to_csc()
     assert np.array_equal(cp, pcp) and np.array_equal(rows, prow) and np.array_equal(vals, pval)
+    # the default exact fold: fp64 sums of three lists rounded once (within
+    # the list-order fold's rounding); every other semiring unchanged
+    cp, rows, vals = local.MultiwayMerge(ins, 700, 500, sr=name, dtype=dt).to_csc()
+    assert np.array_equal(cp, pcp) and np.array_equal(rows, prow)
+    if sr == 0:
+        assert np.max(np.abs(vals - pval) / np.abs(pval)) <= 1e-15
+    else:
+        assert np.array_equal(vals, pval)
 
 
 def test_merge_edges(gpu_ctx):

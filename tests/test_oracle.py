@@ -195,3 +195,80 @@ def test_port_spmv(oracle_lib, golden):
     for sr in (O.SR_PLUSTIMES_F64, O.SR_MINPLUS_F64, O.SR_SELECT2NDMIN_I64, O.SR_BOOL):
         y = O.port_spmv(typed(M, sr, 50 + sr, O), golden[f"spmv/{sr}/x"], golden[f"spmv/{sr}/y0"], sr)
         assert np.array_equal(y, golden[f"spmv/{sr}/y"]), sr
+
+
+def _fsum_product(A, B):
+    """Each entry of A*B as math.fsum of its products fl(a*b): the correctly
+    rounded sum (an independent restatement of the exact fold)."""
+    import math
+
+    cps, rows, vals, negz = [0], [], [], []
+    for j in range(B.ncol):
+        ks = B.rowidx[B.colptr[j]:B.colptr[j + 1]]
+        bv = B.values[B.colptr[j]:B.colptr[j + 1]]
+        if len(ks) == 0:
+            cps.append(cps[-1])
+            continue
+        rr = np.concatenate([A.rowidx[A.colptr[k]:A.colptr[k + 1]] for k in ks])
+        pv = np.concatenate([A.values[A.colptr[k]:A.colptr[k + 1]] * b for k, b in zip(ks, bv)])
+        order = np.argsort(rr, kind="stable")
+        rr, pv = rr[order], pv[order]
+        u, st = np.unique(rr, return_index=True)
+        en = np.append(st[1:], len(rr))
+        rows.append(u)
+        vals.append(np.array([math.fsum(pv[s:e]) for s, e in zip(st, en)]))
+        # fsum returns +0.0 for sums of -0.0 only; the fold keeps -0.0 there
+        negz.append(np.array([bool(np.all((pv[s:e] == 0) & np.signbit(pv[s:e]))) for s, e in zip(st, en)]))
+        cps.append(cps[-1] + len(u))
+    v = np.concatenate(vals)
+    v[np.concatenate(negz)] = -0.0
+    return np.array(cps), np.concatenate(rows), v
+
+
+@pytest.mark.parametrize("case", ["rmat", "signed"])
+def test_port_exact_fold_is_fsum(oracle_lib, case):
+    """The oracle's exact fold gives every entry as the correctly rounded
+    sum of its rounded products (math.fsum), signs of zero included, on
+    admitted columns; it stays within 1e-12 of the hash-path fold."""
+    O = oracle_lib
+    if case == "rmat":
+        A = G.rmat(10, 8, seed=10)
+    else:
+        rng = np.random.default_rng(1)
+        A = G.random_sparse(300, 300, 0.05, seed=3)
+        A.values = rng.standard_normal(A.nnz) * np.exp2(rng.integers(-10, 10, A.nnz).astype(np.float64))
+        A.values[rng.random(A.nnz) < 0.05] = 0.0
+        A.values[rng.random(A.nnz) < 0.02] = -0.0
+    cp, rows, vals = O.port_spgemm(A, A, O.SR_PLUSTIMES_F64, fold="exact")
+    ecp, erows, evals = _fsum_product(A, A)
+    assert np.array_equal(cp, ecp) and np.array_equal(rows, erows)
+    assert np.array_equal(vals.view(np.int64), evals.view(np.int64))
+    if case == "rmat":
+        ocp, orow, oval = O.port_spgemm(A, A, O.SR_PLUSTIMES_F64)
+        assert np.array_equal(orow, rows)
+        assert np.max(np.abs(oval - vals) / np.abs(vals)) <= 1e-12
+        assert np.mean(oval != vals) > 0.01  # the folds do differ in the last bits
+
+
+def test_port_exact_fold_admission(oracle_lib):
+    """A column whose product window spans more than 61 binades keeps the
+    hash-path fold under fold="exact"; the other columns are exact."""
+    O = oracle_lib
+    rng = np.random.default_rng(2)
+    A = G.random_sparse(200, 200, 0.08, seed=4)
+    A.values = 1.0 + rng.random(A.nnz)
+    wide = A.colptr[3], A.colptr[4]
+    A.values[wide[0]] = 2.0 ** -80  # products with column 3 reach 80 binades below the rest
+    x = O.port_spgemm(A, A, O.SR_PLUSTIMES_F64, fold="exact")
+    o = O.port_spgemm(A, A, O.SR_PLUSTIMES_F64)
+    f = _fsum_product(A, A)
+    assert np.array_equal(x[0], o[0]) and np.array_equal(x[1], o[1])
+    # columns j with B(3, j) != 0 (they use A's column 3) and column 3 itself
+    # (its B values hold the small one) take the ordered fold, the rest are exact
+    Bcols = set(np.nonzero([3 in A.rowidx[A.colptr[j]:A.colptr[j + 1]] for j in range(A.ncol)])[0].tolist()) | {3}
+    for j in range(A.ncol):
+        s, e = x[0][j], x[0][j + 1]
+        want = o[2][s:e] if j in Bcols else f[2][s:e]
+        assert np.array_equal(x[2][s:e], want), j
+    assert len(Bcols) > 0 and any(not np.array_equal(o[2][x[0][j]:x[0][j + 1]], f[2][x[0][j]:x[0][j + 1]])
+                                  for j in range(A.ncol) if j not in Bcols)

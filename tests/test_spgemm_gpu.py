@@ -1,5 +1,11 @@
 """GPU SpGEMM through the C ABI against the reference's golden outputs and
-the oracle's C restatement."""
+the oracle's C restatement.
+
+PlusTimes fp64 runs under both folds: "ordered" (the reference's hash-path
+left fold, bit-exact against the reference's hash variants and the oracle)
+and "exact" (the default: each entry the exact sum of the rounded products,
+rounded once -- bit-exact against the oracle's exact fold, within 1e-12 of
+the reference)."""
 import numpy as np
 import pytest
 
@@ -16,10 +22,19 @@ SR_NAME = {0: ("plustimes", np.float64), 1: ("plustimes", np.float32), 2: ("plus
 TOL = {0: 1e-12, 1: 1e-5}  # PlusTimes fp64 / fp32 (relative), against the hybrid's heap columns
 
 
-def gpu_csc(A, B, sr, **kw):
+FOLDS = ["ordered", "exact"]
+
+
+def gpu_csc(A, B, sr, fold="ordered", **kw):
     name, dt = SR_NAME[sr]
-    R = local.spgemm(A, B, sr=name, dtype=dt, **kw)
+    R = local.spgemm(A, B, sr=name, dtype=dt, fold=fold, **kw)
     return R.to_csc()
+
+
+def port(O, A, B, sr, fold="ordered", **kw):
+    """The oracle's product under the fold the GPU ran with (the fold only
+    changes PlusTimes fp64)."""
+    return O.port_spgemm(A, B, sr, fold=fold if sr == 0 else "ordered", **kw)
 
 
 def assert_same(cp, rows, vals, ecp, erows, evals, sr=None, exact=True, what=""):
@@ -32,7 +47,8 @@ def assert_same(cp, rows, vals, ecp, erows, evals, sr=None, exact=True, what="")
         assert rel.max(initial=0) <= TOL[sr], (what, rel.max())
 
 
-def test_golden_products(gpu_ctx, oracle_lib, golden):
+@pytest.mark.parametrize("fold", FOLDS)
+def test_golden_products(gpu_ctx, oracle_lib, golden, fold):
     O = oracle_lib
     g = golden
     for key in prod_cases(g):
@@ -48,38 +64,63 @@ def test_golden_products(gpu_ctx, oracle_lib, golden):
             M = golden_matrix(g, name)
             A = typed(M, sr, 1, O)
             B = A if kind != "AAt" else typed(G.transpose(M), sr, 2, O)
-        cp, rows, vals = gpu_csc(A, B, sr)
+        cp, rows, vals = gpu_csc(A, B, sr, fold)
         ecp, erows, evals = O.tuples_to_csc(g[f"{key}/rows"], g[f"{key}/cols"], g[f"{key}/vals"], B.ncol)
-        exact = variant in (O.V_HASH_SORTED, O.V_HASH_UNSORTED)
+        exact = variant in (O.V_HASH_SORTED, O.V_HASH_UNSORTED) and (fold == "ordered" or sr != 0)
         assert_same(cp, rows, vals, ecp, erows, evals, sr, exact, key)
-        # bit-exact against the oracle (same summation order)
-        pcp, prow, pval = O.port_spgemm(A, B, sr)
+        # bit-exact against the oracle under the same fold
+        pcp, prow, pval = port(O, A, B, sr, fold)
         assert_same(cp, rows, vals, pcp, prow, pval, sr, True, key + " vs port")
 
 
-def test_golden_galerkin(gpu_ctx, oracle_lib, golden):
+@pytest.mark.parametrize("fold", FOLDS)
+def test_golden_galerkin(gpu_ctx, oracle_lib, golden, fold):
+    """Galerkin values are small integers: every fold gives them exactly."""
     O = oracle_lib
     A = golden_matrix(golden, "poisson4")
     R = golden_matrix(golden, "agg4")
     Rt = G.transpose(R)
-    cp, rows, vals = gpu_csc(A, Rt, 0)
+    cp, rows, vals = gpu_csc(A, Rt, 0, fold)
     AR = G.CSC(A.nrow, Rt.ncol, cp, rows, vals)
-    cp2, rows2, vals2 = gpu_csc(R, AR, 0)
+    cp2, rows2, vals2 = gpu_csc(R, AR, 0, fold)
     key = "prod/galerkin4/RAR/0"
     ecp, erows, evals = O.tuples_to_csc(golden[f"{key}/rows"], golden[f"{key}/cols"], golden[f"{key}/vals"], AR.ncol)
     assert_same(cp2, rows2, vals2, ecp, erows, evals, 0, True, key)
 
 
+@pytest.mark.parametrize("fold", FOLDS)
 @pytest.mark.parametrize("scale,ef", [(12, 8), (14, 8), (15, 4)])
-def test_rmat_fp64_bitexact_vs_port(gpu_ctx, oracle_lib, scale, ef):
+def test_rmat_fp64_bitexact_vs_port(gpu_ctx, oracle_lib, scale, ef, fold):
     O = oracle_lib
     A = G.rmat(scale, ef, seed=scale)
-    cp, rows, vals = gpu_csc(A, A, 0)
-    pcp, prow, pval = O.port_spgemm(A, A, O.SR_PLUSTIMES_F64)
+    cp, rows, vals = gpu_csc(A, A, 0, fold)
+    pcp, prow, pval = port(O, A, A, 0, fold)
     assert_same(cp, rows, vals, pcp, prow, pval, 0, True, f"rmat{scale}")
     # repeated runs are bit-identical
-    cp2, rows2, vals2 = gpu_csc(A, A, 0)
+    cp2, rows2, vals2 = gpu_csc(A, A, 0, fold)
     assert np.array_equal(vals, vals2) and np.array_equal(rows, rows2)
+    if fold == "exact":  # and within the reference's rounding of the hash-path fold
+        ocp, orow, oval = O.port_spgemm(A, A, O.SR_PLUSTIMES_F64)
+        assert_same(cp, rows, vals, ocp, orow, oval, 0, False, f"rmat{scale} exact vs ordered")
+
+
+@pytest.mark.parametrize("opts", [{}, dict(tiny_limit=0, small_limit=0)])
+def test_exact_fold_signed_zeros_and_fallback_columns(gpu_ctx, oracle_lib, opts):
+    """Signed values, explicit +0.0/-0.0, exact cancellation, and columns
+    whose products span too many binades (those keep the ordered fold):
+    bit-exact against the oracle's exact fold, which applies the same
+    column admission."""
+    O = oracle_lib
+    rng = np.random.default_rng(11)
+    A = G.random_sparse(3000, 3000, 0.004, seed=12)
+    e = np.where(rng.random(A.nnz) < 0.97, rng.integers(-12, 12, A.nnz), rng.integers(-300, 300, A.nnz))
+    A.values = rng.standard_normal(A.nnz) * np.exp2(e.astype(np.float64))
+    A.values[rng.random(A.nnz) < 0.03] = 0.0
+    A.values[rng.random(A.nnz) < 0.03] = -0.0
+    cp, rows, vals = gpu_csc(A, A, 0, "exact", **opts)
+    pcp, prow, pval = port(O, A, A, 0, "exact")
+    assert np.array_equal(cp, pcp) and np.array_equal(rows, prow)
+    assert np.array_equal(vals.view(np.int64), pval.view(np.int64))  # signs of zero included
 
 
 @pytest.mark.parametrize("sr", [1, 2, 3, 4, 5, 6])
@@ -94,24 +135,26 @@ def test_rmat_semirings_vs_port(gpu_ctx, oracle_lib, sr):
 @pytest.mark.parametrize("opts", [dict(tile_rows=8192), dict(tile_rows=4096),
                                   dict(tile_rows=8192, tiny_limit=64, small_limit=1024),
                                   dict(tiny_limit=0, small_limit=0)])
-@pytest.mark.parametrize("sr", [0, 5])
-def test_tile_and_class_options_vs_port(gpu_ctx, oracle_lib, opts, sr):
+@pytest.mark.parametrize("sr,fold", [(0, "ordered"), (0, "exact"), (5, "ordered")])
+def test_tile_and_class_options_vs_port(gpu_ctx, oracle_lib, opts, sr, fold):
     """Row-tile height and warp-path limits change the schedule, never the
     result: every option set is bit-exact against the oracle."""
     O = oracle_lib
     A = typed(G.rmat(15, 8, seed=5), sr, 7, O)
-    cp, rows, vals = gpu_csc(A, A, sr, **opts)
-    pcp, prow, pval = O.port_spgemm(A, A, sr)
+    cp, rows, vals = gpu_csc(A, A, sr, fold, **opts)
+    pcp, prow, pval = port(O, A, A, sr, fold)
     assert_same(cp, rows, vals, pcp, prow, pval, sr, True, str(opts))
 
 
-def test_tall_matrix_many_tiles(gpu_ctx, oracle_lib):
-    """m > 1M rows: several row tiles and several symbolic bitmaps."""
+@pytest.mark.parametrize("fold", FOLDS)
+def test_tall_matrix_many_tiles(gpu_ctx, oracle_lib, fold):
+    """m > 1M rows: several row tiles and several symbolic bitmaps (beyond
+    the exact kernel's bucketing limit: its per-tile enumeration mode)."""
     O = oracle_lib
     A = G.random_sparse(1_500_000, 400, 2e-5, seed=2)
     B = G.random_sparse(400, 300, 0.05, seed=3)
-    cp, rows, vals = gpu_csc(A, B, 0)
-    pcp, prow, pval = O.port_spgemm(A, B, O.SR_PLUSTIMES_F64)
+    cp, rows, vals = gpu_csc(A, B, 0, fold, tiny_limit=0, small_limit=0)
+    pcp, prow, pval = port(O, A, B, 0, fold)
     assert_same(cp, rows, vals, pcp, prow, pval, 0, True, "tall")
 
 
@@ -124,7 +167,7 @@ def test_dcsc_inputs_and_views(gpu_ctx, oracle_lib):
     cp, jc, ir, num = R.to_host()
     assert np.array_equal(jc, Bd.jc)  # SpTuples view: one column per stored column of B
     full, rows, vals = R.to_csc()
-    pcp, prow, pval = O.port_spgemm(A, B, O.SR_PLUSTIMES_F64)
+    pcp, prow, pval = port(O, A, B, 0, "exact")  # the default fold
     assert_same(full, rows, vals, pcp, prow, pval, 0, True, "dcsc")
     R2 = local.spgemm(Ad, Bd, keep_empty=False)  # SpDCCols view drops empty output columns
     cp2, jc2, ir2, num2 = R2.to_host()
@@ -137,7 +180,7 @@ def test_device_resident_inputs(gpu_ctx, oracle_lib):
     A = G.rmat(11, 8, seed=4)
     Ad = local.DeviceMatrix.from_host(A)
     cp, rows, vals = local.spgemm(Ad, Ad).to_csc()
-    pcp, prow, pval = O.port_spgemm(A, A, O.SR_PLUSTIMES_F64)
+    pcp, prow, pval = port(O, A, A, 0, "exact")
     assert_same(cp, rows, vals, pcp, prow, pval, 0, True, "device")
 
 
@@ -159,9 +202,10 @@ def test_edge_cases(gpu_ctx, oracle_lib):
     cols = np.concatenate([A.col_ids(), np.full(300, 7)])
     D = G.csc_from_coo(300, 300, rows, cols)
     D.values = np.linspace(0.1, 1.0, D.nnz)
-    cp, rows, vals = local.spgemm(D, D).to_csc()
-    pcp, prow, pval = O.port_spgemm(D, D, O.SR_PLUSTIMES_F64)
-    assert_same(cp, rows, vals, pcp, prow, pval, 0, True, "dense column")
+    for fold in FOLDS:
+        cp, rows, vals = local.spgemm(D, D, fold=fold).to_csc()
+        pcp, prow, pval = port(O, D, D, 0, fold)
+        assert_same(cp, rows, vals, pcp, prow, pval, 0, True, "dense column " + fold)
 
 
 def test_errors_are_reported(gpu_ctx):
@@ -209,17 +253,19 @@ def content_hash(cp, rows, vals, cols=None):
         return int(np.sum(x, dtype=u))
 
 
-def test_phased_matches_single_pass(gpu_ctx, oracle_lib):
+@pytest.mark.parametrize("fold", FOLDS)
+def test_phased_matches_single_pass(gpu_ctx, oracle_lib, fold):
     """Column phases (small budget -> many phases) give the same nnz and
     checksums as the single-pass product and the oracle."""
     O = oracle_lib
     A = G.rmat(13, 8, seed=6)
-    cp, rows, vals = gpu_csc(A, A, 0)
-    pcp, prow, pval = O.port_spgemm(A, A, O.SR_PLUSTIMES_F64)
+    cp, rows, vals = gpu_csc(A, A, 0, fold)
+    pcp, prow, pval = port(O, A, A, 0, fold)
     ref_rows = int(prow.sum())
     ref_hash = content_hash(pcp, prow, pval)
+    assert content_hash(cp, rows, vals) == ref_hash
     for budget in (len(rows), 200_000, 50_000):
-        st = local.spgemm_phased(A, A, max_phase_nnz=budget)
+        st = local.spgemm_phased(A, A, max_phase_nnz=budget, fold=fold)
         assert st.nnz == len(prow) and st.row_checksum == ref_rows
         assert st.content_hash == ref_hash
         assert abs(st.val_checksum - pval.sum()) <= 1e-9 * abs(pval.sum())
@@ -228,8 +274,8 @@ def test_phased_matches_single_pass(gpu_ctx, oracle_lib):
         assert st.flops == int(O.port_spgemm(A, A, O.SR_PLUSTIMES_F64, want_counts=True)[1][0].sum())
 
 
-@pytest.mark.parametrize("margin", [None, 0.0])
-def test_phased_learned_identical_to_exact(gpu_ctx, oracle_lib, margin):
+@pytest.mark.parametrize("margin,fold", [(None, "exact"), (0.0, "exact"), (0.0, "ordered")])
+def test_phased_learned_identical_to_exact(gpu_ctx, oracle_lib, margin, fold):
     """Learned phase sizing (model trained on another seed of the same
     class; margin 0 forces many overflow re-runs) gives the exact product's
     nnz, row checksum and content hash."""
@@ -244,11 +290,11 @@ def test_phased_learned_identical_to_exact(gpu_ctx, oracle_lib, margin):
         m.set_margin(margin)
     m.use()
     try:
-        pcp, prow, pval = O.port_spgemm(A, A, O.SR_PLUSTIMES_F64)
+        pcp, prow, pval = port(O, A, A, 0, fold)
         ref_hash = content_hash(pcp, prow, pval)
         for budget in (1 << 40, 400_000):
-            ex = local.spgemm_phased(A, A, max_phase_nnz=budget)
-            le = local.spgemm_phased(A, A, max_phase_nnz=budget, sizing="learned")
+            ex = local.spgemm_phased(A, A, max_phase_nnz=budget, fold=fold)
+            le = local.spgemm_phased(A, A, max_phase_nnz=budget, sizing="learned", fold=fold)
             assert ex.content_hash == ref_hash
             assert (le.nnz, le.row_checksum, le.content_hash) == (ex.nnz, ex.row_checksum, ex.content_hash)
             assert le.alloc_nnz >= 1 and le.flops == ex.flops
