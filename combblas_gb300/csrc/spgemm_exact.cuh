@@ -45,6 +45,38 @@ constexpr int kXNorm = 2047;                 // B entries between carry normalis
 constexpr int kXRows = 4096;                 // rows of one accumulator tile
 constexpr int kXThreads = 512;
 
+// Phase clocks of k_numeric_x for profiling builds (-DGBC_XPROF): thread 0
+// of every block adds the cycles between two block barriers to a counter.
+#ifdef GBC_XPROF
+__device__ unsigned long long g_xprof[32];
+#define XPROF_T0 long long xp_t = clock64()
+#define XPROF_LAP(id)                                                          \
+    do {                                                                       \
+        if (threadIdx.x == 0) {                                                \
+            const long long xp_n = clock64();                                  \
+            atomicAdd(&g_xprof[id], (unsigned long long)(xp_n - xp_t));        \
+            xp_t = xp_n;                                                       \
+        }                                                                      \
+    } while (0)
+#define XPROF_ADD(id, v)                                                       \
+    do {                                                                       \
+        if (threadIdx.x == 0) atomicAdd(&g_xprof[id], (unsigned long long)(v)); \
+    } while (0)
+extern "C" int gbc_xprof_read(unsigned long long *out, int reset)
+{
+    cudaMemcpyFromSymbol(out, g_xprof, sizeof(g_xprof));
+    if (reset) {
+        static const unsigned long long z[32] = {};
+        cudaMemcpyToSymbol(g_xprof, z, sizeof(z));
+    }
+    return (int)cudaDeviceSynchronize();
+}
+#else
+#define XPROF_T0
+#define XPROF_LAP(id)
+#define XPROF_ADD(id, v)
+#endif
+
 // Per column of A: smallest and largest biased exponent of its nonzero
 // values, packed as (int16 min) | (int16 max << 16).  Subnormal values count
 // as exponent -64 (their products can underflow: such columns take the
@@ -379,6 +411,7 @@ __global__ void __launch_bounds__(NT, 2)
     for (int u = tid; u < kXW * RS + RS / 4; u += NT) xsm[u] = 0;
     bool dirty = false;  // the word area holds a range visit's data
     bool first_item = true;
+    XPROF_T0;
 
     // block-wide exclusive prefix of v over the threads (two barriers); *tot the sum
     auto block_prefix = [&](int v, int *tot) -> int {
@@ -463,6 +496,7 @@ __global__ void __launch_bounds__(NT, 2)
             __syncthreads();  // s_col / sa / s_emin reuse
             continue;
         }
+        XPROF_LAP(0);
 
         // dense visit helpers: products of a chunk into the word accumulator,
         // and the write-out of tile row0's touched rows
@@ -564,6 +598,8 @@ __global__ void __launch_bounds__(NT, 2)
                 }
             }
             // s_off[t] is now the end of tile t's segments
+            XPROF_LAP(1);
+            XPROF_ADD(bucketed ? 11 : 12, 1);
         }
 
         if (bucketed) {
@@ -601,8 +637,13 @@ __global__ void __launch_bounds__(NT, 2)
                         int nseg;
                         const int L = compact_chunk<uint32_t, NT>(ch, s0, len, e0, ch_e, nseg);
                         dense_products(L, nseg, row0);
+                        XPROF_ADD(14, L);
                     }
+                    __syncthreads();
+                    XPROF_LAP(2);
                     dense_writeout(row0);
+                    XPROF_LAP(3);
+                    XPROF_ADD(8, 1);
                     ++t;
                 } else {
                     // range visit of tiles t .. t1 (at most kXRange products)
@@ -640,6 +681,9 @@ __global__ void __launch_bounds__(NT, 2)
                         pbase += L;
                         __syncthreads();  // chunk table reuse
                     }
+                    XPROF_LAP(4);
+                    XPROF_ADD(9, 1);
+                    XPROF_ADD(13, prods);
                     // stable LSD radix sort of the keys by row, 7-bit digits:
                     // warp w owns a contiguous run of keys, counts its digits,
                     // the (digit, warp) counts are scanned digit-major, and
@@ -696,6 +740,7 @@ __global__ void __launch_bounds__(NT, 2)
                         src = dst;
                         dst = tmp;
                     }
+                    XPROF_LAP(5);
                     // runs of one row: the head sums its run exactly and writes it
                     for (int u0 = 0; u0 < prods; u0 += NT) {
                         const int u = u0 + tid;
@@ -723,6 +768,7 @@ __global__ void __launch_bounds__(NT, 2)
                         out += tot;
                     }
                     __syncthreads();
+                    XPROF_LAP(6);
                     t = t1 + 1;
                 }
             }
@@ -767,11 +813,14 @@ __global__ void __launch_bounds__(NT, 2)
                     dense_products(L, nseg, row0);
                 }
                 dense_writeout(row0);
+                XPROF_LAP(7);
+                XPROF_ADD(10, 1);
                 t = tn;
             }
         }
         over = __syncthreads_or(over);
         bad = __syncthreads_or(bad);
+        XPROF_LAP(15);
         if (tid == 0) {
             if (out_cnt) out_cnt[g] = out - out0;
             if (over) {
