@@ -200,9 +200,11 @@ __device__ __forceinline__ void x_normalise(int32_t *acc, int stride, int r)
 }
 
 // Round a signed 128-bit integer M (two's complement hi:lo), times
-// 2^(ebase - 1075), to the nearest double (ties to even).  flag bit 1 says
-// whether some term was other than -0.0: an exact zero sum is then +0.0,
-// else -0.0 (what the left fold of the reference gives).
+// 2^(ebase - 1075), to the nearest double (ties to even), in integer
+// arithmetic (IEEE 754 rounding of the exact value; GB300's fp64 units are
+// slow).  flag bit 1 says whether some term was other than -0.0: an exact
+// zero sum is then +0.0, else -0.0 (what the left fold of the reference
+// gives).  For admitted columns |M| < 2^126 and the result is finite.
 __device__ __forceinline__ double x_round(uint64_t hi, uint64_t lo, uint32_t flag, int ebase)
 {
     const bool neg = (int64_t)hi < 0;
@@ -211,24 +213,31 @@ __device__ __forceinline__ double x_round(uint64_t hi, uint64_t lo, uint32_t fla
         hi = ~hi + (lo == 0 ? 1ull : 0ull);
     }
     if ((hi | lo) == 0) return (flag & 2) ? 0.0 : -0.0;
-    double d;
-    if (hi == 0 && lo < (1ull << 53)) {
-        d = ldexp((double)lo, ebase - 1075);  // exact, subnormal results included
+    const int tb = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);  // top bit of |M|
+    const int e = tb + ebase - 52;  // biased exponent when the result is normal
+    uint64_t bits;
+    if (e <= 0) {
+        // subnormal: |M| * 2^(ebase - 1) < 2^52 is the exact subnormal mantissa
+        bits = lo << (ebase - 1);
+    } else if (tb <= 52) {
+        bits = ((uint64_t)e << 52) + ((lo << (52 - tb)) & 0xFFFFFFFFFFFFFull);  // exact
     } else {
-        const int tb = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);
-        uint64_t mant = lo;
-        int sh = 0;
-        if (tb > 63) {
-            sh = tb - 63;  // 1..62
-            mant = (hi << (64 - sh)) | (lo >> sh);
-            mant |= (lo & ((1ull << sh) - 1)) != 0 ? 1ull : 0ull;  // sticky bit below the rounding point
+        const int sh = tb - 52;  // 1..73 bits below the 53 kept
+        uint64_t m, rnd, sticky;
+        if (sh < 64) {
+            m = (lo >> sh) | (sh ? (hi << (64 - sh)) : 0ull);
+            rnd = (lo >> (sh - 1)) & 1;
+            sticky = (sh > 1 && (lo << (65 - sh)) != 0) ? 1 : 0;
+        } else {
+            m = hi >> (sh - 64);
+            rnd = sh == 64 ? (lo >> 63) : ((hi >> (sh - 65)) & 1);
+            sticky = (lo & (sh == 64 ? 0x7FFFFFFFFFFFFFFFull : ~0ull)) != 0 ||
+                     (sh > 65 && (hi << (129 - sh)) != 0);
         }
-        d = __ull2double_rn(mant);
-        // scale by 2^(sh + ebase - 1075): the result is normal and finite
-        // for admitted columns, so adding to the exponent field is exact
-        d = __longlong_as_double(__double_as_longlong(d) + ((long long)(sh + ebase - 1075) << 52));
+        m += (rnd && (sticky || (m & 1))) ? 1 : 0;  // may carry into 2^53: the exponent field absorbs it
+        bits = ((uint64_t)(e - 1) << 52) + m;
     }
-    return neg ? -d : d;
+    return __longlong_as_double((long long)(bits | (neg ? (1ull << 63) : 0ull)));
 }
 
 // The exact sum of row r's words, rounded (x_round); clears the words.
@@ -359,6 +368,7 @@ struct XSeg {
 
 constexpr int kXTMax = 256;                   // row tiles of a bucketed column (rows <= 256 * kXRows)
 constexpr int kXRange = 4096;                 // products of one sorted range visit
+constexpr int kXDense = 512;                  // a tile with more products is a dense visit
 constexpr int64_t kXScap = int64_t(1) << 18;  // bucketed segments of one column (per-block scratch)
 
 // Numeric pass for the columns of the big list, one block per column
@@ -399,6 +409,7 @@ __global__ void __launch_bounds__(NT, 2)
     uint32_t *rwh = reinterpret_cast<uint32_t *>(rval + kXRange);    // [NW][128] digit counts per warp
     static_assert(2 * kXRange * 4 + kXRange * 8 + NW * 128 * 4 <= kXW * RS * 4, "range area inside the words");
     __shared__ ChunkSmemN<NT> ch;
+    static_assert(sizeof(ChunkSmemN<NT>) >= NW * 128 * 2, "write-out row lists fit the chunk table");
     __shared__ uint32_t ch_e[NT];
     __shared__ int32_t s_segcnt[kXTMax], s_prodcnt[kXTMax], s_off[kXTMax + 1];
     __shared__ int32_t s_wsum[NW];
@@ -500,15 +511,38 @@ __global__ void __launch_bounds__(NT, 2)
 
         // dense visit helpers: products of a chunk into the word accumulator,
         // and the write-out of tile row0's touched rows
+        // (the loads of the next 32-product window are issued before the
+        // current window's atomics, so their latency overlaps them)
         auto dense_products = [&](int L, int nseg, int row0) {
-            for_products(L, nseg, [&](int b, int64_t idx, int) {
-                const int r = a.arow[idx] - row0;
-                const double av = aval ? aval[idx] : 1.0;
-                const double bv = bval ? bval[bs + ch_e[b]] : 1.0;
-                if (!x_add(acc, RS, tw, r, (uint64_t)__double_as_longlong(av), (uint64_t)__double_as_longlong(bv),
-                           ebase))
-                    bad = true;
-            });
+            const int span = (((L + NW - 1) / NW) + 31) & ~31;
+            const int wb = warp * span, we = min(L, wb + span);
+            if (wb >= we) return;
+            int bcur = chunk_find_nz(ch, nseg, wb);
+            int r_n = 0;
+            uint64_t a_n = 0, b_n = 0;
+            bool v_n = false;
+            auto load = [&](int p0) {
+                const int p = p0 + lane;
+                const int b = window_seg(ch, nseg, bcur, p);
+                v_n = p < we;
+                if (v_n) {
+                    const int64_t idx = (uint32_t)(ch.base[b] + (uint32_t)p);
+                    r_n = a.arow[idx] - row0;
+                    a_n = (uint64_t)__double_as_longlong(aval ? aval[idx] : 1.0);
+                    b_n = (uint64_t)__double_as_longlong(bval ? bval[bs + ch_e[b]] : 1.0);
+                }
+                int bn = __shfl_sync(0xffffffffu, b, 31);
+                if (bn + 1 < nseg && ch.off[bn + 1] <= p0 + 32) ++bn;
+                bcur = bn;
+            };
+            load(wb);
+            for (int p0 = wb; p0 < we; p0 += 32) {
+                const int r = r_n;
+                const uint64_t av = a_n, bv = b_n;
+                const bool v = v_n;
+                if (p0 + 32 < we) load(p0 + 32);  // warp-uniform
+                if (v && !x_add(acc, RS, tw, r, av, bv, ebase)) bad = true;
+            }
         };
         auto dense_writeout = [&](int row0) {
             __syncthreads();
@@ -519,15 +553,27 @@ __global__ void __launch_bounds__(NT, 2)
             for (int gg = g0; gg < g1; ++gg) cnt += __popc(__ballot_sync(0xffffffffu, tfb[gg * 32 + lane] != 0));
             int tot;
             const int before = __shfl_sync(0xffffffffu, block_prefix(lane == 0 ? cnt : 0, &tot), 0);
+            XPROF_LAP(16);
+            XPROF_ADD(18, tot);
             int64_t pos = out + before;
-            for (int gg = g0; gg < g1; ++gg) {
-                const int r = gg * 32 + lane;
-                const uint32_t f = tfb[r];
-                const unsigned m = __ballot_sync(0xffffffffu, f != 0);
-                if (f) {
-                    const int64_t q = pos + __popc(m & lt);
-                    const double v = x_value(acc, RS, r, f, ebase);
+            // touched rows of 4 groups at a time listed in order (the chunk
+            // table's space, 128 rows per warp), then converted one per lane
+            uint16_t *wl = reinterpret_cast<uint16_t *>(&ch) + warp * 128;
+            for (int gb = g0; gb < g1; gb += 4) {
+                int n = 0;
+                for (int gg = gb; gg < min(g1, gb + 4); ++gg) {
+                    const int r = gg * 32 + lane;
+                    const bool f = tfb[r] != 0;
+                    const unsigned m = __ballot_sync(0xffffffffu, f);
+                    if (f) wl[n + __popc(m & lt)] = (uint16_t)r;
+                    n += __popc(m);
+                }
+                __syncwarp();
+                for (int k = lane; k < n; k += 32) {
+                    const int r = wl[k];
+                    const double v = x_value(acc, RS, r, tfb[r], ebase);
                     tfb[r] = 0;
+                    const int64_t q = pos + k;
                     if (q < lim) {
                         cir[q] = (int64_t)row0 + r;
                         cval[q] = v;
@@ -535,9 +581,11 @@ __global__ void __launch_bounds__(NT, 2)
                         over = true;
                     }
                 }
-                pos += __popc(m);
+                pos += n;
+                __syncwarp();
             }
             out += tot;
+            XPROF_LAP(17);
             __syncthreads();
         };
         auto clean_words = [&]() {
@@ -611,7 +659,7 @@ __global__ void __launch_bounds__(NT, 2)
                     ++t;
                     continue;
                 }
-                if (s_prodcnt[t] > kXRange) {
+                if (s_prodcnt[t] > kXDense) {
                     // dense visit of tile t
                     clean_words();
                     const int row0 = t * a.R;
@@ -646,9 +694,10 @@ __global__ void __launch_bounds__(NT, 2)
                     XPROF_ADD(8, 1);
                     ++t;
                 } else {
-                    // range visit of tiles t .. t1 (at most kXRange products)
+                    // range visit of light tiles t .. t1 (at most kXRange products)
                     int t1 = t, prods = s_prodcnt[t];
-                    while (t1 + 1 < a.T && (s_segcnt[t1 + 1] == 0 || prods + s_prodcnt[t1 + 1] <= kXRange)) {
+                    while (t1 + 1 < a.T && (s_segcnt[t1 + 1] == 0 ||
+                                            (s_prodcnt[t1 + 1] <= kXDense && prods + s_prodcnt[t1 + 1] <= kXRange))) {
                         ++t1;
                         prods += s_prodcnt[t1];
                     }
@@ -741,29 +790,40 @@ __global__ void __launch_bounds__(NT, 2)
                         dst = tmp;
                     }
                     XPROF_LAP(5);
-                    // runs of one row: the head sums its run exactly and writes it
-                    for (int u0 = 0; u0 < prods; u0 += NT) {
-                        const int u = u0 + tid;
-                        const uint32_t key = u < prods ? src[u] : 0u;
-                        const bool head = u < prods && (u == 0 || (src[u - 1] >> 12) != (key >> 12));
+                    // runs of one row: thread tid owns the sorted keys [8 tid,
+                    // 8 tid + 8); it sums (exactly) and writes every run whose
+                    // first key it owns, reading past its own keys to finish
+                    // its last run.  Output positions: one block prefix of the
+                    // runs started per thread.
+                    {
+                        const int k0t = 8 * tid, k1t = min(prods, k0t + 8);
+                        int heads = 0;
+                        for (int u = k0t; u < k1t; ++u)
+                            heads += (u == 0 || (src[u - 1] >> 12) != (src[u] >> 12)) ? 1 : 0;
                         int tot;
-                        const int before = block_prefix(head ? 1 : 0, &tot);
-                        if (head) {
+                        int64_t q = out + block_prefix(heads, &tot);
+                        int u = k0t;
+                        // keys continuing a run that an earlier thread started
+                        while (u < k1t && u > 0 && (src[u - 1] >> 12) == (src[u] >> 12)) ++u;
+                        while (u < k1t) {
+                            const uint32_t row = src[u] >> 12;
                             uint64_t hi = 0, lo = 0;
                             uint32_t fl = 0;
-                            for (int q = u; q < prods; ++q) {
-                                const uint32_t kq = src[q];
-                                if ((kq >> 12) != (key >> 12)) break;
-                                if (!x_acc128(hi, lo, fl, __longlong_as_double((long long)rval[kq & 4095]), ebase))
+                            int v = u;
+                            for (; v < prods; ++v) {
+                                const uint32_t kv = src[v];
+                                if ((kv >> 12) != row) break;
+                                if (!x_acc128(hi, lo, fl, __longlong_as_double((long long)rval[kv & 4095]), ebase))
                                     bad = true;
                             }
-                            const int64_t q = out + before;
                             if (q < lim) {
-                                cir[q] = (int64_t)rbase + (int64_t)(key >> 12);
+                                cir[q] = (int64_t)rbase + (int64_t)row;
                                 cval[q] = x_round(hi, lo, fl, ebase);
                             } else {
                                 over = true;
                             }
+                            ++q;
+                            u = v;
                         }
                         out += tot;
                     }
