@@ -1143,8 +1143,8 @@ static int plan_finalize(Workspace &ws, Plan &P)
         GBC_TRY(ws.alloc_n(&P.fb_cnt, 1));
         // bucketing scratch of the exact kernel: kXScap segments per resident block
         const size_t smem = (size_t)kXW * kXRows * 4 + kXRows;
-        GBC_TRY(set_smem(k_numeric_x<kXThreads>, smem));
-        P.x_blocks = ws.ctx->num_sms * resident_blocks(k_numeric_x<kXThreads>, kXThreads, smem, 2);
+        GBC_TRY(set_smem(k_numeric_x<kXThreads, kXRows>, smem));
+        P.x_blocks = ws.ctx->num_sms * resident_blocks(k_numeric_x<kXThreads, kXRows>, kXThreads, smem, 2);
         GBC_TRY(ws.alloc_n(&P.xscratch, (size_t)P.x_blocks * kXScap));
     }
     GBC_CUDA_TRY(cudaMemcpyAsync(P.d, P.h.data(), P.h.size() * sizeof(SpgemmArgs), cudaMemcpyHostToDevice,
@@ -1305,7 +1305,7 @@ static int launch_big_exact(Context *ctx, Plan &P, const Lists &L, const int64_t
     const int grid = (int)std::min<int64_t>(P.x_blocks, L.n[2]);  // the scratch holds P.x_blocks blocks
     GBC_CUDA_TRY(cudaMemsetAsync(P.work + 1, 0, 2 * sizeof(unsigned long long), s));
     GBC_CUDA_TRY(cudaMemsetAsync(P.fb_cnt, 0, sizeof(unsigned long long), s));
-    k_numeric_x<NT><<<grid, NT, smem, s>>>(P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir,
+    k_numeric_x<NT, kXRows><<<grid, NT, smem, s>>>(P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir,
                                            static_cast<double *>(cval), P.work + 1, P.fb_items, P.fb_cnt,
                                            P.xscratch);
     note_launch();

@@ -42,7 +42,10 @@ constexpr int kXW = 6;                       // words per row
 constexpr uint32_t kXMask = (1u << kXP) - 1;
 constexpr int kXOMax = kXP * kXW - 53;       // largest product exponent above the base (61)
 constexpr int kXNorm = 2047;                 // B entries between carry normalisations
-constexpr int kXRows = 4096;                 // rows of one accumulator tile
+// Accumulator tile and block shape of k_numeric_x: kXRows rows (24 B of
+// words + 1 flag byte each) in shared memory, kXThreads threads, two blocks
+// per SM.
+constexpr int kXRows = 4096;
 constexpr int kXThreads = 512;
 
 // Phase clocks of k_numeric_x for profiling builds (-DGBC_XPROF): thread 0
@@ -145,18 +148,19 @@ __device__ __forceinline__ uint64_t x_mul_bits(uint64_t abits, uint64_t bbits)
 // zero or normal, product normal) to row r of the accumulator (words at
 // acc[i * stride + r]) and mark the row touched in its flag byte (bit 0
 // touched, bit 1 touched by something other than -0.0, which decides the
-// sign of an exact zero sum).  Returns false when the product lies outside
+// sign of an exact zero sum); a row's first touch counts it in band[r / 256]
+// (touched rows per 256-row band, the write-out's offsets).  Returns false when the product lies outside
 // the column's admitted exponent window (cannot happen for admitted
 // columns; nothing is added then).
-__device__ __forceinline__ bool x_add(int32_t *acc, int stride, uint32_t *tw, int r, uint64_t abits, uint64_t bbits,
-                                      int ebase)
+__device__ __forceinline__ bool x_add(int32_t *acc, int stride, uint32_t *tw, int32_t *band, int r, uint64_t abits,
+                                      uint64_t bbits, int ebase)
 {
     const bool neg = ((abits ^ bbits) >> 63) != 0;
-    if ((abits << 1) == 0 || (bbits << 1) == 0) {  // a zero product: +0.0 or -0.0
-        atomicOr(&tw[r >> 2], (neg ? 1u : 3u) << ((r & 3) << 3));
-        return true;
-    }
-    atomicOr(&tw[r >> 2], 3u << ((r & 3) << 3));
+    const int sh8 = (r & 3) << 3;
+    const bool zero = (abits << 1) == 0 || (bbits << 1) == 0;  // a zero product: +0.0 or -0.0
+    const uint32_t old = atomicOr(&tw[r >> 2], ((zero && neg) ? 1u : 3u) << sh8);
+    if (((old >> sh8) & 0xff) == 0) atomicAdd(&band[r >> 8], 1);  // first touch: count the row in its band
+    if (zero) return true;
     uint64_t m;
     int ex;
     x_mul(abits, bbits, m, ex);
@@ -389,15 +393,16 @@ constexpr int64_t kXScap = int64_t(1) << 18;  // bucketed segments of one column
 // kXTMax tiles, visit every touched tile and look up their B entries' A
 // segments per tile (tptr) instead of step 1.  Columns outside the exact
 // window are appended to fb_items for the ordered kernel.
-template <int NT>
+template <int NT, int RS>
 __global__ void __launch_bounds__(NT, 2)
     k_numeric_x(const SpgemmArgs *args, const int64_t *items, int64_t nitems, const int64_t *ccp, int64_t ccp_base,
                 const int64_t *cap, int64_t *out_cnt, int32_t *overflow, int64_t *cir, double *cval,
                 unsigned long long *work, int64_t *fb_items, unsigned long long *fb_count, XSeg *scratch_all)
 {
-    constexpr int NW = NT / 32;
-    constexpr int RS = kXRows;  // word stride
-    static_assert(kXRange == 4096 && NT == 512, "range keys carry a 12-bit slot; two blocks per SM");
+    constexpr int NW = NT / 32;  // RS: rows of the tile = word stride
+    static_assert(kXRange == 4096 && NT * 8 >= kXRange && (NW * 128) % NT == 0 && RS % (32 * NW) == 0 &&
+                      kXTMax * RS <= (1 << 20),
+                  "range keys: 20-bit row offset and 12-bit slot; eight sorted keys per thread");
     extern __shared__ __align__(16) int32_t xsm[];
     int32_t *acc = xsm;                                           // [kXW][RS]
     uint32_t *tw = reinterpret_cast<uint32_t *>(xsm + kXW * RS);  // [RS/4] flag bytes
@@ -413,6 +418,7 @@ __global__ void __launch_bounds__(NT, 2)
     __shared__ uint32_t ch_e[NT];
     __shared__ int32_t s_segcnt[kXTMax], s_prodcnt[kXTMax], s_off[kXTMax + 1];
     __shared__ int32_t s_wsum[NW];
+    __shared__ int32_t s_band[RS / 256];  // touched rows per 256-row band of the dense tile
     __shared__ int32_t s_emin[NW], s_emax[NW];
     __shared__ int64_t s_col;
     __shared__ SpgemmArgs sa;
@@ -420,6 +426,7 @@ __global__ void __launch_bounds__(NT, 2)
     const unsigned lt = (1u << lane) - 1;
     XSeg *scratch = scratch_all + (int64_t)blockIdx.x * kXScap;
     for (int u = tid; u < kXW * RS + RS / 4; u += NT) xsm[u] = 0;
+    for (int u = tid; u < RS / 256; u += NT) s_band[u] = 0;
     bool dirty = false;  // the word area holds a range visit's data
     bool first_item = true;
     XPROF_T0;
@@ -541,21 +548,31 @@ __global__ void __launch_bounds__(NT, 2)
                 const uint64_t av = a_n, bv = b_n;
                 const bool v = v_n;
                 if (p0 + 32 < we) load(p0 + 32);  // warp-uniform
-                if (v && !x_add(acc, RS, tw, r, av, bv, ebase)) bad = true;
+                if (v && !x_add(acc, RS, tw, s_band, r, av, bv, ebase)) bad = true;
             }
         };
+        // (callers end the products with a block barrier)
         auto dense_writeout = [&](int row0) {
-            __syncthreads();
-            const int ngroups = a.R >> 5;
-            const int gpw = (ngroups + NW - 1) / NW;
-            const int g0 = min(ngroups, warp * gpw), g1 = min(ngroups, g0 + gpw);
-            int cnt = 0;
-            for (int gg = g0; gg < g1; ++gg) cnt += __popc(__ballot_sync(0xffffffffu, tfb[gg * 32 + lane] != 0));
-            int tot;
-            const int before = __shfl_sync(0xffffffffu, block_prefix(lane == 0 ? cnt : 0, &tot), 0);
+            // warp w writes the rows of 256-row bands w, w + NW, ... in order;
+            // offsets from the bands' first-touch counts
+            static_assert(RS / 256 <= 32, "bands fit one warp");
+            const int nband = (a.R + 255) >> 8;
+            const int bc = lane < nband ? s_band[lane] : 0;
+            int inc = bc;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += y;
+            }
+            const int tot = __shfl_sync(0xffffffffu, inc, 31);
+            __syncthreads();  // every warp has read the band counts before they are reset
             XPROF_LAP(16);
             XPROF_ADD(18, tot);
-            int64_t pos = out + before;
+            for (int bd = warp; bd < nband; bd += NW) {
+                const int before = __shfl_sync(0xffffffffu, inc - bc, bd);
+                if (lane == 0) s_band[bd] = 0;
+                const int g0 = bd * 8, g1 = min(a.R >> 5, g0 + 8);
+                int64_t pos = out + before;
             // touched rows of 4 groups at a time listed in order (the chunk
             // table's space, 128 rows per warp), then converted one per lane
             uint16_t *wl = reinterpret_cast<uint16_t *>(&ch) + warp * 128;
@@ -583,6 +600,7 @@ __global__ void __launch_bounds__(NT, 2)
                 }
                 pos += n;
                 __syncwarp();
+            }
             }
             out += tot;
             XPROF_LAP(17);
@@ -872,6 +890,7 @@ __global__ void __launch_bounds__(NT, 2)
                     const int L = compact_chunk<uint32_t, NT>(ch, s0, len, (uint32_t)(e - bs), ch_e, nseg);
                     dense_products(L, nseg, row0);
                 }
+                __syncthreads();
                 dense_writeout(row0);
                 XPROF_LAP(7);
                 XPROF_ADD(10, 1);
