@@ -13,6 +13,15 @@ the reference's estimateFLOP counts them, divided by time).  The line also
 carries BFS GTEPS on the same graph (64 seeded roots, SelectMin parents) and
 the MCL expansion step (n = 2^20, fp32) exact vs learned.
 
+The default run also measures every other configuration in the same line
+(``configs``): C1 (R-MAT s14 A*A), C2 (BFS s20, top-down and
+direction-optimizing), C3 (MCL expansion n = 2^20), C4 (the 256-problem
+uneven batch) and C5 (multi-source BFS s22, 512 roots), each with its own
+roofline, CPU baseline, end-to-end figure and a parity check against the
+oracle; ``parity`` collects them together with the headline's own check
+(the s20 product on a 4096-column sample, bit-exact under both folds).
+``--headline-only`` skips them.
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--workload spgemm20|bfs20|spgemm14] [--scale S] [--no-mcl] [--no-cpu]
 
@@ -646,6 +655,8 @@ def bench_batch(args, world, ctx, stream, hbm, peak_kind):
     groups.append(cur)
     ng = len(rm)
 
+    nnz_second = [0] * len(gk)
+
     def batched(inputs=None, R_in=None, read_back=False):
         inputs = inputs or first
         flops, d2h = 0, 0
@@ -661,6 +672,7 @@ def bench_batch(args, world, ctx, stream, hbm, peak_kind):
             b.close()
         b2 = BT.Batch(R_in or Rs, [ars[q] for q in range(len(gk))], ctx=ctx)
         flops += b2.flops()
+        nnz_second[:] = [int(b2.info(q)[1]) for q in range(len(gk))]
         if read_back:
             d2h += sum(b2.column_pointers(q).nbytes for q in range(len(gk)))
         b2.close()
@@ -712,6 +724,14 @@ def bench_batch(args, world, ctx, stream, hbm, peak_kind):
     e2e_s = max_over_ranks(time.perf_counter() - t0, world, "cuda")
     h2d = sum(M.colptr.nbytes + M.rowidx.nbytes + M.values.nbytes for pair in first_host for M in pair) + \
         sum(M.colptr.nbytes + M.rowidx.nbytes + M.values.nbytes for M in Rs_host)
+    # algorithmic bytes of one step: every product reads its operands once and
+    # writes its output (16 B per entry + column pointers)
+    csc_bytes = lambda M: M.colptr.nbytes + M.rowidx.nbytes + M.values.nbytes
+    ba = sum(csc_bytes(a) + csc_bytes(b) + 16 * nz + 8 * (b.ncol + 1) for (a, b), nz in zip(first_host, nnz_first))
+    ba += sum(csc_bytes(R) + 16 * nz_ar + 8 * (dims[q][1] + 1) + 16 * nz2 + 8 * (dims[q][1] + 1)
+              for q, (R, nz_ar, nz2) in enumerate(zip(Rs_host, nnz_first[ng:], nnz_second)))
+    achieved = ba / (ms / args.steps * 1e-3) / 1e9
+    result_sets = (rm, gk)
     return {
         "e2e": {"value": flops * args.steps * world / e2e_s / 1e9, "unit": "Gmults/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
@@ -722,10 +742,267 @@ def bench_batch(args, world, ctx, stream, hbm, peak_kind):
         "batch": {"problems": 256, "groups": len(groups), "budget_nnz": budget, "flops": flops,
                   "one_by_one_gmults": flops * args.steps / (ms_1 * 1e-3) / 1e9,
                   "one_by_one_ms_per_step": ms_1 / args.steps, "batched_speedup": ms_1 / ms},
-        "roofline": {"bound": "hbm", "kernel": "k_numeric", "achieved": None, "peak": hbm, "peak_kind": peak_kind,
-                     "unit": "GB/s", "frac": None, "traffic": None,
-                     "note": "per-kernel figures for this workload are not derived"},
+        "roofline": {"bound": "hbm", "kernel": "whole batched step (every pass of every product)",
+                     "achieved": achieved, "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": achieved / hbm, "algorithmic_bytes": ba, "traffic": None,
+                     "note": "operands read once and outputs written once per product (16 B per entry)"},
+        "_problems": result_sets,
     }
+
+
+# ------------------------------------------- every configuration, one line
+def _timed(stream, fn, reps):
+    """Device time of `reps` calls of fn (CUDA events on `stream`), ms per call."""
+    import torch
+
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def _same(a, b):
+    """Bit-exact equality of (colptr, rows, values) triples."""
+    return all(np.array_equal(np.asarray(x).view(np.int64) if np.asarray(x).dtype == np.float64 else x,
+                              np.asarray(y).view(np.int64) if np.asarray(y).dtype == np.float64 else y)
+               for x, y in zip(a, b))
+
+
+def parity_spgemm_sample(A, Ad, ctx, ncols=4096):
+    """The scale-20 product on a seeded sample of B columns (the full row
+    range) against the oracle, under both folds: bit-exact."""
+    import oracle as O
+    from combblas_gb300 import local as LC
+
+    Bh, cols = column_sample(A, ncols / A.ncol, seed=11)
+    Bd = LC.DeviceMatrix.from_host(Bh)
+    out = {"columns": len(cols), "check": "bit-exact (pattern and value bits) against oracle/oracle.c"}
+    for fold in ("exact", "ordered"):
+        R = LC.spgemm(Ad, Bd, ctx=ctx, fold=fold)
+        got = R.to_csc()
+        R.free()
+        (pcp, prow, pval), (flop, _) = O.port_spgemm(A, Bh, O.SR_PLUSTIMES_F64, fold=fold, want_counts=True)
+        out[f"{fold}_fold"] = bool(_same(got, (pcp, prow, pval)))
+        out["mults"] = int(flop.sum())
+        out["entries"] = int(len(prow))
+        if fold == "exact":
+            xv = pval
+        else:
+            out["max_rel_exact_vs_hash_order"] = float(np.max(np.abs(xv - pval) / np.abs(pval))) if len(pval) else 0.0
+    out["ok"] = out["exact_fold"] and out["ordered_fold"]
+    return out
+
+
+def bench_c1(args, ctx, stream, hbm, peak_kind):
+    """C1: C = A*A on the scale-14 R-MAT (ef 8), PlusTimes fp64, exact
+    two-phase, device-resident inputs; the whole product is checked."""
+    import torch
+    import oracle as O
+    from combblas_gb300 import generators as G
+    from combblas_gb300 import local as LC
+
+    A = G.rmat(14, 8, seed=SEED)
+    Ad = LC.DeviceMatrix.from_host(A)
+    reps = max(args.steps, 5)
+    for _ in range(3):
+        LC.spgemm(Ad, Ad, ctx=ctx).free()
+    st = {}
+
+    def one():
+        R = LC.spgemm(Ad, Ad, ctx=ctx)
+        st["s"] = R.stats
+        R.free()
+
+    ms = _timed(stream, one, reps)
+    s0 = st["s"]
+    got = LC.spgemm(Ad, Ad, ctx=ctx).to_csc()
+    t0 = time.perf_counter()
+    (pcp, prow, pval), (flop, _) = O.port_spgemm(A, A, O.SR_PLUSTIMES_F64, want_counts=True)
+    cpu_s = time.perf_counter() - t0
+    exact_ok = _same(got, O.port_spgemm(A, A, O.SR_PLUSTIMES_F64, fold="exact"))
+    ordered_ok = _same(LC.spgemm(Ad, Ad, ctx=ctx, fold="ordered").to_csc(), (pcp, prow, pval))
+    ba = bytes_alg(A.nnz, A.ncol, s0.nnz)
+    # e2e: host CSC in (pinned), the whole product read back
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    Ah = G.CSC(A.nrow, A.ncol, pin(A.colptr), pin(A.rowidx), pin(A.values))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        R = LC.spgemm(Ah, Ah, ctx=ctx)
+        R.to_csc()
+        R.free()
+    e2e_s = (time.perf_counter() - t0) / reps
+    return {
+        "workload": "R-MAT s14 ef8 A*A, PlusTimes fp64 (exact fold), exact two-phase, inputs resident",
+        "value": s0.flops / (ms * 1e-3) / 1e9, "unit": "Gmults/s", "ms_per_step": ms, "flops": s0.flops,
+        "nnz_c": s0.nnz, "ms_symbolic": s0.ms_symbolic, "ms_numeric": s0.ms_numeric,
+        "roofline": {"bound": "hbm", "kernel": "whole product (symbolic + numeric kernels)",
+                     "achieved": ba / (ms * 1e-3) / 1e9, "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": ba / (ms * 1e-3) / 1e9 / hbm, "algorithmic_bytes": ba, "traffic": None},
+        "cpu_baseline": {"value": int(flop.sum()) / cpu_s / 1e9, "unit": "Gmults/s", "cores": O.port_num_threads(),
+                         "kind": "port", "sample": "the whole product (oracle/oracle.c, the reference's hash path)"},
+        "e2e": {"value": s0.flops / e2e_s / 1e9, "unit": "Gmults/s",
+                "h2d_bytes_per_step": int(2 * (A.colptr.nbytes + A.rowidx.nbytes + A.values.nbytes)),
+                "d2h_bytes_per_step": int(s0.nnz * 16 + (A.ncol + 1) * 8),
+                "path": "gbc_spgemm with pinned host CSC inputs, the product copied back to the host"},
+        "parity": {"ok": bool(exact_ok and ordered_ok), "exact_fold_vs_oracle": bool(exact_ok),
+                   "ordered_fold_vs_oracle": bool(ordered_ok), "check": "whole product, bit-exact"},
+    }
+
+
+def bench_c2(args, A, ctx, stream, hbm, peak_kind, world):
+    """C2: BFS on the scale-20 R-MAT from 64 seeded roots, top-down only
+    (the configuration's algorithm) and direction-optimizing; parents and
+    levels of 4 roots checked against the oracle."""
+    import torch
+    import oracle as O
+    from combblas_gb300 import _lib
+    from combblas_gb300 import bfs as B
+
+    P = A.with_values(None)
+    g = B.Graph(P, ctx)
+    par = torch.empty(A.ncol, dtype=torch.int64, device="cuda")
+    lev = torch.empty(A.ncol, dtype=torch.int64, device="cuda")
+    roots = bfs_roots(A)
+    res = {}
+    for policy in ("topdown", "auto"):
+        g.set_policy(policy)
+        for r in roots[:3]:
+            B.bfs_device(g, int(r), par.data_ptr(), lev.data_ptr())
+        edges = [0]
+        l0 = _lib.lib().gbc_launch_count()
+
+        def run():
+            for r in roots:
+                edges[0] += B.bfs_device(g, int(r), par.data_ptr(), lev.data_ptr()).edges
+
+        ms = _timed(stream, run, 1)
+        res[policy] = {"gteps": edges[0] / (ms * 1e-3) / 1e9, "ms_64_roots": ms, "edges": edges[0],
+                       "gpu_launches": _lib.lib().gbc_launch_count() - l0}
+    g.set_policy("topdown")
+    ok = True
+    for r in roots[:4]:
+        p1, l1, _ = B.bfs(g, int(r))
+        p2, l2, _ = O.port_bfs(P, int(r))
+        ok = ok and np.array_equal(p1, p2) and np.array_equal(l1, l2)
+    g.close()
+    t0 = time.perf_counter()
+    e_edges = 0
+    for r in roots[:8]:
+        _, _, st_h = B.bfs(P, int(r), ctx=ctx)
+        e_edges += st_h.edges
+    e2e_s = time.perf_counter() - t0
+    v, desc, th = cpu_bfs_rate(A, roots[:8], 10.0)
+    td = res["topdown"]
+    bytes_td = td["edges"] * 2 * 4 + len(roots) * A.ncol * 16
+    return {
+        "workload": "BFS R-MAT s20 ef16, 64 roots, SelectMin parents; value = top-down only",
+        "value": td["gteps"] * world, "unit": "GTEPS", "topdown": td, "direction_optimizing": res["auto"],
+        "roofline": {"bound": "hbm", "kernel": "k_bfs_td (top-down levels)", "achieved": bytes_td / (td["ms_64_roots"] * 1e-3) / 1e9,
+                     "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": bytes_td / (td["ms_64_roots"] * 1e-3) / 1e9 / hbm, "traffic": None,
+                     "algorithmic_bytes": bytes_td,
+                     "note": "4 B per scanned edge (each undirected edge scanned twice) + 16 B parent/level per vertex"},
+        "cpu_baseline": {"value": v, "unit": "GTEPS", "cores": th, "kind": "port", "sample": desc},
+        "e2e": {"value": e_edges / e2e_s / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": int(A.colptr.nbytes + A.rowidx.nbytes),
+                "d2h_bytes_per_step": 2 * A.ncol * 8, "path": "gbc_bfs from host CSC, parents and levels to host, 8 roots"},
+        "parity": {"ok": bool(ok), "roots": 4, "check": "parents and levels bit-exact against the oracle's BFS"},
+    }
+
+
+def bench_c3(ctx, hbm, peak_kind):
+    """C3: MCL expansion step (n = 2^20 planted clusters, fp32): exact vs
+    learned sizing (bench_mcl), plus roofline, CPU baseline, e2e and the
+    whole selected product against the oracle."""
+    import torch
+    import oracle as O
+    from combblas_gb300 import generators as G
+    from combblas_gb300 import mcl as MCL
+
+    out = bench_mcl(ctx)
+    n = 1 << 20
+    A = G.mcl_planted(n, 1024, 24.0, 6.0, seed=3)
+    R, st = MCL.mcl_expand(A, 1e-4, 100, ctx=ctx)
+    got = R.to_csc()
+    R.free()
+    t0 = time.perf_counter()
+    (pcp, prow, pval), (flop, _) = O.port_spgemm(A, A, O.SR_PLUSTIMES_F32, sorted=False, want_counts=True)
+    scp, srow, sval = O.port_mcl_select(pcp, prow, pval, 1e-4, 100)
+    cpu_s = time.perf_counter() - t0
+    exp = O.canonical_csc(scp, srow, sval)
+    ok = all(np.array_equal(x, y) for x, y in zip(got, exp))
+    # e2e: the host matrix in, the selected product back
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reps = 3
+    for _ in range(reps):
+        R, st_e = MCL.mcl_expand(A, 1e-4, 100, ctx=ctx)
+        R.to_csc()
+        R.free()
+    e2e_s = (time.perf_counter() - t0) / reps
+    ex = out["exact"]
+    nnz_sel = len(exp[1])
+    ba = 2 * (A.nnz * 12 + (n + 1) * 8) + ex["nnz_c"] * 12 + ex["nnz_c"] * 12 + nnz_sel * 12
+    out.update({
+        "value": ex["gmults_per_s"], "unit": "Gmults/s",
+        "roofline": {"bound": "hbm", "kernel": "expansion + prune/select (whole step, exact sizing)",
+                     "achieved": ba / (ex["ms"] * 1e-3) / 1e9, "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": ba / (ex["ms"] * 1e-3) / 1e9 / hbm, "algorithmic_bytes": ba, "traffic": None,
+                     "note": "A read twice, C written and read once, selected entries written (12 B per entry)"},
+        "cpu_baseline": {"value": int(flop.sum()) / cpu_s / 1e9, "unit": "Gmults/s", "cores": O.port_num_threads(),
+                         "kind": "port", "sample": "the whole step (hash-path product + MCLPruneRecoverySelect restatement)"},
+        "e2e": {"value": st_e.flops / e2e_s / 1e9, "unit": "Gmults/s",
+                "h2d_bytes_per_step": int(A.colptr.nbytes + A.rowidx.nbytes + A.values.nbytes),
+                "d2h_bytes_per_step": int(nnz_sel * 12 + (n + 1) * 8),
+                "path": "gbc_mcl_expand_f32 from host CSC, the selected product copied back"},
+        "parity": {"ok": bool(ok), "check": "the whole selected product bit-exact against the oracle "
+                                            "(PlusTimes fp32 product in hash order + prune/select)"},
+    })
+    return out
+
+
+def parity_batch(rm, gk, ctx, nprob=16):
+    """16 of the 256 batch problems (the first R-MAT and Galerkin ones by a
+    seeded choice) through a batch, against the oracle's exact fold."""
+    import oracle as O
+    from combblas_gb300 import batch as BT
+
+    rng = np.random.default_rng(SEED + 300)
+    pick_r = sorted(rng.choice(len(rm), nprob // 2, replace=False).tolist())
+    pick_g = sorted(rng.choice(len(gk), nprob // 2, replace=False).tolist())
+    As = [rm[p] for p in pick_r] + [gk[q][0] for q in pick_g]
+    Bs = [rm[p] for p in pick_r] + [gk[q][2] for q in pick_g]
+    b = BT.Batch(As, Bs, ctx=ctx)
+    ok = True
+    for i, (A, B) in enumerate(zip(As, Bs)):
+        ok = ok and _same(b.result(i), O.port_spgemm(A, B, O.SR_PLUSTIMES_F64, fold="exact"))
+    b.close()
+    return {"ok": bool(ok), "problems": nprob, "check": "first-stage products through one batch, bit-exact "
+                                                        "against the oracle's exact fold"}
+
+
+def parity_msbfs(A, ctx, roots):
+    """Parent rows of 2 roots of the multi-source traversal against the
+    oracle's single-source BFS (min-parent semantics)."""
+    import oracle as O
+    from combblas_gb300 import bfs as B
+
+    P = A.with_values(None)
+    g = B.Graph(P, ctx)
+    par, _ = B.msbfs(g, roots[:2])
+    g.close()
+    ok = True
+    for i in range(2):
+        p2, _, _ = O.port_bfs(P, int(roots[i]))
+        other = np.arange(A.ncol) != int(roots[i])
+        ok = ok and par[i][int(roots[i])] == int(roots[i]) and np.array_equal(np.asarray(par[i])[other], p2[other])
+    return {"ok": bool(ok), "roots": 2,
+            "check": "parent rows bit-exact against the oracle's single-source BFS (min parent); the root's own "
+                     "entry is the root (sources start visited in the multi-source loop)"}
 
 
 def result_to_torch(R):
@@ -764,9 +1041,10 @@ def run_ours(args, world, rank, local):
         torch.cuda.synchronize()
 
     # ---- SpGEMM, inputs resident in HBM -------------------------------
+    every = args.workload == "spgemm20" and not args.headline_only  # every configuration in this line
     if args.workload.startswith("spgemm"):
         result.update(bench_spgemm(args, world, A, Ad, ctx, stream, scale, ef, hbm, peak_kind))
-        if not args.no_mcl and world >= 1:
+        if not args.no_mcl and world >= 1 and not every:
             result["mcl"] = bench_mcl(ctx)
 
     if args.workload == "msbfs22":
@@ -777,7 +1055,7 @@ def run_ours(args, world, rank, local):
         result["spmv"] = bench_spmv(A, ctx, stream, hbm, peak_kind)
 
     # ---- BFS: 64 roots, level loop as a replayed CUDA graph --------------
-    if args.workload == "bfs20" or (args.workload.startswith("spgemm") and not args.no_bfs):
+    if args.workload == "bfs20" or (args.workload.startswith("spgemm") and not args.no_bfs and not every):
         g = B.Graph(A.with_values(None), ctx)
         par = torch.empty(A.ncol, dtype=torch.int64, device="cuda")
         lev = torch.empty(A.ncol, dtype=torch.int64, device="cuda")
@@ -823,6 +1101,61 @@ def run_ours(args, world, rank, local):
             result["roofline"] = {"bound": "hbm", "kernel": "k_bfs_td + k_bfs_bu", "achieved": achieved, "peak": hbm,
                                   "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm, "traffic": None}
 
+    # ---- the other configurations, each with its own roofline, CPU
+    # baseline, e2e and parity check; parity of the headline on a column
+    # sample of the full-size product ------------------------------------
+    if every:
+        import types
+
+        import torch
+
+        sub = types.SimpleNamespace(**vars(args))
+        sub.steps, sub.warmup = min(args.steps, 3), 1
+        cfg = {}
+        parity = {"spgemm20_sample": parity_spgemm_sample(A, Ad, ctx)}
+        log("parity s20 sample:", parity["spgemm20_sample"])
+        cfg["C1_spgemm14"] = bench_c1(sub, ctx, stream, hbm, peak_kind)
+        cfg["C2_bfs20"] = bench_c2(sub, A, ctx, stream, hbm, peak_kind, world)
+        if not args.no_mcl:
+            cfg["C3_mcl20"] = bench_c3(ctx, hbm, peak_kind)
+        if not args.no_bfs:
+            spmv = bench_spmv(A, ctx, stream, hbm, peak_kind)
+            result["spmv"] = spmv
+        del Ad
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        # C4: the uneven batch
+        c4 = bench_batch(sub, world, ctx, stream, hbm, peak_kind)
+        rm4, gk4 = c4.pop("_problems")
+        v, desc, th = cpu_batch_rate(8.0)
+        c4 = {"workload": metric_name("batch256", 0, 0), "value": c4["value"], "unit": c4["unit"], "ms_per_step": c4["ms_per_step"],
+              "batch": c4["batch"], "roofline": c4["roofline"], "e2e": c4["e2e"], "gpu_launches": c4["gpu_launches"],
+              "cpu_baseline": {"value": v, "unit": "Gmults/s", "cores": th, "kind": "port", "sample": desc},
+              "parity": parity_batch(rm4, gk4, ctx)}
+        cfg["C4_batch256"] = c4
+        del rm4, gk4
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        # C5: multi-source BFS on scale 22
+        A22, s22, e22 = make_graph("msbfs22")
+        c5 = bench_msbfs(sub, world, A22, ctx, stream, hbm, peak_kind, s22, e22)
+        roots22 = np.random.default_rng(SEED + 200).choice(np.nonzero(np.diff(A22.colptr))[0], MS_ROOTS,
+                                                           replace=False)
+        v, desc, th = cpu_bfs_rate(A22, roots22[:2], 10.0)
+        cfg["C5_msbfs22"] = {"workload": metric_name("msbfs22", s22, e22), "value": c5["value"], "unit": "GTEPS",
+                             "ms_per_step": c5["ms_per_step"], "msbfs": c5["msbfs"], "roofline": c5["roofline"],
+                             "e2e": c5["e2e"], "gpu_launches": c5["gpu_launches"],
+                             "cpu_baseline": {"value": v, "unit": "GTEPS", "cores": th, "kind": "port",
+                                              "sample": desc + " (single-source BFS of the oracle; the multi-source "
+                                                               "loop does the same work per root)"},
+                             "parity": parity_msbfs(A22, ctx, roots22)}
+        del A22
+        for k, c in cfg.items():
+            parity[k] = c["parity"]["ok"]
+        parity["all_ok"] = bool(parity["spgemm20_sample"]["ok"] and all(c["parity"]["ok"] for c in cfg.values()))
+        result["configs"] = cfg
+        result["parity"] = parity
+
     # ---- CPU baseline (rank 0, N=1 only) -------------------------------
     if rank == 0 and world == 1 and not args.no_cpu:
         if args.workload == "batch256":
@@ -847,7 +1180,7 @@ def run_ours(args, world, rank, local):
         "config": workload_config(args, scale, ef, world),
     }
     for k in ("roofline", "cpu_baseline", "e2e", "gpu_launches", "clocks", "spgemm", "exact_two_phase", "mcl", "bfs",
-              "msbfs", "batch", "spmv"):
+              "msbfs", "batch", "spmv", "parity", "configs"):
         if k in result:
             line[k] = result[k]
     if rank == 0:
@@ -869,6 +1202,8 @@ def main():
     ap.add_argument("--scale", type=int, default=0, help="override the R-MAT scale (profiling runs)")
     ap.add_argument("--batch-budget-nnz", type=int, default=6 << 30,
                     help="batch256: output entries one batch group may hold")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="spgemm20: only the headline product (not the other configurations and parity checks)")
     ap.add_argument("--bcols", type=int, default=0,
                     help="profiling case: B = A(:, this many seeded random columns) instead of A")
     args = ap.parse_args()

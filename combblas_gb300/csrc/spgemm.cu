@@ -1472,7 +1472,7 @@ static int spgemm_exact(Context *ctx, const DevMatrix &A, const DevMatrix &B, co
 // ------------------------------------------------------- learned sizing
 // Per-column features of the sizing MLP: log2(1+x) of nnz(B(:,j)), flop,
 // the largest and the spread (standard deviation) of the referenced A
-// column lengths, the number of row tiles touched, and the row count.
+// column lengths, the number of 8192-row bands touched, and the row count.
 __global__ void k_features(SpgemmArgs a, int64_t nb, float *feat)
 {
     const int lane = threadIdx.x & 31;
@@ -1488,8 +1488,18 @@ __global__ void k_features(SpgemmArgs a, int64_t nb, float *feat)
             sq += len * len;
             mx = fmax(mx, len);
         }
+        // touched 8192-row bands, whatever the plan's tile height: groups
+        // of f = 8192 / R tile bits are OR-folded (R a power of two that
+        // divides 8192; other heights count their own tiles)
+        const int f = (a.R <= 8192 && (8192 % a.R) == 0 && (a.R & (a.R - 1)) == 0) ? 8192 / a.R : 1;
+        uint64_t keep = 0;  // bit 0 of every group of f
+        for (int b = 0; b < 64; b += f) keep |= 1ull << b;
         int tiles = 0;
-        for (int w = lane; w < a.mask_words; w += 32) tiles += __popcll(a.tmask[i * a.mask_words + w]);
+        for (int w = lane; w < a.mask_words; w += 32) {
+            uint64_t m = a.tmask[i * a.mask_words + w];
+            for (int sh = 1; sh < f; sh <<= 1) m |= m >> sh;
+            tiles += __popcll(m & keep);
+        }
 #pragma unroll
         for (int o = 16; o; o >>= 1) {
             sum += __shfl_xor_sync(0xffffffffu, sum, o);
