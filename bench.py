@@ -49,10 +49,10 @@ sys.path.insert(0, ROOT)
 
 SEED = 1
 BFS_ROOTS = 64
-# DRAM bytes of k_numeric measured by ncu on a scale-20 column sample
-# (profiles/k_numeric_s20_cols4096.txt), used to scale roofline.traffic
-NUMERIC_DRAM_READ_PER_MULT = 5.57
-NUMERIC_DRAM_WRITE_PER_ENTRY = 15.66
+# DRAM bytes of k_numeric_x measured by ncu on a scale-20 column sample
+# (profiles/k_numeric_x_s20_cols4096.txt), used to scale roofline.traffic
+NUMERIC_DRAM_READ_PER_MULT = 6.16
+NUMERIC_DRAM_WRITE_PER_ENTRY = 17.22
 # DRAM bytes of the multi-source BFS kernels per scanned edge (expand +
 # finalize, profiles/launches_msbfs22.txt)
 MSBFS_DRAM_PER_SCANNED_EDGE = 19.5
@@ -408,12 +408,12 @@ def bench_spgemm(args, world, A, Ad, ctx, stream, scale, ef, hbm, peak_kind):
                             "ms_per_step": ms_x / args.steps, "ms_symbolic": agg_x["sizing"],
                             "ms_numeric": agg_x["numeric"], "phases": st_x.phases,
                             "identical_output": same, "learned_speedup": ms_x / ms},
-        "roofline": {"bound": "hbm", "kernel": "k_numeric", "achieved": achieved, "peak": hbm,
-                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
+        "roofline": {"bound": "hbm", "kernel": "k_numeric_x (numeric pass of the big columns, exact fold)",
+                     "achieved": achieved, "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": (NUMERIC_DRAM_READ_PER_MULT * flops + NUMERIC_DRAM_WRITE_PER_ENTRY * st.nnz)
                      / max(st.phases, 1),
                      "algorithmic_bytes_per_launch": ba_num / max(st.phases, 1),
-                     "traffic_note": "DRAM bytes per launch scaled from profiles/k_numeric_s20_cols4096.txt "
+                     "traffic_note": "DRAM bytes per launch scaled from profiles/k_numeric_x_s20_cols4096.txt "
                                      "(reads per multiplication, writes per output entry)"},
         "gpu_launches": launches,
         "clocks": ck,
