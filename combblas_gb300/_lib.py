@@ -132,6 +132,17 @@ _SIGS.update({
     "gbc_mcl_expand_f32": (C.c_int, [C.c_void_p, C.POINTER(gbc_matrix), C.c_float, C.c_int64, C.c_int,
                                      C.POINTER(C.c_void_p), C.POINTER(gbc_spgemm_stats)]),
     "gbc_mcl_prune_select_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_float, C.c_int64, C.POINTER(C.c_void_p)]),
+    "gbc_mcl_prune_select_recover_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_float, C.c_int64, C.c_int64,
+                                                   C.c_float, C.POINTER(C.c_void_p)]),
+    "gbc_mcl_expand_recover_f32": (C.c_int, [C.c_void_p, C.POINTER(gbc_matrix), C.c_float, C.c_int64, C.c_int64,
+                                             C.c_float, C.c_int, C.POINTER(C.c_void_p),
+                                             C.POINTER(gbc_spgemm_stats)]),
+    "gbc_mcl_make_col_stochastic_f32": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gbc_mcl_inflate_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double]),
+    "gbc_mcl_chaos_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_float)]),
+    "gbc_mcl_iterate_f32": (C.c_int, [C.c_void_p, C.POINTER(gbc_matrix), C.c_double, C.c_float, C.c_int64,
+                                      C.c_int64, C.c_float, C.c_int, C.c_int64, C.POINTER(C.c_void_p),
+                                      C.POINTER(C.c_int64), C.POINTER(C.c_float)]),
     "gbc_graph_create": (C.c_int, [C.c_void_p, C.POINTER(gbc_matrix), C.POINTER(C.c_void_p)]),
     "gbc_graph_destroy": (C.c_int, [C.c_void_p]),
     "gbc_graph_set_policy": (C.c_int, [C.c_void_p, C.c_int]),

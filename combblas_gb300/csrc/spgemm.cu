@@ -2098,11 +2098,11 @@ int spgemm_features(gbc_context *ctx, const gbc_matrix *Am, const gbc_matrix *Bm
 // directly (no compaction pass).
 int mcl_select_device2(Context *ctx, int64_t nrow, int64_t n, const int64_t *cnt, const int32_t *flag,
                        const int64_t *beg0, const int64_t *ir0, const float *v0, const int64_t *beg1,
-                       const int64_t *ir1, const float *v1, float thr, int64_t select, const int64_t *jc,
-                       gbc_result **out);
+                       const int64_t *ir1, const float *v1, float thr, int64_t select, int64_t rnum, float rpct,
+                       const int64_t *jc, gbc_result **out);
 
-int mcl_expand(gbc_context *ctx, const gbc_matrix *Am, float thr, int64_t select, int sizing, gbc_result **out,
-               gbc_spgemm_stats *st)
+int mcl_expand(gbc_context *ctx, const gbc_matrix *Am, float thr, int64_t select, int64_t rnum, float rpct,
+               int sizing, gbc_result **out, gbc_spgemm_stats *st)
 {
     if (!ctx || !Am || !out) return fail(GBC_EINVAL, "null argument");
     if (Am->nrow != Am->ncol) return fail(GBC_EINVAL, "MCL needs a square matrix");
@@ -2123,7 +2123,8 @@ int mcl_expand(gbc_context *ctx, const gbc_matrix *Am, float thr, int64_t select
             note_launch();
         }
         GBC_TRY(mcl_select_device2(ctx, A.nrow, O.nb, O.cnt, O.flag, O.beg0, O.ir0, static_cast<const float *>(O.v0),
-                                   O.beg1, O.ir1, static_cast<const float *>(O.v1), thr, select, jc, out));
+                                   O.beg1, O.ir1, static_cast<const float *>(O.v1), thr, select, rnum, rpct, jc,
+                                   out));
         cudaEventRecord(ctx->ev[4], s);
         GBC_CUDA_TRY(cudaEventSynchronize(ctx->ev[4]));
         if (st) {
@@ -2144,7 +2145,8 @@ int mcl_expand(gbc_context *ctx, const gbc_matrix *Am, float thr, int64_t select
     gbc_spgemm_stats s1{};
     GBC_TRY(spgemm_exact<PlusTimes<float>>(ctx, A, A, opt, GBC_F32, &C, &s1));
     int rc = mcl_select_device2(ctx, C->nrow, C->nzc, nullptr, nullptr, C->cp, C->ir,
-                                static_cast<const float *>(C->num), nullptr, nullptr, nullptr, thr, select, C->jc, out);
+                                static_cast<const float *>(C->num), nullptr, nullptr, nullptr, thr, select, rnum, rpct,
+                                C->jc, out);
     gbc_result_free(C);
     GBC_TRY(rc);
     cudaEventRecord(ctx->ev[4], s);
@@ -2597,7 +2599,13 @@ int gbc_context_set_mlp(gbc_context *ctx, gbc_mlp *m)
 int gbc_mcl_expand_f32(gbc_context *ctx, const gbc_matrix *A, float thr, int64_t select, int sizing, gbc_result **out,
                        gbc_spgemm_stats *st)
 {
-    return mcl_expand(ctx, A, thr, select, sizing, out, st);
+    return mcl_expand(ctx, A, thr, select, 0, 0.0f, sizing, out, st);
+}
+
+int gbc_mcl_expand_recover_f32(gbc_context *ctx, const gbc_matrix *A, float thr, int64_t select, int64_t recover_num,
+                               float recover_pct, int sizing, gbc_result **out, gbc_spgemm_stats *st)
+{
+    return mcl_expand(ctx, A, thr, select, recover_num, recover_pct, sizing, out, st);
 }
 
 int gbc_spgemm_colstats(gbc_context *ctx, const gbc_matrix *A, const gbc_matrix *B, int64_t *flop, int64_t *nnz,

@@ -84,7 +84,7 @@ extern "C" int gbc_xprof_read(unsigned long long *out, int reset)
 // values, packed as (int16 min) | (int16 max << 16).  Subnormal values count
 // as exponent -64 (their products can underflow: such columns take the
 // ordered kernel); a column without nonzero values gets min > max.
-__global__ void k_aexp_f64(int64_t ncol, const int64_t *acp, const double *aval, int32_t *aexp)
+static __global__ void k_aexp_f64(int64_t ncol, const int64_t *acp, const double *aval, int32_t *aexp)
 {
     const int lane = threadIdx.x & 31;
     const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
@@ -327,7 +327,7 @@ __device__ __forceinline__ bool x_admit(int &ebase, int etop, int64_t nb)
 // column's tile structure): entries ptr[k] .. ptr[k+1]-1 hold, for each
 // touched tile in order, the tile and the first position of A(:,k) inside
 // it, followed by one end marker (tile 0xFFFF, start = the column's end).
-__global__ void k_ktl_count(int64_t ncol, const uint64_t *amask, int mask_words, int64_t *cnt)
+static __global__ void k_ktl_count(int64_t ncol, const uint64_t *amask, int mask_words, int64_t *cnt)
 {
     const int64_t c = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (c >= ncol) return;
@@ -337,7 +337,7 @@ __global__ void k_ktl_count(int64_t ncol, const uint64_t *amask, int mask_words,
 }
 
 // One warp per column; lanes test 32 tiles at a time.
-__global__ void k_ktl_fill(int64_t ncol, const uint32_t *tptr, int T, const int64_t *ptr, uint32_t *kstart,
+static __global__ void k_ktl_fill(int64_t ncol, const uint32_t *tptr, int T, const int64_t *ptr, uint32_t *kstart,
                            uint16_t *ktile)
 {
     const int lane = threadIdx.x & 31;

@@ -275,6 +275,39 @@ int gbc_mcl_prune_select_f32(gbc_context *ctx, const gbc_result *C, float thr, i
  * GBC_SIZING_EXACT or GBC_SIZING_LEARNED; stats describe the SpGEMM. */
 int gbc_mcl_expand_f32(gbc_context *ctx, const gbc_matrix *A, float thr, int64_t select, int sizing, gbc_result **out,
                        gbc_spgemm_stats *stats);
+/* The same two steps with recovery (recoverNum > 0, ParFriends.h:290-330):
+ * a column left with fewer than recover_num entries > thr whose kept sum is
+ * below recover_pct takes back its entries >= the recover_num-th largest
+ * value (Kselect1 over the sparse column, SpParMat.cpp:1411-1690: the
+ * column's smallest value when it holds fewer, FLT_MIN when empty).  Column
+ * sums here are exact sums of the kept values rounded once to fp32, so they
+ * do not depend on the entries' storage order.  recover_num == 0 gives the
+ * calls above. */
+int gbc_mcl_prune_select_recover_f32(gbc_context *ctx, const gbc_result *C, float thr, int64_t select,
+                                     int64_t recover_num, float recover_pct, gbc_result **out);
+int gbc_mcl_expand_recover_f32(gbc_context *ctx, const gbc_matrix *A, float thr, int64_t select, int64_t recover_num,
+                               float recover_pct, int sizing, gbc_result **out, gbc_spgemm_stats *stats);
+/* The MCL vector glue on a device fp32 result, in place (Applications/
+ * MCL.cpp:389-449).  MakeColStochastic scales every column by 1 / (its sum),
+ * FLT_MAX for a zero sum (safemultinv).  Inflate raises every value to
+ * `power` (pow in double, rounded to fp32).  Chaos is the max over columns
+ * of (column max - sum of squares) * nnz(column), at least 0; the column
+ * sums are exact sums rounded once to fp32. */
+int gbc_mcl_make_col_stochastic_f32(gbc_context *ctx, gbc_result *A);
+int gbc_mcl_inflate_f32(gbc_context *ctx, gbc_result *A, double power);
+int gbc_mcl_chaos_f32(gbc_context *ctx, const gbc_result *A, float *chaos);
+/* The HipMCL iteration loop (MCL.cpp:526-626, one layer, one phase) on a
+ * square fp32 matrix whose loops are already adjusted (AdjustLoops,
+ * :463-473, is the caller's): MakeColStochastic; prune/select/recovery
+ * once before the loop when nnz / n > max(select, recover_num); then, while
+ * chaos > 0.0001: expansion with prune/select/recovery, MakeColStochastic,
+ * Chaos, Inflate(inflation), MakeColStochastic.  max_iter > 0 caps the
+ * iterations.  The matrix stays on the device between iterations; *out is
+ * the converged matrix, *iterations and *chaos (either may be NULL) the
+ * loop count and the last chaos. */
+int gbc_mcl_iterate_f32(gbc_context *ctx, const gbc_matrix *A, double inflation, float thr, int64_t select,
+                        int64_t recover_num, float recover_pct, int sizing, int64_t max_iter, gbc_result **out,
+                        int64_t *iterations, float *chaos);
 
 /* ------------------------------------------------------------ SpMSpV / BFS */
 /* A square pattern matrix prepared once for repeated sparse-vector

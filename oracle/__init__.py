@@ -92,6 +92,11 @@ def _ref():
         lib.ref_mcl_expand.argtypes = [C.c_int64, _P64, _P64, np.ctypeslib.ndpointer(dtype=np.float32),
                                        C.c_float, C.c_int64, C.c_int64, C.c_float]
         lib.ref_num_threads.restype = C.c_int
+        lib.ref_result_nnz.restype = C.c_int64
+        lib.ref_mcl_iterate.restype = C.c_int64
+        lib.ref_mcl_iterate.argtypes = [C.c_int64, _P64, _P64, np.ctypeslib.ndpointer(dtype=np.float32), C.c_double,
+                                        C.c_float, C.c_int64, C.c_int64, C.c_float, C.c_int64, C.c_int,
+                                        C.POINTER(C.c_float)]
         lib.ref_spmv.restype = C.c_int
         lib.ref_spmv.argtypes = [C.c_int, C.c_int64, C.c_int64, _P64, _P64, C.c_void_p, C.c_void_p, C.c_void_p]
         lib.ref_multiway_merge.restype = C.c_int64
@@ -173,6 +178,21 @@ def ref_mcl_expand(A, thr: float, select: int, recover_num: int = 0, recover_pct
     return rows, cols, vals, lib.ref_result_seconds()
 
 
+def ref_mcl_iterate(A, inflation: float = 2.0, thr: float = 1e-4, select: int = 1100, recover_num: int = 1400,
+                    recover_pct: float = 0.9, max_iter: int = 0, mode: int = 0):
+    """The HipMCL loop (mode 0) or one of its vector steps (1 MakeColStochastic,
+    2 Inflate, 3 Chaos) run by the reference's own SpParMat calls
+    (ref_harness.cpp ref_mcl_iterate).  Returns (canonical CSC, iterations,
+    chaos)."""
+    lib = _ref()
+    chaos = C.c_float(0.0)
+    it = lib.ref_mcl_iterate(A.ncol, np.ascontiguousarray(A.colptr), np.ascontiguousarray(A.rowidx),
+                             np.ascontiguousarray(A.values, np.float32), float(inflation), float(thr), int(select),
+                             int(recover_num), float(recover_pct), int(max_iter), int(mode), C.byref(chaos))
+    rows, cols, vals = _fetch(lib, lib.ref_result_nnz(), np.float32)
+    return tuples_to_csc(rows, cols, vals, A.ncol), it, chaos.value
+
+
 def ref_num_threads() -> int:
     return _ref().ref_num_threads()
 
@@ -197,6 +217,15 @@ def _port():
         lib.gbc_o_mcl_select.restype = C.c_int64
         lib.gbc_o_mcl_select.argtypes = [C.c_int64, _P64, _P64, np.ctypeslib.ndpointer(dtype=np.float32),
                                          C.c_float, C.c_int64]
+        lib.gbc_o_mcl_select_recover.restype = C.c_int64
+        lib.gbc_o_mcl_select_recover.argtypes = [C.c_int64, _P64, _P64, np.ctypeslib.ndpointer(dtype=np.float32),
+                                                 C.c_float, C.c_int64, C.c_int64, C.c_float]
+        lib.gbc_o_mcl_colscale.restype = None
+        lib.gbc_o_mcl_colscale.argtypes = [C.c_int64, _P64, np.ctypeslib.ndpointer(dtype=np.float32)]
+        lib.gbc_o_mcl_chaos.restype = C.c_float
+        lib.gbc_o_mcl_chaos.argtypes = [C.c_int64, _P64, np.ctypeslib.ndpointer(dtype=np.float32)]
+        lib.gbc_o_mcl_inflate.restype = None
+        lib.gbc_o_mcl_inflate.argtypes = [C.c_int64, np.ctypeslib.ndpointer(dtype=np.float32), C.c_double]
         lib.gbc_o_num_threads.restype = C.c_int
         _port_lib = lib
     return _port_lib
@@ -430,12 +459,64 @@ def ref_msbfs(A, roots):
     return msbfs_loop(Ap, roots, mult)
 
 
-def port_mcl_select(Ccp, Cri, Cv, thr: float, select: int):
+def port_mcl_select(Ccp, Cri, Cv, thr: float, select: int, recover_num: int = 0, recover_pct: float = 0.0):
+    """MCLPruneRecoverySelect restated (oracle.c gbc_o_mcl_select_recover)."""
     lib = _port()
     n = len(Ccp) - 1
-    nnz = lib.gbc_o_mcl_select(n, np.ascontiguousarray(Ccp, np.int64), np.ascontiguousarray(Cri, np.int64),
-                               np.ascontiguousarray(Cv, np.float32), thr, select)
+    nnz = lib.gbc_o_mcl_select_recover(n, np.ascontiguousarray(Ccp, np.int64), np.ascontiguousarray(Cri, np.int64),
+                                       np.ascontiguousarray(Cv, np.float32), thr, select, recover_num, recover_pct)
     return _port_csc(lib, n, nnz, np.float32)
+
+
+def port_mcl_colscale(cp, v):
+    """MakeColStochastic restated (oracle.c gbc_o_mcl_colscale); new values."""
+    v = np.array(v, np.float32)
+    _port().gbc_o_mcl_colscale(len(cp) - 1, np.ascontiguousarray(cp, np.int64), v)
+    return v
+
+
+def port_mcl_chaos(cp, v) -> float:
+    """Chaos restated (oracle.c gbc_o_mcl_chaos)."""
+    return _port().gbc_o_mcl_chaos(len(cp) - 1, np.ascontiguousarray(cp, np.int64), np.ascontiguousarray(v, np.float32))
+
+
+def port_mcl_inflate(v, power: float):
+    """Inflate restated (oracle.c gbc_o_mcl_inflate); new values."""
+    v = np.array(v, np.float32)
+    _port().gbc_o_mcl_inflate(len(v), v, float(power))
+    return v
+
+
+class _Csc:
+    def __init__(self, n, cp, ri, v):
+        self.nrow = self.ncol = n
+        self.colptr, self.rowidx, self.values = cp, ri, v
+        self.nnz = len(ri)
+
+
+def port_mcl_iterate(A, inflation: float = 2.0, thr: float = 1e-4, select: int = 1100, recover_num: int = 1400,
+                     recover_pct: float = 0.9, max_iter: int = 0):
+    """The HipMCL loop of Applications/MCL.cpp:526-626 (one layer, one phase)
+    restated over the port's SpGEMM, prune/select/recovery and vector steps:
+    MakeColStochastic, the pre-loop prune when nnz / n > max(select,
+    recover_num), then while chaos > 0.0001 (EPS, :55): expand + prune,
+    MakeColStochastic, Chaos, Inflate, MakeColStochastic.  Returns
+    (canonical CSC, iterations, chaos)."""
+    n = A.ncol
+    cp, ri = np.asarray(A.colptr, np.int64), np.asarray(A.rowidx, np.int64)
+    v = port_mcl_colscale(cp, A.values)
+    if n > 0 and len(ri) // n > max(select, recover_num):
+        cp, ri, v = port_mcl_select(cp, ri, v, thr, select, recover_num, recover_pct)
+    chaos, it = np.float32(1.0), 0
+    while float(chaos) > 0.0001 and (max_iter <= 0 or it < max_iter):
+        M = _Csc(n, cp, ri, v)
+        pcp, pri, pv = port_spgemm(M, M, SR_PLUSTIMES_F32, sorted=True)
+        cp, ri, v = port_mcl_select(pcp, pri, pv, thr, select, recover_num, recover_pct)
+        v = port_mcl_colscale(cp, v)
+        chaos = np.float32(port_mcl_chaos(cp, v))
+        v = port_mcl_colscale(cp, port_mcl_inflate(v, inflation))
+        it += 1
+    return canonical_csc(cp, ri, v), it, float(chaos)
 
 
 def port_num_threads() -> int:

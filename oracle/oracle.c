@@ -19,7 +19,9 @@
  *                     touched rows, output sorted by row.
  *   gbc_o_bfs         BFS_CSC level loop (SpMSpVBench.cpp:105-156) over
  *                     SelectMinSR (SpMSpVBench.cpp:79-100).
- *   gbc_o_mcl_select  MCLPruneRecoverySelect with recoverNum == 0
+ *   gbc_o_mcl_select  MCLPruneRecoverySelect (recovery: gbc_o_mcl_select_recover)
+ *   gbc_o_mcl_colscale / gbc_o_mcl_chaos / gbc_o_mcl_inflate
+ *                     MakeColStochastic, Chaos, Inflate (Applications/MCL.cpp:389-449)
  *                     (ParFriends.h:185-354) and Kselect1
  *                     (SpParMat.cpp:1191-1300): prune <= thr for the
  *                     statistics, select columns whose pruned nnz > k, kth =
@@ -80,6 +82,12 @@ int gbc_o_num_threads(void)
     return 1;
 #endif
 }
+
+int64_t gbc_o_mcl_select_recover(int64_t n, const int64_t *Ccp, const int64_t *Cri, const float *Cv, float thr,
+                                 int64_t select, int64_t recover_num, float recover_pct);
+void gbc_o_mcl_colscale(int64_t n, const int64_t *cp, float *v);
+float gbc_o_mcl_chaos(int64_t n, const int64_t *cp, const float *v);
+void gbc_o_mcl_inflate(int64_t nnz, float *v, double power);
 
 /* ------------------------------------------------------- symbolic passes */
 /* estimateFLOP, CSC form (mtSpGEMM.h:1318-1359). */
@@ -554,11 +562,74 @@ static int cmp_f32_desc(const void *x, const void *y)
     return (a < b) - (a > b);
 }
 
-/* Prune + select of one MCL expansion step with recoverNum = 0
- * (ParFriends.h:185-354).  Input C is CSC fp32 (rows in any order); output
- * keeps the input's within-column order.  Returns nnz of the result. */
-int64_t gbc_o_mcl_select(int64_t n, const int64_t *Ccp, const int64_t *Cri, const float *Cv, float thr,
-                         int64_t select)
+/* Column sum of the fp32 values of [b, e) that pass keep(v) (mode 0: v > thr,
+ * mode 1: !(v < thr)): the exact sum of their parts
+ * (with 2^emax the largest value's exponent among them, every part below
+ * 2^(emax - 72) is truncated),
+ * rounded to double and then to float -- independent of the column's
+ * storage order (the library's definition of the MCL column sums). */
+static float mcl_colsum(const float *v, int64_t b, int64_t e, float thr, int mode)
+{
+    int emax = -1000;
+    for (int64_t p = b; p < e; ++p) {
+        const float x = mode == 2 ? (float)((double)v[p] * v[p]) : v[p];
+        if (mode == 0 ? !(x > thr) : mode == 1 ? (x < thr) : 0) continue;
+        uint32_t u;
+        memcpy(&u, &x, 4);
+        if ((u << 1) == 0) continue;
+        int ex = (int)((u >> 23) & 0xff);
+        if (ex == 0) ex = 1;
+        if (ex > emax) emax = ex;
+    }
+    if (emax == -1000) return 0.0f;
+    const int unit = emax - 150 - 72; /* value of the accumulator's lowest bit: 2^unit */
+    __int128 acc = 0;
+    for (int64_t p = b; p < e; ++p) {
+        const float x = mode == 2 ? (float)((double)v[p] * v[p]) : v[p];
+        if (mode == 0 ? !(x > thr) : mode == 1 ? (x < thr) : 0) continue;
+        uint32_t u;
+        memcpy(&u, &x, 4);
+        int ex = (int)((u >> 23) & 0xff);
+        uint32_t m = u & 0x7fffff;
+        if (ex) m |= 0x800000; else ex = 1;
+        const int sh = ex - 150 - unit; /* m * 2^(ex - 150) = (m << sh) * 2^unit */
+        __int128 t = sh >= 0 ? ((__int128)m << sh) : (__int128)(m >> (-sh < 32 ? -sh : 31));
+        acc += (u >> 31) ? -t : t;
+    }
+    return (float)round_exact(acc, 1, unit + 1075);
+}
+
+/* Kselect1 with a sparse column list (SpParMat.cpp:1411-1690): the k-th
+ * largest value of the column, its smallest value when it holds fewer than
+ * k entries, numeric_limits<float>::min() when it is empty. */
+static float mcl_kth(const float *v, int64_t b, int64_t e, int64_t k, float **buf, int64_t *cap)
+{
+    if (e == b) return 1.17549435e-38f;
+    if (e - b > *cap) {
+        free(*buf);
+        *cap = e - b;
+        *buf = (float *)malloc((size_t)*cap * sizeof(float));
+    }
+    memcpy(*buf, v + b, (size_t)(e - b) * sizeof(float));
+    qsort(*buf, (size_t)(e - b), sizeof(float), cmp_f32_desc);
+    return e - b >= k ? (*buf)[k - 1] : (*buf)[e - b - 1];
+}
+
+/* Prune + select + recovery of one MCL expansion step
+ * (MCLPruneRecoverySelect, ParFriends.h:185-354).  Per column of C (fp32
+ * CSC, rows in any order; the output keeps the within-column order):
+ *   nnzP, sumP of the entries with val > thr (the "val <= thr" prune);
+ *   recovered when recover_num > 0, nnzP < recover_num, nnz > nnzP and
+ *     sumP < recover_pct: cut = Kselect(recover_num) of the whole column;
+ *   else selected when select > 0 and nnzP > select: cut = Kselect(select),
+ *     and, when recover_num > 0, the selection is recovered if the entries
+ *     it keeps (val >= cut) number fewer than recover_num and sum below
+ *     recover_pct: cut = Kselect(recover_num);
+ *   else cut = thr;
+ * then PruneColumn(std::less) drops val < cut.  Column sums: mcl_colsum.
+ * Returns nnz of the result. */
+int64_t gbc_o_mcl_select_recover(int64_t n, const int64_t *Ccp, const int64_t *Cri, const float *Cv, float thr,
+                                 int64_t select, int64_t recover_num, float recover_pct)
 {
     float *cut = (float *)malloc((size_t)(n > 0 ? n : 1) * sizeof(float));
     int64_t *keep = (int64_t *)malloc((size_t)(n > 0 ? n : 1) * sizeof(int64_t));
@@ -568,20 +639,22 @@ int64_t gbc_o_mcl_select(int64_t n, const int64_t *Ccp, const int64_t *Cri, cons
         int64_t cap = 0;
 #pragma omp for schedule(dynamic, 64)
         for (int64_t j = 0; j < n; ++j) {
-            int64_t b = Ccp[j], e = Ccp[j + 1];
+            const int64_t b = Ccp[j], e = Ccp[j + 1];
             int64_t npruned = 0; /* entries surviving "val <= thr" pruning */
             for (int64_t p = b; p < e; ++p) npruned += !(Cv[p] <= thr);
             float c = thr; /* pruneCols default: hardThreshold */
-            if (select > 0 && npruned > select) {
-                /* Kselect1: k-th largest of the unpruned column */
-                if (e - b > cap) {
-                    free(buf);
-                    cap = e - b;
-                    buf = (float *)malloc((size_t)cap * sizeof(float));
+            const int recover = recover_num > 0 && npruned < recover_num && (e - b) > npruned &&
+                                mcl_colsum(Cv, b, e, thr, 0) < recover_pct;
+            if (recover) {
+                c = mcl_kth(Cv, b, e, recover_num, &buf, &cap);
+            } else if (select > 0 && npruned > select) {
+                c = mcl_kth(Cv, b, e, select, &buf, &cap);
+                if (recover_num > 0) {
+                    int64_t n1 = 0;
+                    for (int64_t p = b; p < e; ++p) n1 += !(Cv[p] < c);
+                    if (n1 < recover_num && mcl_colsum(Cv, b, e, c, 1) < recover_pct)
+                        c = mcl_kth(Cv, b, e, recover_num, &buf, &cap);
                 }
-                memcpy(buf, Cv + b, (size_t)(e - b) * sizeof(float));
-                qsort(buf, (size_t)(e - b), sizeof(float), cmp_f32_desc);
-                c = buf[select - 1];
             }
             cut[j] = c;
             int64_t kcount = 0; /* PruneColumn(std::less): drop val < cut */
@@ -606,4 +679,48 @@ int64_t gbc_o_mcl_select(int64_t n, const int64_t *Ccp, const int64_t *Cri, cons
     free(cut);
     free(keep);
     return tot;
+}
+
+/* recoverNum = 0 (the expansion step of MemEfficientSpGEMM without recovery). */
+int64_t gbc_o_mcl_select(int64_t n, const int64_t *Ccp, const int64_t *Cri, const float *Cv, float thr,
+                         int64_t select)
+{
+    return gbc_o_mcl_select_recover(n, Ccp, Cri, Cv, thr, select, 0, 0.0f);
+}
+
+/* MakeColStochastic (Applications/MCL.cpp:389-394) in place: every column
+ * scaled by 1 / (its sum), FLT_MAX for a zero sum (safemultinv,
+ * Operations.h:103-110).  The sum is mcl_colsum over all values. */
+void gbc_o_mcl_colscale(int64_t n, const int64_t *cp, float *v)
+{
+    _Pragma("omp parallel for schedule(dynamic, 256)")
+    for (int64_t j = 0; j < n; ++j) {
+        const float sum = mcl_colsum(v, cp[j], cp[j + 1], -3.4028235e38f, 1);
+        const float inv = sum == 0.0f ? 3.4028235e38f : 1.0f / sum;
+        for (int64_t p = cp[j]; p < cp[j + 1]; ++p) v[p] = v[p] * inv;
+    }
+}
+
+/* Chaos (MCL.cpp:407-421): max over columns of (column max - sum of
+ * squares) * nnz(column); both maxima start from 0 (the entries are
+ * non-negative).  Each square is rounded to float, as static_cast<float> of
+ * pow(val, 2) is; the sum of squares is mcl_colsum's exact sum. */
+float gbc_o_mcl_chaos(int64_t n, const int64_t *cp, const float *v)
+{
+    float best = 0.0f;
+    for (int64_t j = 0; j < n; ++j) {
+        float mx = 0.0f;
+        for (int64_t p = cp[j]; p < cp[j + 1]; ++p) mx = v[p] > mx ? v[p] : mx;
+        const float sq = mcl_colsum(v, cp[j], cp[j + 1], 0.0f, 2);
+        const float c = (mx - sq) * (float)(cp[j + 1] - cp[j]);
+        best = c > best ? c : best;
+    }
+    return best;
+}
+
+/* Inflate (MCL.cpp:446-450) in place: pow(val, power) in double, stored as
+ * float. */
+void gbc_o_mcl_inflate(int64_t nnz, float *v, double power)
+{
+    for (int64_t p = 0; p < nnz; ++p) v[p] = (float)pow((double)v[p], power);
 }

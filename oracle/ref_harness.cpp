@@ -16,6 +16,9 @@
 //                           Applications/SpMSpV-IPDPS2017/SpMSpVBench.cpp:105-156
 //   ref_mcl_expand       -> MemEfficientSpGEMM + MCLPruneRecoverySelect
 //                           (ParFriends.h:452,185)
+//   ref_mcl_iterate      -> the HipMCL loop of Applications/MCL.cpp:526-626
+//                           (one layer), over MemEfficientSpGEMM and the
+//                           reference's SpParMat Reduce / DimApply / Apply
 //   ref_multiway_merge   -> MultiwayMerge (MultiwayMerge.h:428)
 //   ref_spmv             -> dcsc_gespmv (Friends.h:63)
 #include "CombBLAS/CombBLAS.h"
@@ -294,6 +297,8 @@ void ref_result_copy(int64_t *rows, int64_t *cols, void *vals)
 
 double ref_result_seconds() { return g_res.seconds; }
 
+int64_t ref_result_nnz() { return (int64_t)g_res.rows.size(); }
+
 // which = 0: estimateFLOP per nonempty column of B; 1: estimateNNZ_Hash.
 // Pattern-only (values ignored).  Returns nzc(B).
 int64_t ref_colstats(int which, int64_t m, int64_t k, int64_t n, const int64_t *Acp, const int64_t *Ari,
@@ -397,6 +402,75 @@ int64_t ref_mcl_expand(int64_t n, const int64_t *Acp, const int64_t *Ari, const 
     g_res.seconds = now() - t0;
     store_dcsc(C.seq());
     return C.seq().getnnz();
+}
+
+// MakeColStochastic, Chaos and Inflate as Applications/MCL.cpp:389-449
+// writes them (that file holds a main() and cannot be included): the
+// reference's own SpParMat::Reduce, DimApply and Apply do the arithmetic.
+typedef SpParMat<int64_t, float, SpDCCols<int64_t, float>> MclMat;
+
+static void mcl_make_col_stochastic(MclMat &A)
+{
+    FullyDistVec<int64_t, float> colsums = A.Reduce(Column, std::plus<float>(), 0.0);
+    colsums.Apply(safemultinv<float>());
+    A.DimApply(Column, colsums, std::multiplies<float>());
+}
+
+static float mcl_chaos(MclMat &A)
+{
+    FullyDistVec<int64_t, float> colssqs = A.Reduce(Column, std::plus<float>(), 0.0, [](float val) { return pow(val, 2); });
+    FullyDistVec<int64_t, float> colmaxs = A.Reduce(Column, maximum<float>(), 0.0);
+    colmaxs -= colssqs;
+    FullyDistVec<int64_t, float> nnzPerColumn = A.Reduce(Column, std::plus<float>(), 0.0, [](float val) { return 1.0; });
+    colmaxs.EWiseApply(nnzPerColumn, std::multiplies<float>());
+    return colmaxs.Reduce(maximum<float>(), 0.0);
+}
+
+static void mcl_inflate(MclMat &A, double power)
+{
+    A.Apply([power](float val) { return pow(val, power); });
+}
+
+// The HipMCL loop from the loop-adjusted matrix on (MCL.cpp:526-626 with
+// layers == 1, phases == 1, kselectVersion 1, computationKernel 1).  mode 0
+// runs the loop (at most max_iter iterations when max_iter > 0) and returns
+// the iteration count, the last chaos in *chaos; mode 1 applies only
+// MakeColStochastic, mode 2 only Inflate(inflation), mode 3 only Chaos (into
+// *chaos).  The matrix ends in g_res (DCSC order).
+int64_t ref_mcl_iterate(int64_t n, const int64_t *Acp, const int64_t *Ari, const float *Av, double inflation,
+                        float thr, int64_t select, int64_t recover_num, float recover_pct, int64_t max_iter, int mode,
+                        float *chaos_out)
+{
+    auto grid = std::make_shared<CommGrid>(MPI_COMM_WORLD, 1, 1);
+    MclMat A(make_dcsc<float>(n, n, Acp, Ari, Av), grid);
+    int64_t it = 0;
+    double t0 = now();
+    if (mode == 1) {
+        mcl_make_col_stochastic(A);
+    } else if (mode == 2) {
+        mcl_inflate(A, inflation);
+    } else if (mode == 3) {
+        *chaos_out = mcl_chaos(A);
+    } else {
+        mcl_make_col_stochastic(A);
+        const int64_t nnz = A.getnnz(), nv = A.getnrow();
+        if (nnz / nv > std::max(select, recover_num))
+            MCLPruneRecoverySelect(A, thr, select, recover_num, recover_pct, 1);
+        float chaos = 1;
+        while (chaos > 0.0001 && (max_iter <= 0 || it < max_iter)) {
+            A = MemEfficientSpGEMM<PlusTimesSRing<float, float>, float, SpDCCols<int64_t, float>>(
+                A, A, 1, thr, select, recover_num, recover_pct, 1, 1, (int64_t)0);
+            mcl_make_col_stochastic(A);
+            chaos = mcl_chaos(A);
+            mcl_inflate(A, inflation);
+            mcl_make_col_stochastic(A);
+            ++it;
+        }
+        *chaos_out = chaos;
+    }
+    g_res.seconds = now() - t0;
+    store_dcsc(A.seq());
+    return it;
 }
 
 int ref_num_threads()

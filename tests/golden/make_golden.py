@@ -200,6 +200,30 @@ def main(ref_root: str):
         d[f"{key}/rows"] = r
         d[f"{key}/cols"] = c
         d[f"{key}/vals"] = v
+    # MCL prune/select with recovery (ParFriends.h:290-330)
+    for thr, k, rn, pct in ((1e-2, 30, 40, 0.9), (5e-3, 20, 30, 0.95), (2e-2, 10, 25, 0.8), (3e-2, 5, 12, 0.9)):
+        r, c, v, _ = O.ref_mcl_expand(M, thr, k, rn, pct)
+        key = f"mclrec/mcl4096/{thr:g}/{k}/{rn}/{pct:g}"
+        d[f"{key}/rows"] = r
+        d[f"{key}/cols"] = c
+        d[f"{key}/vals"] = v
+    # MCL vector steps (MCL.cpp:389-449) and the HipMCL loop (:526-626)
+    (cp, r, v), _, _ = O.ref_mcl_iterate(M, mode=1)
+    d["mclstep/mcl4096/colscale"] = v
+    for power in (2.0, 1.5):
+        (cp, r, v), _, _ = O.ref_mcl_iterate(M, inflation=power, mode=2)
+        d[f"mclstep/mcl4096/inflate/{power:g}"] = v
+    _, _, chaos = O.ref_mcl_iterate(M, mode=3)
+    d["mclstep/mcl4096/chaos"] = np.array([chaos], np.float32)
+    for infl, thr, k, rn, pct, mi in ((2.0, 1e-4, 30, 40, 0.9, 0), (1.5, 1e-3, 20, 30, 0.9, 0),
+                                      (2.0, 1e-4, 30, 40, 0.9, 2)):
+        (cp, r, v), it, chaos = O.ref_mcl_iterate(M, infl, thr, k, rn, pct, mi)
+        key = f"mclloop/mcl4096/{infl:g}/{thr:g}/{k}/{rn}/{pct:g}/{mi}"
+        d[f"{key}/colptr"] = cp
+        d[f"{key}/rowidx"] = r
+        d[f"{key}/values"] = v
+        d[f"{key}/iterations"] = np.array([it], np.int64)
+        d[f"{key}/chaos"] = np.array([chaos], np.float32)
     # Galerkin triple product R * (A * R^T) on a 4^3 Poisson grid
     A = G.poisson27(4)
     R = G.aggregation(4)

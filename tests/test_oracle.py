@@ -122,6 +122,68 @@ def test_port_mcl(oracle_lib, golden):
         assert np.array_equal(scp, gcp) and np.array_equal(srows, grows) and np.array_equal(svals, gvals)
 
 
+MCL_RECOVERY = ((1e-2, 30, 40, 0.9), (5e-3, 20, 30, 0.95), (2e-2, 10, 25, 0.8), (3e-2, 5, 12, 0.9))
+
+
+@pytest.mark.parametrize("thr,k,rn,pct", MCL_RECOVERY)
+def test_port_mcl_recovery(oracle_lib, golden, thr, k, rn, pct):
+    """MCLPruneRecoverySelect with recoverNum > 0 (ParFriends.h:290-330)
+    against the reference's own MemEfficientSpGEMM output."""
+    O = oracle_lib
+    M = golden_matrix(golden, "mcl4096")
+    cp, rows, vals = O.port_spgemm(M, M, O.SR_PLUSTIMES_F32, sorted=False)
+    scp, srows, svals = O.canonical_csc(*O.port_mcl_select(cp, rows, vals, thr, k, rn, pct))
+    key = f"mclrec/mcl4096/{thr:g}/{k}/{rn}/{pct:g}"
+    gcp, grows, gvals = O.tuples_to_csc(golden[f"{key}/rows"], golden[f"{key}/cols"], golden[f"{key}/vals"], M.ncol)
+    assert np.array_equal(scp, gcp) and np.array_equal(srows, grows) and np.array_equal(svals, gvals)
+    # recovery changed the outcome: more entries than the same step without it
+    ncp, _, _ = O.port_mcl_select(cp, rows, vals, thr, k)
+    assert gcp[-1] > ncp[-1]
+
+
+def test_port_mcl_vector_steps(oracle_lib, golden):
+    """MakeColStochastic / Inflate / Chaos (MCL.cpp:389-449).  The port's
+    column sums are exact sums rounded once, the reference's a left fold in
+    storage order: scaled values agree within 1e-6 relative (fp32 tolerance
+    1e-5); Inflate is bit-exact; Chaos agrees within 1e-6."""
+    O = oracle_lib
+    M = golden_matrix(golden, "mcl4096")
+    cp, v = np.asarray(M.colptr), np.asarray(M.values, np.float32)
+    sc = O.port_mcl_colscale(cp, v)
+    ref = golden["mclstep/mcl4096/colscale"]
+    assert np.max(np.abs(sc - ref) / ref) < 1e-6
+    for power in (2.0, 1.5):
+        assert np.array_equal(O.port_mcl_inflate(v, power), golden[f"mclstep/mcl4096/inflate/{power:g}"])
+    c = O.port_mcl_chaos(cp, v)
+    assert abs(c - float(golden["mclstep/mcl4096/chaos"][0])) <= 1e-6 * abs(c)
+    # stochastic columns sum to 1 within rounding; a zero column stays zero
+    sums = np.add.reduceat(sc.astype(np.float64), cp[:-1][np.diff(cp) > 0])
+    assert np.all(np.abs(sums - 1.0) < 1e-5)
+
+
+MCL_LOOPS = ((2.0, 1e-4, 30, 40, 0.9, 0), (1.5, 1e-3, 20, 30, 0.9, 0), (2.0, 1e-4, 30, 40, 0.9, 2))
+
+
+@pytest.mark.parametrize("infl,thr,k,rn,pct,mi", MCL_LOOPS)
+def test_port_mcl_loop(oracle_lib, golden, infl, thr, k, rn, pct, mi):
+    """The HipMCL loop (MCL.cpp:526-626) restated against the reference's
+    own loop: converged runs end bit-identical after the same number of
+    iterations; a two-iteration run has the same pattern and values within
+    the fp32 tolerance (1e-5 relative)."""
+    O = oracle_lib
+    M = golden_matrix(golden, "mcl4096")
+    (cp, rows, vals), it, chaos = O.port_mcl_iterate(M, infl, thr, k, rn, pct, mi)
+    key = f"mclloop/mcl4096/{infl:g}/{thr:g}/{k}/{rn}/{pct:g}/{mi}"
+    assert it == int(golden[f"{key}/iterations"][0])
+    assert np.array_equal(cp, golden[f"{key}/colptr"]) and np.array_equal(rows, golden[f"{key}/rowidx"])
+    gv = golden[f"{key}/values"]
+    if mi == 0:
+        assert np.array_equal(vals, gv) and chaos <= 0.0001
+    else:
+        assert np.max(np.abs(vals - gv) / gv) < 1e-5
+        assert abs(chaos - float(golden[f"{key}/chaos"][0])) <= 1e-5 * chaos
+
+
 def test_reference_build_reproduces_golden(oracle_lib, golden):
     """Where the reference was compiled (this container), it still produces
     the committed fixtures."""
