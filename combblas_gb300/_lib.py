@@ -19,6 +19,8 @@ SR_PLUSTIMES = 0
 SR_MINPLUS = 1
 SR_SELECT2NDMIN = 2
 SR_BOOL = 3
+SR_SELECT2ND = 4
+SR_SELECTMAX = 5
 
 VT_F64 = 0
 VT_F32 = 1
@@ -131,6 +133,12 @@ _SIGS.update({
                                       C.c_void_p, C.c_void_p, C.c_int]),
     "gbc_mcl_expand_f32": (C.c_int, [C.c_void_p, C.POINTER(gbc_matrix), C.c_float, C.c_int64, C.c_int,
                                      C.POINTER(C.c_void_p), C.POINTER(gbc_spgemm_stats)]),
+    "gbc_spmspv_plan_create": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(gbc_matrix), C.POINTER(C.c_void_p)]),
+    "gbc_spmspv_plan_destroy": (C.c_int, [C.c_void_p]),
+    "gbc_spmspv_plan_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                       C.POINTER(C.c_int64)]),
+    "gbc_spmspv": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
+                             C.c_void_p, C.POINTER(C.c_int32), C.c_int]),
     "gbc_mcl_prune_select_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_float, C.c_int64, C.POINTER(C.c_void_p)]),
     "gbc_mcl_prune_select_recover_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_float, C.c_int64, C.c_int64,
                                                    C.c_float, C.POINTER(C.c_void_p)]),

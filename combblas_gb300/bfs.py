@@ -57,6 +57,59 @@ def SpMXSpV(graph: Graph, indx: np.ndarray, numx: np.ndarray):
     return indy[:ny.value].copy(), numy[:ny.value].copy()
 
 
+_SX = {"select2ndmin": L.SR_SELECT2NDMIN, "selectmin": L.SR_SELECT2NDMIN, "select2nd": L.SR_SELECT2ND,
+       "selectmax": L.SR_SELECTMAX, "plustimes": L.SR_PLUSTIMES}
+_VT = {np.dtype(np.float64): L.VT_F64, np.dtype(np.float32): L.VT_F32, np.dtype(np.int64): L.VT_I64,
+       np.dtype(np.bool_): L.VT_BOOL}
+
+
+class SpMSpVPlan:
+    """Any m x n matrix held on the device for repeated sparse-vector
+    multiplies over the reference's SpMXSpV semirings (gbc_spmspv_plan):
+    "select2ndmin" / "selectmin", "select2nd" (the value of the largest
+    hitting column, TopDownBFS's boolean Select2ndSRing), "selectmax" and
+    "plustimes" (ascending-column left fold, as SpMXSpV_Bucket).  dtype is
+    the value type of A and, for plustimes, of x and y; None keeps only the
+    pattern (the select semirings)."""
+
+    def __init__(self, A, dtype=None, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        keep: list = []
+        self.dtype = np.dtype(dtype) if dtype is not None else np.dtype(np.bool_)
+        g = as_gbc_matrix(A, keep, None if dtype is None else self.dtype.type)
+        if dtype is None:
+            g.num = None
+        self.h = C.c_void_p()
+        L.check(L.lib().gbc_spmspv_plan_create(self.ctx.h, _VT[self.dtype], C.byref(g), C.byref(self.h)))
+        self.m, self.n = int(A.nrow), int(A.ncol)
+
+    def multiply(self, indx, numx, semiring: str = "select2ndmin"):
+        """y = A x: returns (indy int32 ascending, numy)."""
+        sr = _SX[semiring]
+        dt = self.dtype if sr == L.SR_PLUSTIMES else np.dtype(np.int64)
+        indx = np.ascontiguousarray(indx, np.int32)
+        numx = np.ascontiguousarray(numx, dt)
+        indy = np.empty(max(self.m, 1), np.int32)
+        numy = np.empty(max(self.m, 1), dt)
+        ny = C.c_int32()
+        L.check(L.lib().gbc_spmspv(self.ctx.h, self.h, sr, indx.ctypes.data, numx.ctypes.data, len(indx),
+                                   indy.ctypes.data, numy.ctypes.data, C.byref(ny), L.GBC_HOST))
+        return indy[:ny.value].copy(), numy[:ny.value].copy()
+
+    def close(self):
+        if self.h:
+            L.lib().gbc_spmspv_plan_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        if sys.is_finalizing():
+            return
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def bfs(A_or_graph, source: int, ctx: Context | None = None):
     """BFS from ``source``: (parents int64[n], levels int64[n], stats)."""
     g = A_or_graph if isinstance(A_or_graph, Graph) else Graph(A_or_graph, ctx)

@@ -18,6 +18,7 @@
 
 #include "gbc_internal.cuh"
 #include "semiring.cuh"
+#include "spmv_plan.cuh"
 
 namespace gbc {
 
@@ -284,24 +285,6 @@ __global__ void k_fill_chunks(int64_t m, const int64_t *rowptr, const int64_t *c
     }
 }
 
-struct SpmvPlan {
-    Context *ctx = nullptr;
-    int64_t m = 0, n = 0, nnz = 0;
-    int vt = 0;
-    int64_t *rowptr = nullptr;  // [m+1]
-    int32_t *col = nullptr;     // [nnz]
-    void *val = nullptr;        // [nnz]
-    int64_t nchunks = 0, nlong = 0;
-    int64_t *chunk_start = nullptr;  // [nchunks]
-    int32_t *chunk_row = nullptr;    // [nchunks]
-    int8_t *partial_slot = nullptr;  // [nchunks] -1: the row's only chunk, 1: part of a longer row
-    int64_t *chunk_end = nullptr;    // [nchunks]
-    int64_t nshort = 0;
-    int32_t *short_rows = nullptr;   // [nshort] rows of 1..kShort entries
-    int32_t *long_row = nullptr;     // [nlong] rows of more than one chunk
-    int64_t *long_first = nullptr, *long_end = nullptr;  // their chunk ranges
-    void *partial = nullptr;         // [nchunks] chunk results of long rows
-};
 
 template <typename V>
 static int plan_values(SpmvPlan *p, Workspace &ws, const DevMatrix &A, const int32_t *perm, const int32_t *col_cm)
@@ -315,7 +298,7 @@ static int plan_values(SpmvPlan *p, Workspace &ws, const DevMatrix &A, const int
     return GBC_OK;
 }
 
-static int spmv_plan_build(SpmvPlan *p, const gbc_matrix *Am)
+int spmv_plan_build(SpmvPlan *p, const gbc_matrix *Am)
 {
     Context *ctx = p->ctx;
     cudaStream_t s = ctx->stream;
@@ -450,6 +433,26 @@ static int spmv_run(SpmvPlan *p, const void *x, void *y)
     return GBC_OK;
 }
 
+void spmv_plan_release(SpmvPlan *p)
+{
+    if (!p->ctx) return;
+    cudaSetDevice(p->ctx->device);
+    cudaStreamSynchronize(p->ctx->stream);
+    device_free(p->ctx, p->rowptr);
+    device_free(p->ctx, p->col);
+    device_free(p->ctx, p->val);
+    device_free(p->ctx, p->chunk_start);
+    device_free(p->ctx, p->chunk_row);
+    device_free(p->ctx, p->partial_slot);
+    device_free(p->ctx, p->chunk_end);
+    device_free(p->ctx, p->short_rows);
+    device_free(p->ctx, p->long_row);
+    device_free(p->ctx, p->long_first);
+    device_free(p->ctx, p->long_end);
+    device_free(p->ctx, p->partial);
+    cudaStreamSynchronize(p->ctx->stream);
+}
+
 }  // namespace gbc
 
 using namespace gbc;
@@ -479,21 +482,7 @@ int gbc_spmv_plan_create(gbc_context *ctx, int vt, const gbc_matrix *A, gbc_spmv
 int gbc_spmv_plan_destroy(gbc_spmv_plan *p)
 {
     if (!p) return GBC_OK;
-    cudaSetDevice(p->ctx->device);
-    cudaStreamSynchronize(p->ctx->stream);
-    device_free(p->ctx, p->rowptr);
-    device_free(p->ctx, p->col);
-    device_free(p->ctx, p->val);
-    device_free(p->ctx, p->chunk_start);
-    device_free(p->ctx, p->chunk_row);
-    device_free(p->ctx, p->partial_slot);
-    device_free(p->ctx, p->chunk_end);
-    device_free(p->ctx, p->short_rows);
-    device_free(p->ctx, p->long_row);
-    device_free(p->ctx, p->long_first);
-    device_free(p->ctx, p->long_end);
-    device_free(p->ctx, p->partial);
-    cudaStreamSynchronize(p->ctx->stream);
+    spmv_plan_release(p);
     delete p;
     return GBC_OK;
 }

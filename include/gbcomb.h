@@ -42,6 +42,8 @@ extern "C" {
 #define GBC_SR_MINPLUS 1      /* MinPlusSRing (Semirings.h:235-255) */
 #define GBC_SR_SELECT2NDMIN 2 /* Select2ndMinSR (Applications/FastSV.h:25-44) */
 #define GBC_SR_BOOL 3         /* PlusTimesSRing<bool,bool>: or / and */
+#define GBC_SR_SELECT2ND 4    /* Select2ndSRing (Semirings.h:144-163): add keeps its second argument */
+#define GBC_SR_SELECTMAX 5    /* SelectMaxSRing<bool,T> (Semirings.h:192-210): add = max */
 
 /* value types */
 #define GBC_F64 0
@@ -338,6 +340,31 @@ int gbc_graph_set_policy(gbc_graph *g, int policy);
  * entries.  All four arrays live where `where` says. */
 int gbc_spmspv_select2ndmin_i64(gbc_context *ctx, gbc_graph *g, const int32_t *indx, const int64_t *numx,
                                 int32_t veclen, int32_t *indy, int64_t *numy, int32_t *nnzy, int where);
+
+/* y = A x for any m x n matrix (CSC or DCSC, host or device) over the
+ * semirings of the reference's SpMXSpV overload set (SpImpl.h:49-142).  The
+ * plan copies A to the device once (for a numeric vt also row-major), so
+ * repeated multiplies by one matrix move only the vectors.  sr:
+ *   GBC_SR_SELECT2NDMIN  y(r) = min of the x values hitting r
+ *                        (SpMXSpV_Bucket over SelectMinSR, SpImpl.cpp:389-699);
+ *   GBC_SR_SELECT2ND     y(r) = the x value of the largest hitting column
+ *                        (boolean SpMXSpV over Select2ndSRing, SpImpl.cpp:
+ *                        167-328; TopDownBFS's path, BFSFriends.h:198-207);
+ *   GBC_SR_SELECTMAX     y(r) = max of the hitting x values (SelectMaxSRing);
+ *   GBC_SR_PLUSTIMES     y(r) = sum of A(r,c) * x(c), folded left in
+ *                        ascending column order as SpMXSpV_Bucket's SPA does
+ *                        (bit-exact); numeric plans only.
+ * For the select semirings numx / numy are int64 and A's values are
+ * ignored; for PlusTimes they have the plan's value type.  indx holds
+ * distinct column ids (a repeated id is GBC_EINVAL).  indy / numy receive
+ * nnzy entries sorted by row and must hold up to nrow entries; the vectors
+ * live where `where` says. */
+typedef struct gbc_spmspv_plan gbc_spmspv_plan;
+int gbc_spmspv_plan_create(gbc_context *ctx, int vt, const gbc_matrix *A, gbc_spmspv_plan **plan);
+int gbc_spmspv_plan_destroy(gbc_spmspv_plan *plan);
+int gbc_spmspv_plan_info(const gbc_spmspv_plan *plan, int64_t *nrow, int64_t *ncol, int64_t *nnz);
+int gbc_spmspv(gbc_context *ctx, gbc_spmspv_plan *plan, int sr, const int32_t *indx, const void *numx, int32_t veclen,
+               int32_t *indy, void *numy, int32_t *nnzy, int where);
 
 /* BFS from `source` by repeated SpMSpV with the per-level glue fused, as the
  * BFS_CSC loop of Applications/SpMSpV-IPDPS2017/SpMSpVBench.cpp:128-156:

@@ -9,6 +9,7 @@
  *   gbcomb::LocalSpGEMMHash<SR, NTO>(A, B, clearA, clearB, sort) mtSpGEMM.h:463-467
  *   gbcomb::LocalHybridSpGEMM<SR, NTO>(SpCCols A, SpCCols B, ...)  mtSpGEMM.h:1142-1152
  *   gbcomb::SpMXSpV<SR>(Csc, mA, indx, numx, veclen, indy, numy, SPA)  SpImpl.h:115-124
+ *   gbcomb::SpMXSpV<SR>(Dcsc, mA, indx, numx, veclen, indy*, numy*, cnts, dspls, p_c)  SpImpl.h:59-65
  *   gbcomb::MultiwayMerge<SR>(ArrSpTups, mdim, ndim, delarrs)  MultiwayMerge.h:428-708
  *   gbcomb::dcsc_gespmv<SR>(A, x, y)                           Friends.h:63-77
  *
@@ -32,6 +33,7 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <map>
 #include <memory>
 #include <new>
 #include <stdexcept>
@@ -367,15 +369,147 @@ void dcsc_gespmv(const combblas::SpDCCols<IU, NU> &A, const RHS *x, LHS *y)
     }
 }
 
-// y = A x over a min-select semiring (registered with GBC_SR_SELECT2NDMIN /
-// GBC_I64): appended to indy / numy sorted by row, as SpMXSpV_Bucket does.
+// ------------------------------------------------------------------ SpMSpV
+// Semiring code for the sparse-vector multiplies: the stock boolean
+// Select2ndSRing (TopDownBFS, BFSFriends.h:198-207) and SelectMaxSRing, or a
+// registered Select2ndMin / PlusTimes semiring.
+template <class SR>
+struct spmspv_of {
+    static constexpr int sr = semiring_of<SR>::sr == GBC_SR_SELECT2NDMIN || semiring_of<SR>::sr == GBC_SR_PLUSTIMES
+                                  ? semiring_of<SR>::sr
+                                  : -1;
+};
+template <class T1, class T2>
+struct spmspv_of<combblas::Select2ndSRing<bool, T1, T2>> {
+    static constexpr int sr = GBC_SR_SELECT2ND;
+};
+template <class T2>
+struct spmspv_of<combblas::SelectMaxSRing<bool, T2>> {
+    static constexpr int sr = GBC_SR_SELECTMAX;
+};
+
+namespace detail {
+
+// Device copies of the matrices multiplied so far, one gbc_spmspv_plan per
+// matrix, keyed by the addresses and sizes of its arrays and a strided
+// sample of their contents: a BFS that multiplies one matrix level after
+// level copies it to the device once.
+struct PlanKey {
+    const void *cp, *ir, *num;
+    int64_t m, n, nz, sample;
+    int vt;
+    bool operator<(const PlanKey &o) const
+    {
+        return std::tie(cp, ir, num, m, n, nz, sample, vt) < std::tie(o.cp, o.ir, o.num, o.m, o.n, o.nz, o.sample, o.vt);
+    }
+};
+
+inline std::map<PlanKey, gbc_spmspv_plan *> &plan_cache()
+{
+    static std::map<PlanKey, gbc_spmspv_plan *> cache;
+    return cache;
+}
+
+inline long long &plan_builds()
+{
+    static long long n = 0;
+    return n;
+}
+
+inline int64_t sample_of(const int64_t *cp, int64_t ncp, const int64_t *ir, int64_t nz)
+{
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&h](uint64_t v) { h = (h ^ v) * 1099511628211ull; };
+    for (int64_t k = 0; k < 64 && ncp > 0; ++k) mix((uint64_t)cp[(ncp - 1) * k / 63]);
+    for (int64_t k = 0; k < 64 && nz > 0; ++k) mix((uint64_t)ir[(nz - 1) * k / 63]);
+    return (int64_t)h;
+}
+
+inline gbc_spmspv_plan *spmspv_plan(const gbc_matrix &g, int vt)
+{
+    const PlanKey key{g.cp, g.ir, g.num, g.nrow, g.ncol, g.nnz, sample_of(g.cp, g.nzc + 1, g.ir, g.nnz), vt};
+    auto it = plan_cache().find(key);
+    if (it != plan_cache().end()) return it->second;
+    gbc_spmspv_plan *p = nullptr;
+    check(gbc_spmspv_plan_create(context(), vt, &g, &p), "gbc_spmspv_plan_create");
+    ++plan_builds();
+    plan_cache()[key] = p;
+    return p;
+}
+
+template <class SR, class NUM, class IVT, class OVT>
+constexpr int spmspv_vt()
+{
+    constexpr int sr = spmspv_of<SR>::sr;
+    if constexpr (sr == GBC_SR_SELECT2NDMIN || sr == GBC_SR_SELECT2ND || sr == GBC_SR_SELECTMAX) {
+        return std::is_integral<IVT>::value && std::is_integral<OVT>::value && sizeof(IVT) <= 8 && sizeof(OVT) <= 8
+                   ? GBC_BOOL
+                   : -1;
+    } else if constexpr (sr == GBC_SR_PLUSTIMES) {
+        constexpr int vt = semiring_of<SR>::vt;
+        if constexpr (vt == GBC_F64 || vt == GBC_F32 || vt == GBC_I64) {
+            typedef typename value_c<vt>::type V;
+            return std::is_same<NUM, V>::value && std::is_same<IVT, V>::value && std::is_same<OVT, V>::value ? vt
+                                                                                                              : -1;
+        } else {
+            return -1;
+        }
+    } else {
+        return -1;
+    }
+}
+
+// y = A x on the GPU into (row, value) arrays sorted by row; x entries whose
+// column is not below g.ncol hit nothing and are dropped first.
+template <class SR, class IVT, class OVT>
+void spmspv_run(const gbc_matrix &g, int vt, const int32_t *indx, const IVT *numx, int32_t veclen,
+                std::vector<int32_t> &rows, std::vector<OVT> &vals)
+{
+    constexpr int sr = spmspv_of<SR>::sr;
+    typedef typename std::conditional<sr == GBC_SR_PLUSTIMES, IVT, int64_t>::type XV;
+    typedef typename std::conditional<sr == GBC_SR_PLUSTIMES, OVT, int64_t>::type YV;
+    std::vector<int32_t> xi;
+    std::vector<XV> xv;
+    xi.reserve(veclen);
+    xv.reserve(veclen);
+    for (int32_t k = 0; k < veclen; ++k)
+        if (indx[k] >= 0 && indx[k] < g.ncol) {
+            xi.push_back(indx[k]);
+            xv.push_back(static_cast<XV>(numx[k]));
+        }
+    gbc_spmspv_plan *p = spmspv_plan(g, vt);
+    rows.resize(g.nrow > 0 ? g.nrow : 1);
+    std::vector<YV> yv(g.nrow > 0 ? g.nrow : 1);
+    int32_t ny = 0;
+    check(gbc_spmspv(context(), p, sr, xi.data(), xv.data(), (int32_t)xi.size(), rows.data(), yv.data(), &ny,
+                     GBC_HOST),
+          "gbc_spmspv");
+    rows.resize(ny);
+    vals.resize(ny);
+    for (int32_t k = 0; k < ny; ++k) vals[k] = static_cast<OVT>(yv[k]);
+}
+
+}  // namespace detail
+
+// Drop the device copies of every matrix multiplied so far (call after
+// changing a matrix in place).
+inline void forget_matrices()
+{
+    for (auto &e : detail::plan_cache()) gbc_spmspv_plan_destroy(e.second);
+    detail::plan_cache().clear();
+}
+
+// y = A x (SpImpl.h:115-124, the PreAllocatedSPA overload that reaches
+// SpMXSpV_Bucket): appended to indy / numy sorted by row.  Offloaded for
+// Select2ndMin (registered), boolean Select2nd and SelectMax (integer
+// vectors; A's values ignored) and PlusTimes (registered value type
+// throughout), with int64 indices; any m x n matrix.
 template <class SR, class IT, class NUM, class IVT, class OVT>
 void SpMXSpV(const combblas::Csc<IT, NUM> &Acsc, int32_t mA, const int32_t *indx, const IVT *numx, int32_t veclen,
              std::vector<int32_t> &indy, std::vector<OVT> &numy, combblas::PreAllocatedSPA<OVT> &SPA)
 {
-    constexpr bool gpu = semiring_of<SR>::sr == GBC_SR_SELECT2NDMIN && std::is_same<IT, int64_t>::value &&
-                         std::is_same<IVT, int64_t>::value && std::is_same<OVT, int64_t>::value;
-    if constexpr (!gpu) {
+    constexpr int vt = detail::spmspv_vt<SR, NUM, IVT, OVT>();
+    if constexpr (vt < 0 || !std::is_same<IT, int64_t>::value) {
         combblas::SpMXSpV<SR>(Acsc, mA, indx, numx, veclen, indy, numy, SPA);
     } else {
         gbc_matrix g{};
@@ -383,23 +517,55 @@ void SpMXSpV(const combblas::Csc<IT, NUM> &Acsc, int32_t mA, const int32_t *indx
         g.ncol = Acsc.n;
         g.nzc = Acsc.n;
         g.nnz = Acsc.nz;
-        g.cp = Acsc.jc;
+        g.cp = Acsc.jc;  // Csc::jc holds the column pointers
         g.ir = Acsc.ir;
-        g.num = nullptr;
+        g.num = vt == GBC_BOOL ? nullptr : static_cast<const void *>(Acsc.num);
         g.where = GBC_HOST;
-        if (mA != Acsc.n) throw std::runtime_error("gbcomb::SpMXSpV: the GPU path takes a square matrix");
-        gbc_graph *gr = nullptr;
-        detail::check(gbc_graph_create(detail::context(), &g, &gr), "gbc_graph_create");
-        const size_t base = indy.size();
-        indy.resize(base + mA);
-        numy.resize(base + mA);
-        int32_t ny = 0;
-        const int rc = gbc_spmspv_select2ndmin_i64(detail::context(), gr, indx, numx, veclen, indy.data() + base,
-                                                   numy.data() + base, &ny, GBC_HOST);
-        gbc_graph_destroy(gr);
-        detail::check(rc, "gbc_spmspv_select2ndmin_i64");
-        indy.resize(base + ny);
-        numy.resize(base + ny);
+        std::vector<int32_t> r;
+        std::vector<OVT> v;
+        detail::spmspv_run<SR>(g, vt, indx, numx, veclen, r, v);
+        indy.insert(indy.end(), r.begin(), r.end());
+        numy.insert(numy.end(), v.begin(), v.end());
+    }
+}
+
+// y = A x with the optbuf outputs (SpImpl.h:59-65 -> SpImpl.cpp:222-272, the
+// call of BFSFriends.h:207): entries split among p_c receivers by row
+// (owner = min(row / (mA / p_c), p_c - 1)), each receiver's rows ascending
+// and local to its offset; cnts[p] entries land at indy/numy + dspls[p].
+template <class SR, class IT, class NUM, class IVT, class OVT>
+void SpMXSpV(const combblas::Dcsc<IT, NUM> &Adcsc, int32_t mA, const int32_t *indx, const IVT *numx, int32_t veclen,
+             int32_t *indy, OVT *numy, int *cnts, int *dspls, int p_c)
+{
+    constexpr int vt = detail::spmspv_vt<SR, NUM, IVT, OVT>();
+    if constexpr (vt < 0 || !std::is_same<IT, int64_t>::value) {
+        combblas::SpMXSpV<SR>(Adcsc, mA, indx, numx, veclen, indy, numy, cnts, dspls, p_c);
+    } else {
+        gbc_matrix g{};
+        g.nrow = mA;
+        g.ncol = Adcsc.nzc > 0 ? Adcsc.jc[Adcsc.nzc - 1] + 1 : 0;
+        g.nzc = Adcsc.nzc;
+        g.nnz = Adcsc.nz;
+        g.cp = Adcsc.cp;
+        g.jc = Adcsc.jc;
+        g.ir = Adcsc.ir;
+        g.num = vt == GBC_BOOL ? nullptr : static_cast<const void *>(Adcsc.numx);
+        g.where = GBC_HOST;
+        std::vector<int32_t> r;
+        std::vector<OVT> v;
+        if (g.nnz > 0) detail::spmspv_run<SR>(g, vt, indx, numx, veclen, r, v);
+        const int32_t perproc = p_c > 0 ? mA / p_c : mA;
+        for (int p = 0; p < p_c; ++p) cnts[p] = 0;
+        size_t k = 0;
+        for (int p = 0; p < p_c; ++p) {
+            const int32_t offset = perproc * p;
+            while (k < r.size() && (p == p_c - 1 || perproc == 0 || r[k] / perproc <= p)) {
+                indy[dspls[p] + cnts[p]] = r[k] - offset;
+                numy[dspls[p] + cnts[p]] = v[k];
+                ++cnts[p];
+                ++k;
+            }
+        }
     }
 }
 

@@ -93,6 +93,9 @@ def _ref():
                                        C.c_float, C.c_int64, C.c_int64, C.c_float]
         lib.ref_num_threads.restype = C.c_int
         lib.ref_result_nnz.restype = C.c_int64
+        lib.ref_spmspv_sr.restype = C.c_int64
+        lib.ref_spmspv_sr.argtypes = [C.c_int, C.c_int, C.c_int64, C.c_int64, _P64, _P64, C.c_void_p, _P32,
+                                      C.c_void_p, C.c_int32]
         lib.ref_mcl_iterate.restype = C.c_int64
         lib.ref_mcl_iterate.argtypes = [C.c_int64, _P64, _P64, np.ctypeslib.ndpointer(dtype=np.float32), C.c_double,
                                         C.c_float, C.c_int64, C.c_int64, C.c_float, C.c_int64, C.c_int,
@@ -212,6 +215,9 @@ def _port():
         lib.gbc_o_result.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         lib.gbc_o_spmspv.restype = C.c_int64
         lib.gbc_o_spmspv.argtypes = [C.c_int64, _P64, _P64, _P32, _P64, C.c_int32, C.c_int]
+        lib.gbc_o_spmspv_sr.restype = C.c_int64
+        lib.gbc_o_spmspv_sr.argtypes = [C.c_int, C.c_int, C.c_int64, _P64, _P64, C.c_void_p, _P32, C.c_void_p,
+                                        C.c_int32]
         lib.gbc_o_bfs.restype = C.c_int
         lib.gbc_o_bfs.argtypes = [C.c_int64, _P64, _P64, C.c_int64, _P64, C.c_void_p]
         lib.gbc_o_mcl_select.restype = C.c_int64
@@ -275,6 +281,48 @@ def port_spgemm(A, B, sr: int, sorted: bool = True, want_counts: bool = False, f
     if want_counts:
         return (cp, rows, vals), (flop, cnt)
     return cp, rows, vals
+
+
+# SpMSpV semiring codes of ref_spmspv_sr / gbc_o_spmspv_sr
+SX_SELECTMIN, SX_SELECT2ND, SX_SELECTMAX, SX_PLUSTIMES = 0, 1, 2, 3
+_SX_VT = {np.float64: 0, np.float32: 1, np.int64: 2}
+
+
+def _sx_args(A, sx, indx, numx, dtype):
+    dt = np.int64 if sx != SX_PLUSTIMES else dtype
+    indx = np.ascontiguousarray(indx, np.int32)
+    numx = np.ascontiguousarray(numx, dt)
+    av = None
+    if sx == SX_PLUSTIMES:
+        av = np.ascontiguousarray(A.values if A.values is not None else np.ones(A.nnz), dt)
+    return dt, indx, numx, av
+
+
+def ref_spmspv_sr(A, sx: int, indx, numx, dtype=np.float64):
+    """The reference's own SpMXSpV over Select2nd (boolean optbuf path),
+    SelectMax or PlusTimes (SpMXSpV_Bucket).  Returns (rows, values)."""
+    lib = _ref()
+    dt, indx, numx, av = _sx_args(A, sx, indx, numx, dtype)
+    ny = lib.ref_spmspv_sr(sx, _SX_VT.get(dt, 2), A.nrow, A.ncol, np.ascontiguousarray(A.colptr),
+                           np.ascontiguousarray(A.rowidx), None if av is None else av.ctypes.data_as(C.c_void_p),
+                           indx, numx.ctypes.data_as(C.c_void_p), len(indx))
+    if ny < 0:
+        raise ValueError("bad semiring")
+    rows, _, vals = _fetch(lib, ny, dt, with_cols=False)
+    return rows, vals
+
+
+def port_spmspv_sr(A, sx: int, indx, numx, dtype=np.float64):
+    """The restatement (oracle.c gbc_o_spmspv_sr).  Returns (rows, values)."""
+    lib = _port()
+    dt, indx, numx, av = _sx_args(A, sx, indx, numx, dtype)
+    ny = lib.gbc_o_spmspv_sr(sx, _SX_VT.get(dt, 2), A.nrow, np.ascontiguousarray(A.colptr),
+                             np.ascontiguousarray(A.rowidx), None if av is None else av.ctypes.data_as(C.c_void_p),
+                             indx, numx.ctypes.data_as(C.c_void_p), len(indx))
+    rows = np.empty(ny, np.int64)
+    vals = np.empty(ny, dt)
+    lib.gbc_o_result(None, rows.ctypes.data_as(C.c_void_p), vals.ctypes.data_as(C.c_void_p))
+    return rows, vals
 
 
 def port_spmspv(A, indx, numx, buckets: int = 32):

@@ -17,16 +17,18 @@
  *   gbc_o_spmspv      SpMXSpV_Bucket (SpImpl.cpp:389-699): per-bucket row
  *                     split, SPA merge with the semiring add, sort of the
  *                     touched rows, output sorted by row.
+ *   gbc_o_spmspv_sr   the other SpMXSpV semirings (Select2nd, SelectMax,
+ *                     PlusTimes; SpImpl.cpp:167-328, 389-699)
  *   gbc_o_bfs         BFS_CSC level loop (SpMSpVBench.cpp:105-156) over
  *                     SelectMinSR (SpMSpVBench.cpp:79-100).
  *   gbc_o_mcl_select  MCLPruneRecoverySelect (recovery: gbc_o_mcl_select_recover)
- *   gbc_o_mcl_colscale / gbc_o_mcl_chaos / gbc_o_mcl_inflate
- *                     MakeColStochastic, Chaos, Inflate (Applications/MCL.cpp:389-449)
  *                     (ParFriends.h:185-354) and Kselect1
  *                     (SpParMat.cpp:1191-1300): prune <= thr for the
  *                     statistics, select columns whose pruned nnz > k, kth =
  *                     k-th largest of the unpruned column, then remove < kth
  *                     there and < thr elsewhere (PruneColumn with std::less).
+ *   gbc_o_mcl_colscale / gbc_o_mcl_chaos / gbc_o_mcl_inflate
+ *                     MakeColStochastic, Chaos, Inflate (Applications/MCL.cpp:389-449)
  */
 #include <limits.h>
 #include <math.h>
@@ -488,6 +490,69 @@ int64_t gbc_o_spmspv(int64_t m, const int64_t *Acp, const int64_t *Ari, const in
     free(nz);
     free(nzcnt);
     free(bcnt);
+    return ny;
+}
+
+/* y = A x over the other SpMXSpV semirings (SpImpl.h:49-142).  Every
+ * variant visits the vector's columns in the vector's (ascending) order and,
+ * per row, stores the first product and folds later ones in with the add
+ * (the SPA of SpMXSpV_Bucket, SpImpl.cpp:389-699, and of the boolean loops,
+ * SpImpl.cpp:167-328); rows come out ascending.  sx: 0 SelectMin (add min,
+ * multiply returns x), 1 Select2nd (add keeps the second argument), 2
+ * SelectMax (add max), 3 PlusTimes (multiply A*x, add +).  Values: int64 for
+ * 0-2; for 3 vt 0 double, 1 float, 2 int64 (matrix and vector alike).
+ * Returns nnz(y); rows and values in the result buffers. */
+int64_t gbc_o_spmspv_sr(int sx, int vt, int64_t m, const int64_t *Acp, const int64_t *Ari, const void *Av,
+                        const int32_t *indx, const void *numx, int32_t veclen)
+{
+    const size_t vs = sx == 3 && vt == 1 ? 4 : 8;
+    char *spa = (char *)malloc((size_t)(m > 0 ? m : 1) * vs);
+    uint8_t *seen = (uint8_t *)calloc((size_t)(m > 0 ? m : 1), 1);
+    int32_t *nz = (int32_t *)malloc((size_t)(m > 0 ? m : 1) * sizeof(int32_t));
+    int64_t ny = 0;
+    for (int32_t f = 0; f < veclen; ++f) {
+        const int64_t c = indx[f];
+        for (int64_t p = Acp[c]; p < Acp[c + 1]; ++p) {
+            const int64_t r = Ari[p];
+            const int first = !seen[r];
+            if (first) {
+                seen[r] = 1;
+                nz[ny++] = (int32_t)r;
+            }
+            if (sx == 3 && vt == 0) {
+                const double v = ((const double *)Av)[p] * ((const double *)numx)[f];
+                double *y = (double *)spa + r;
+                *y = first ? v : *y + v;
+            } else if (sx == 3 && vt == 1) {
+                const float v = ((const float *)Av)[p] * ((const float *)numx)[f];
+                float *y = (float *)spa + r;
+                *y = first ? v : *y + v;
+            } else {
+                const int64_t v = sx == 3 ? ((const int64_t *)Av)[p] * ((const int64_t *)numx)[f]
+                                          : ((const int64_t *)numx)[f];
+                int64_t *y = (int64_t *)spa + r;
+                if (first)
+                    *y = v;
+                else if (sx == 0)
+                    *y = v < *y ? v : *y;
+                else if (sx == 1)
+                    *y = v;
+                else if (sx == 2)
+                    *y = v > *y ? v : *y;
+                else
+                    *y = *y + v;
+            }
+        }
+    }
+    qsort(nz, (size_t)ny, sizeof(int32_t), cmp_i32);
+    result_reset(0, ny, vs);
+    for (int64_t i = 0; i < ny; ++i) {
+        g_rows[i] = nz[i];
+        memcpy((char *)g_vals + i * vs, spa + (size_t)nz[i] * vs, vs);
+    }
+    free(spa);
+    free(seen);
+    free(nz);
     return ny;
 }
 

@@ -12,6 +12,10 @@
 //   ref_colstats         -> estimateFLOP (mtSpGEMM.h:1057),
 //                           estimateNNZ_Hash (mtSpGEMM.h:806)
 //   ref_spmspv_bucket    -> SpMXSpV_Bucket (SpImpl.cpp:389)
+//   ref_spmspv_sr        -> boolean SpMXSpV over Select2ndSRing with the
+//                           optbuf outputs (SpImpl.cpp:222-272, TopDownBFS's
+//                           path), SpMXSpV_Bucket over SelectMaxSRing and
+//                           PlusTimesSRing (SpImpl.cpp:389-699)
 //   ref_bfs_selectmin    -> the BFS_CSC level loop of
 //                           Applications/SpMSpV-IPDPS2017/SpMSpVBench.cpp:105-156
 //   ref_mcl_expand       -> MemEfficientSpGEMM + MCLPruneRecoverySelect
@@ -231,6 +235,24 @@ int run_spmv(int64_t m, int64_t n, const int64_t *cp, const int64_t *ri, const v
 
 }  // namespace
 
+template <typename SR, typename NT, typename VT>
+static int64_t spmspv_bucket(int64_t m, int64_t n, const int64_t *Acp, const int64_t *Ari, const void *Av,
+                             const int32_t *indx, const VT *numx, int32_t veclen)
+{
+    std::unique_ptr<SpCCols<int64_t, NT>> A(make_csc<NT>(m, n, Acp, Ari, Av));
+    PreAllocatedSPA<VT> SPA(*A, 32);
+    std::vector<int32_t> indy;
+    std::vector<VT> numy;
+    double t0 = now();
+    SpMXSpV_Bucket<SR>(*A->GetCSC(), (int32_t)m, indx, numx, veclen, indy, numy, SPA);
+    g_res.seconds = now() - t0;
+    g_res.rows.assign(indy.begin(), indy.end());
+    g_res.cols.clear();
+    g_res.vals.resize(numy.size() * sizeof(VT));
+    std::memcpy(g_res.vals.data(), numy.data(), numy.size() * sizeof(VT));
+    return (int64_t)indy.size();
+}
+
 extern "C" {
 
 // Semiring codes: 0 PlusTimes<double>, 1 PlusTimes<float>, 2 PlusTimes<int64>,
@@ -337,6 +359,46 @@ int64_t ref_spmspv_bucket(int64_t m, int64_t n, const int64_t *Acp, const int64_
     g_res.vals.resize(numy.size() * sizeof(int64_t));
     std::memcpy(g_res.vals.data(), numy.data(), numy.size() * sizeof(int64_t));
     return (int64_t)indy.size();
+}
+
+// y = A x over the other SpMXSpV semirings: sx 1 Select2ndSRing<bool,int64,
+// int64> through the boolean DCSC SpMXSpV with the optbuf outputs and one
+// receiver (what TopDownBFS's LocalSpMV calls, BFSFriends.h:198-207); sx 2
+// SelectMaxSRing<bool,int64> and sx 3 PlusTimesSRing (vt 0 double, 1 float,
+// 2 int64) through SpMXSpV_Bucket.  Result in g_res.rows / g_res.vals.
+int64_t ref_spmspv_sr(int sx, int vt, int64_t m, int64_t n, const int64_t *Acp, const int64_t *Ari, const void *Av,
+                      const int32_t *indx, const void *numx, int32_t veclen)
+{
+    if (sx == 1) {
+        std::unique_ptr<SpDCCols<int64_t, bool>> A(make_dcsc<bool>(m, n, Acp, Ari, nullptr));
+        std::vector<int32_t> indy(m > 0 ? m : 1);
+        std::vector<int64_t> numy(m > 0 ? m : 1);
+        int cnts[1] = {0}, dspls[1] = {0};
+        double t0 = now();
+        if (A->getnnz() > 0 && veclen > 0)
+            SpMXSpV<Select2ndSRing<bool, int64_t, int64_t>>(*A->GetDCSC(), (int32_t)m, indx,
+                                                             static_cast<const int64_t *>(numx), veclen, indy.data(),
+                                                             numy.data(), cnts, dspls, 1);
+        g_res.seconds = now() - t0;
+        g_res.rows.assign(indy.begin(), indy.begin() + cnts[0]);
+        g_res.cols.clear();
+        g_res.vals.resize(cnts[0] * sizeof(int64_t));
+        std::memcpy(g_res.vals.data(), numy.data(), cnts[0] * sizeof(int64_t));
+        return cnts[0];
+    }
+    if (sx == 2)
+        return spmspv_bucket<SelectMaxSRing<bool, int64_t>, bool, int64_t>(m, n, Acp, Ari, nullptr, indx,
+                                                                           static_cast<const int64_t *>(numx), veclen);
+    if (sx == 3 && vt == 0)
+        return spmspv_bucket<PlusTimesSRing<double, double>, double, double>(m, n, Acp, Ari, Av, indx,
+                                                                            static_cast<const double *>(numx), veclen);
+    if (sx == 3 && vt == 1)
+        return spmspv_bucket<PlusTimesSRing<float, float>, float, float>(m, n, Acp, Ari, Av, indx,
+                                                                        static_cast<const float *>(numx), veclen);
+    if (sx == 3 && vt == 2)
+        return spmspv_bucket<PlusTimesSRing<int64_t, int64_t>, int64_t, int64_t>(
+            m, n, Acp, Ari, Av, indx, static_cast<const int64_t *>(numx), veclen);
+    return -1;
 }
 
 // BFS from `source` over the symmetric pattern A, as the BFS_CSC loop of

@@ -25,6 +25,18 @@ struct MinPlusSRing {
     static T1 multiply(const T1 &a, const T2 &b) { return a + b; }
 };
 
+template <class T1, class T2, class OUT>
+struct Select2ndSRing {
+    static OUT add(const OUT &, const OUT &b) { return b; }
+    static OUT multiply(const T1 &, const T2 &b) { return static_cast<OUT>(b); }
+};
+template <class T1, class T2>
+struct SelectMaxSRing {
+    typedef T2 T_promote;
+    static T2 add(const T2 &a, const T2 &b) { return std::max(a, b); }
+    static T2 multiply(const T1 &, const T2 &b) { return b; }
+};
+
 template <class IT, class NT>
 struct Dcsc {
     IT *cp = nullptr, *jc = nullptr, *ir = nullptr;
@@ -221,6 +233,12 @@ SpTuples<IT, NT> *MultiwayMerge(std::vector<SpTuples<IT, NT> *> &L, IT mdim = 0,
 template <class SR, class IT, class NUM, class IVT, class OVT>
 void SpMXSpV(const Csc<IT, NUM> &, int32_t, const int32_t *, const IVT *, int32_t, std::vector<int32_t> &,
              std::vector<OVT> &, PreAllocatedSPA<OVT> &)
+{
+    ++fallback_calls();
+}
+template <class SR, class IT, class NUM, class IVT, class OVT>
+void SpMXSpV(const Dcsc<IT, NUM> &, int32_t, const int32_t *, const IVT *, int32_t, int32_t *, OVT *, int *, int *,
+             int)
 {
     ++fallback_calls();
 }

@@ -201,6 +201,117 @@ int main()
             ++k;
         }
     }
+    // 7b. the other SpMXSpV semirings on a rectangular matrix (300 x 900):
+    // SelectMax and PlusTimes through the Csc overload, Select2nd through the
+    // Dcsc optbuf overload with three receivers; one device copy per matrix
+    {
+        std::mt19937_64 rng(77);
+        const I m = 300, n = 900;
+        std::vector<I> cp{0}, ir, jc, dcp{0};
+        std::vector<double> val;
+        std::vector<bool> dummy;
+        for (I j = 0; j < n; ++j) {
+            std::vector<I> rows;
+            if (j % 3 != 1)
+                for (I r = 0; r < m; ++r)
+                    if (rng() % 100 < 3) rows.push_back(r);
+            for (I r : rows) {
+                ir.push_back(r);
+                val.push_back(double(rng() % 2000) / 1000.0 - 1.0);
+            }
+            cp.push_back((I)ir.size());
+            if (!rows.empty()) {
+                jc.push_back(j);
+                dcp.push_back((I)ir.size());
+            }
+        }
+        Csc<I, double> csc;
+        csc.jc = cp.data();
+        csc.ir = ir.data();
+        csc.num = val.data();
+        csc.n = n;
+        csc.nz = (I)ir.size();
+        std::vector<int32_t> indx;
+        std::vector<int64_t> xi;
+        std::vector<double> xd;
+        for (int32_t c = 0; c < n; c += 1 + (int32_t)(rng() % 5)) {
+            indx.push_back(c);
+            xi.push_back((int64_t)(rng() % 100000) - 50000);
+            xd.push_back(double(rng() % 1000) / 997.0);
+        }
+        // CPU expectations: ascending columns, first stored, later folded
+        std::map<I, int64_t> emax, elast;
+        std::map<I, double> esum;
+        for (size_t t = 0; t < indx.size(); ++t)
+            for (I p = cp[indx[t]]; p < cp[indx[t] + 1]; ++p) {
+                const I r = ir[p];
+                const double prod = val[p] * xd[t];
+                if (!emax.count(r)) {
+                    emax[r] = xi[t];
+                    esum[r] = prod;
+                } else {
+                    emax[r] = std::max(emax[r], xi[t]);
+                    esum[r] = esum[r] + prod;
+                }
+                elast[r] = xi[t];
+            }
+        typedef SelectMaxSRing<bool, int64_t> SMAX;
+        typedef Select2ndSRing<bool, int64_t, int64_t> S2ND;
+        Csc<I, bool> bcsc;
+        std::unique_ptr<bool[]> bv(new bool[ir.size() + 1]);
+        bcsc.jc = cp.data();
+        bcsc.ir = ir.data();
+        bcsc.num = bv.get();
+        bcsc.n = n;
+        bcsc.nz = (I)ir.size();
+        const int fb = fallback_calls();
+        const long long builds = gbcomb::detail::plan_builds();
+        PreAllocatedSPA<int64_t> spa;
+        for (int rep = 0; rep < 2; ++rep) {
+            std::vector<int32_t> indy;
+            std::vector<int64_t> numy;
+            gbcomb::SpMXSpV<SMAX>(bcsc, (int32_t)m, indx.data(), xi.data(), (int32_t)indx.size(), indy, numy, spa);
+            EXPECT(indy.size() == emax.size());
+            size_t k = 0;
+            for (auto &e : emax) {
+                EXPECT(k < indy.size() && indy[k] == e.first && numy[k] == e.second);
+                ++k;
+            }
+        }
+        EXPECT(gbcomb::detail::plan_builds() == builds + 1);  // the second call reused the device copy
+        PreAllocatedSPA<double> dspa;
+        std::vector<int32_t> indy;
+        std::vector<double> numy;
+        gbcomb::SpMXSpV<PT>(csc, (int32_t)m, indx.data(), xd.data(), (int32_t)indx.size(), indy, numy, dspa);
+        EXPECT(indy.size() == esum.size());
+        size_t k = 0;
+        for (auto &e : esum) {
+            EXPECT(k < indy.size() && indy[k] == e.first && numy[k] == e.second);
+            ++k;
+        }
+        Dcsc<I, bool> d;
+        d.cp = dcp.data();
+        d.jc = jc.data();
+        d.ir = ir.data();
+        d.numx = bv.get();
+        d.nz = (I)ir.size();
+        d.nzc = (I)jc.size();
+        std::vector<int32_t> oind(m);
+        std::vector<int64_t> onum(m);
+        int cnts[3], dspls[3] = {0, 100, 200};
+        gbcomb::SpMXSpV<S2ND>(d, (int32_t)m, indx.data(), xi.data(), (int32_t)indx.size(), oind.data(), onum.data(),
+                              cnts, dspls, 3);
+        int got[3] = {0, 0, 0};
+        for (auto &e : elast) {
+            const int p = std::min((int)(e.first / (m / 3)), 2);
+            const int q = dspls[p] + got[p]++;
+            EXPECT(q < m && oind[q] == e.first - (m / 3) * p && onum[q] == e.second);
+        }
+        EXPECT(cnts[0] == got[0] && cnts[1] == got[1] && cnts[2] == got[2]);
+        EXPECT(fallback_calls() == fb);
+        gbcomb::forget_matrices();
+        EXPECT(gbcomb::detail::plan_cache().empty());
+    }
     // 8. MultiwayMerge of three products of one shape (GPU) against the CPU merge
     {
         SpDCCols<I, double> *X = random_dcsc<double>(600, 300, 0.02, 0.1, 8);

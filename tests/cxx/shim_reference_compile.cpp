@@ -51,6 +51,21 @@ template void gbcomb::SpMXSpV<S2M, int64_t, int64_t, int64_t, int64_t>(
     const Csc<int64_t, int64_t> &, int32_t, const int32_t *, const int64_t *, int32_t, std::vector<int32_t> &,
     std::vector<int64_t> &, PreAllocatedSPA<int64_t> &);
 
+// the other SpMXSpV semirings: boolean Select2nd through the optbuf Dcsc
+// overload (TopDownBFS), SelectMax and PlusTimes through the Csc overload
+typedef Select2ndSRing<bool, int64_t, int64_t> S2ND;
+typedef SelectMaxSRing<bool, int64_t> SMAX;
+template void gbcomb::SpMXSpV<S2ND, int64_t, bool, int64_t, int64_t>(const Dcsc<int64_t, bool> &, int32_t,
+                                                                     const int32_t *, const int64_t *, int32_t,
+                                                                     int32_t *, int64_t *, int *, int *, int);
+template void gbcomb::SpMXSpV<SMAX, int64_t, bool, int64_t, int64_t>(
+    const Csc<int64_t, bool> &, int32_t, const int32_t *, const int64_t *, int32_t, std::vector<int32_t> &,
+    std::vector<int64_t> &, PreAllocatedSPA<int64_t> &);
+// fall-through: 32-bit indices
+template void gbcomb::SpMXSpV<S2ND, int32_t, bool, int64_t, int64_t>(const Dcsc<int32_t, bool> &, int32_t,
+                                                                     const int32_t *, const int64_t *, int32_t,
+                                                                     int32_t *, int64_t *, int *, int *, int);
+
 template SpTuples<int64_t, double> *gbcomb::MultiwayMerge<PTD, int64_t, double>(
     std::vector<SpTuples<int64_t, double> *> &, int64_t, int64_t, bool);
 template SpTuples<int32_t, double> *gbcomb::MultiwayMerge<PTD, int32_t, double>(

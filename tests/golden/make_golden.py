@@ -155,6 +155,23 @@ def main(ref_root: str):
     d["spmspv/rmat8/x_val"] = xv
     d["spmspv/rmat8/y_ind"] = yr
     d["spmspv/rmat8/y_val"] = yv
+    # the other SpMXSpV semirings on a rectangular 1500 x 1000 matrix
+    rng = np.random.default_rng(12)
+    R = G.csc_from_coo(1500, 1000, rng.integers(0, 1500, 12000), rng.integers(0, 1000, 12000),
+                       rng.random(12000) * 2 - 1)
+    put_mat(d, "in/rect1500", R)
+    x = np.sort(rng.choice(1000, 120, replace=False)).astype(np.int32)
+    d["spmspvsr/x_ind"] = x
+    d["spmspvsr/x_i64"] = rng.integers(-1000, 1000, 120).astype(np.int64)
+    d["spmspvsr/x_f64"] = rng.random(120) * 2 - 1
+    for sx in (O.SX_SELECT2ND, O.SX_SELECTMAX):
+        d[f"spmspvsr/{sx}/y_ind"], d[f"spmspvsr/{sx}/y_val"] = O.ref_spmspv_sr(R, sx, x, d["spmspvsr/x_i64"])
+    for dt in (np.float64, np.float32):
+        d[f"spmspvsr/3/{np.dtype(dt).name}/y_ind"], d[f"spmspvsr/3/{np.dtype(dt).name}/y_val"] = O.ref_spmspv_sr(
+            R.with_values(R.values.astype(dt)), O.SX_PLUSTIMES, x, d["spmspvsr/x_f64"].astype(dt), dt)
+    Ri = R.with_values(np.round(R.values * 100).astype(np.int64))
+    d["spmspvsr/3/int64/y_ind"], d["spmspvsr/3/int64/y_val"] = O.ref_spmspv_sr(Ri, O.SX_PLUSTIMES, x,
+                                                                                d["spmspvsr/x_i64"], np.int64)
     # multi-source BFS (MD.cpp's Select2ndMin SpGEMM loop) on rmat8 and torus
     for name, Mm in (("rmat8", rm), ("torus", torus)):
         P = Mm.with_values(None)

@@ -122,6 +122,26 @@ def test_port_mcl(oracle_lib, golden):
         assert np.array_equal(scp, gcp) and np.array_equal(srows, grows) and np.array_equal(svals, gvals)
 
 
+def test_port_spmspv_semirings(oracle_lib, golden):
+    """Select2nd (boolean optbuf path), SelectMax and PlusTimes SpMXSpV
+    restated, against the reference's own output on a rectangular matrix."""
+    O = oracle_lib
+    R = golden_matrix(golden, "rect1500")
+    x = golden["spmspvsr/x_ind"]
+    for sx in (O.SX_SELECT2ND, O.SX_SELECTMAX):
+        r, v = O.port_spmspv_sr(R, sx, x, golden["spmspvsr/x_i64"])
+        assert np.array_equal(r, golden[f"spmspvsr/{sx}/y_ind"]) and np.array_equal(v, golden[f"spmspvsr/{sx}/y_val"])
+    for dt in (np.float64, np.float32):
+        name = np.dtype(dt).name
+        r, v = O.port_spmspv_sr(R.with_values(R.values.astype(dt)), O.SX_PLUSTIMES, x,
+                                golden["spmspvsr/x_f64"].astype(dt), dt)
+        assert np.array_equal(r, golden[f"spmspvsr/3/{name}/y_ind"])
+        assert np.array_equal(v, golden[f"spmspvsr/3/{name}/y_val"])
+    Ri = R.with_values(np.round(R.values * 100).astype(np.int64))
+    r, v = O.port_spmspv_sr(Ri, O.SX_PLUSTIMES, x, golden["spmspvsr/x_i64"], np.int64)
+    assert np.array_equal(r, golden["spmspvsr/3/int64/y_ind"]) and np.array_equal(v, golden["spmspvsr/3/int64/y_val"])
+
+
 MCL_RECOVERY = ((1e-2, 30, 40, 0.9), (5e-3, 20, 30, 0.95), (2e-2, 10, 25, 0.8), (3e-2, 5, 12, 0.9))
 
 
