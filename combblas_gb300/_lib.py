@@ -72,12 +72,14 @@ class gbc_phased_stats(C.Structure):
 class gbc_bfs_stats(C.Structure):
     _fields_ = [
         ("iterations", C.c_int64), ("reached", C.c_int64), ("edges", C.c_int64), ("ms", C.c_double),
+        ("host_checks", C.c_int64),
     ]
 
 
 class gbc_msbfs_stats(C.Structure):
     _fields_ = [
         ("levels", C.c_int64), ("reached", C.c_int64), ("edges", C.c_int64), ("ms", C.c_double),
+        ("host_checks", C.c_int64),
     ]
 
 

@@ -43,7 +43,10 @@ struct Graph {
     int64_t *h_ctl = nullptr;  // pinned mirror
     cudaGraphExec_t level_exec = nullptr;
     long long level_kernels = 0;  // kernels one replay of the level graph runs
+    cudaGraphExec_t loop_exec = nullptr;  // the whole traversal: a while node around one level
+    long long loop_kernels = 0;           // kernels of one trip of its body
     int64_t *g_parents = nullptr, *g_levels = nullptr;  // pointers baked into the graph
+    int64_t *own_parents = nullptr, *own_levels = nullptr;  // device outputs of host-array calls
     bool bfs_ready = false;
     int policy = 0;  // direction policy (see gbc_graph_set_policy)
     // multi-source BFS state, sized for ms_roots roots (allocated on use)
@@ -55,6 +58,8 @@ struct Graph {
     int64_t *h_ms_ctl = nullptr;      // pinned mirror
     cudaGraphExec_t ms_exec = nullptr;
     long long ms_kernels = 0;
+    cudaGraphExec_t ms_loop_exec = nullptr;
+    long long ms_loop_kernels = 0;
     int64_t *ms_g_parents = nullptr;  // parents pointer baked into ms_exec
 };
 
@@ -586,6 +591,57 @@ __global__ void k_bfs_init2(int64_t n, int64_t nnz, int64_t *levels, int64_t sou
     ctl[CTL_E] = 0;
 }
 
+// Condition of a traversal's while node: another level while the frontier
+// is nonempty, at most `cap` levels (a level loop over n vertices ends
+// within n + 1 levels, so the cap never cuts a traversal short).
+__global__ void k_loop_cond(const int64_t *nf, const int64_t *level, int64_t cap, cudaGraphConditionalHandle h)
+{
+    cudaGraphSetConditional(h, (*nf != 0 && *level < cap) ? 1u : 0u);
+}
+
+// An executable graph of one while node whose body is what `body` launches
+// on the capturing stream, followed by the condition kernel.  The whole
+// traversal then runs from one graph launch with no host round trip.
+template <class F>
+static int loop_graph(F body, const int64_t *nf, const int64_t *level, int64_t cap, cudaGraphExec_t *exec,
+                      long long *kernels)
+{
+    cudaGraph_t graph = nullptr;
+    GBC_CUDA_TRY(cudaGraphCreate(&graph, 0));
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (e == cudaSuccess) e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np);
+    cudaStream_t cs = nullptr;
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    cudaGraph_t bodyg = e == cudaSuccess ? np.conditional.phGraph_out[0] : nullptr;
+    if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(cs, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    int rc = GBC_OK;
+    if (e == cudaSuccess) {
+        const long long c0 = launch_count();
+        rc = body(cs);
+        k_loop_cond<<<1, 1, 0, cs>>>(nf, level, cap, h);
+        note_launch();
+        *kernels = launch_count() - c0;
+        note_launches(-*kernels);  // captured, not run
+        e = cudaStreamEndCapture(cs, &bodyg);
+    }
+    if (cs) cudaStreamDestroy(cs);
+    if (e == cudaSuccess && rc == GBC_OK) e = cudaGraphInstantiate(exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (rc != GBC_OK) return rc;
+    if (e != cudaSuccess) {
+        *exec = nullptr;
+        cudaGetLastError();
+        return fail(GBC_ECUDA, std::string("traversal graph: ") + cudaGetErrorString(e));
+    }
+    return GBC_OK;
+}
+
 // -------------------------------------------------------------- host side
 static int graph_alloc_bfs(Graph *g)
 {
@@ -601,6 +657,8 @@ static int graph_alloc_bfs(Graph *g)
     GBC_TRY(device_alloc(ctx, (void **)&g->off, (g->n + 2) * sizeof(int64_t)));
     GBC_TRY(device_alloc(ctx, (void **)&g->tile, ((g->n + kScanTile - 1) / kScanTile + 2) * sizeof(int64_t)));
     GBC_TRY(device_alloc(ctx, (void **)&g->ctl, (kCtlWords + 8) * sizeof(int64_t)));
+    GBC_TRY(device_alloc(ctx, (void **)&g->own_parents, (g->n + 1) * sizeof(int64_t)));
+    GBC_TRY(device_alloc(ctx, (void **)&g->own_levels, (g->n + 1) * sizeof(int64_t)));
     GBC_CUDA_TRY(cudaMallocHost(&g->h_ctl, (kCtlWords + 8) * sizeof(int64_t)));
     // pointer tables after the control words: fronts[2], fbits[2]
     void *tab[4] = {g->front[0], g->front[1], g->fbits[0], g->fbits[1]};
@@ -664,6 +722,13 @@ static int level_graph(Graph *g, int64_t *parents, int64_t *levels)
     if (e != cudaSuccess) return fail(GBC_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
     g->g_parents = parents;
     g->g_levels = levels;
+    if (g->loop_exec) cudaGraphExecDestroy(g->loop_exec);
+    g->loop_exec = nullptr;
+    // the whole traversal as one while node (replays of the level graph with
+    // a host check every few levels remain the path where the driver cannot
+    // build conditional nodes)
+    loop_graph([&](cudaStream_t cs) { return launch_level(g, parents, levels, cs); }, g->ctl + CTL_NF,
+               g->ctl + CTL_ITER, g->n + 2, &g->loop_exec, &g->loop_kernels);
     return GBC_OK;
 }
 
@@ -682,10 +747,17 @@ static int bfs_device(Graph *g, int64_t source, int64_t *parents, int64_t *level
     note_launches(2);
     GBC_CUDA_TRY(cudaGetLastError());
     if (use_graph) GBC_TRY(level_graph(g, parents, levels));
-    // Levels are replayed in batches; a finished BFS leaves nf == 0 and the
-    // remaining replays of the batch are empty launches.
+    if (use_graph && g->loop_exec) {
+        GBC_CUDA_TRY(cudaGraphLaunch(g->loop_exec, s));
+        GBC_CUDA_TRY(cudaMemcpyAsync(g->h_ctl, g->ctl, kCtlWords * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        GBC_CUDA_TRY(cudaStreamSynchronize(s));
+        note_launches(g->loop_kernels * std::max<int64_t>(g->h_ctl[CTL_ITER], 1));
+    }
+    // Otherwise levels are replayed in batches; a finished BFS leaves nf == 0
+    // and the remaining replays of the batch are empty launches.
     const int batch = 4;
-    for (int64_t lvl = 0; lvl <= g->n + 1; lvl += batch) {
+    int64_t checks = 0;
+    for (int64_t lvl = 0; !(use_graph && g->loop_exec) && lvl <= g->n + 1; lvl += batch, ++checks) {
         for (int k = 0; k < batch; ++k) {
             if (use_graph) {
                 GBC_CUDA_TRY(cudaGraphLaunch(g->level_exec, s));
@@ -707,6 +779,7 @@ static int bfs_device(Graph *g, int64_t source, int64_t *parents, int64_t *level
         st->reached = g->h_ctl[CTL_REACHED];
         st->edges = g->h_ctl[CTL_EDGES] / 2;
         st->ms = ms;
+        st->host_checks = checks;
     }
     return GBC_OK;
 }
@@ -893,6 +966,8 @@ static void ms_free(Graph *g)
     Context *c = g->ctx;
     if (g->ms_exec) cudaGraphExecDestroy(g->ms_exec);
     g->ms_exec = nullptr;
+    if (g->ms_loop_exec) cudaGraphExecDestroy(g->ms_loop_exec);
+    g->ms_loop_exec = nullptr;
     device_free(c, g->ms_cand);
     device_free(c, g->ms_visited);
     device_free(c, g->ms_front[0]);
@@ -970,6 +1045,10 @@ static int ms_level_graph(Graph *g, int64_t *parents)
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return fail(GBC_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
     g->ms_g_parents = parents;
+    if (g->ms_loop_exec) cudaGraphExecDestroy(g->ms_loop_exec);
+    g->ms_loop_exec = nullptr;
+    loop_graph([&](cudaStream_t cs) { return ms_launch_level(g, parents, cs); }, g->ms_ctl + MS_NF,
+               g->ms_ctl + MS_LEVEL, g->n + 2, &g->ms_loop_exec, &g->ms_loop_kernels);
     return GBC_OK;
 }
 
@@ -991,8 +1070,16 @@ static int msbfs_device(Graph *g, const int64_t *d_roots, int64_t nroots, int64_
     GBC_CUDA_TRY(cudaMemcpyAsync(g->ms_ctl + MS_NF, &nf, sizeof(int64_t), cudaMemcpyHostToDevice, s));
     GBC_CUDA_TRY(cudaGetLastError());
     GBC_TRY(ms_level_graph(g, parents));
+    if (g->ms_loop_exec) {
+        GBC_CUDA_TRY(cudaGraphLaunch(g->ms_loop_exec, s));
+        GBC_CUDA_TRY(
+            cudaMemcpyAsync(g->h_ms_ctl, g->ms_ctl, kMsCtlWords * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        GBC_CUDA_TRY(cudaStreamSynchronize(s));
+        note_launches(g->ms_loop_kernels * std::max<int64_t>(g->h_ms_ctl[MS_LEVEL], 1));
+    }
     const int batch = 2;
-    for (int64_t lvl = 0; lvl <= g->n + 1; lvl += batch) {
+    int64_t checks = 0;
+    for (int64_t lvl = 0; !g->ms_loop_exec && lvl <= g->n + 1; lvl += batch, ++checks) {
         for (int k = 0; k < batch; ++k) {
             GBC_CUDA_TRY(cudaGraphLaunch(g->ms_exec, s));
             note_launches(g->ms_kernels);
@@ -1011,6 +1098,7 @@ static int msbfs_device(Graph *g, const int64_t *d_roots, int64_t nroots, int64_
         st->reached = g->h_ms_ctl[MS_REACHED];
         st->edges = g->h_ms_ctl[MS_EDGES] / 2;
         st->ms = ms;
+        st->host_checks = checks;
     }
     return GBC_OK;
 }
@@ -1071,6 +1159,7 @@ int gbc_graph_destroy(gbc_graph *g)
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     if (g->level_exec) cudaGraphExecDestroy(g->level_exec);
+    if (g->loop_exec) cudaGraphExecDestroy(g->loop_exec);
     ms_free(g);
     device_free(c, g->cp);
     device_free(c, g->cp32);
@@ -1084,6 +1173,8 @@ int gbc_graph_destroy(gbc_graph *g)
     device_free(c, g->off);
     device_free(c, g->tile);
     device_free(c, g->ctl);
+    device_free(c, g->own_parents);
+    device_free(c, g->own_levels);
     if (g->h_ctl) cudaFreeHost(g->h_ctl);
     cudaStreamSynchronize(c->stream);
     delete g;
@@ -1171,11 +1262,15 @@ int gbc_bfs(gbc_context *ctx, gbc_graph *g, int64_t source, int64_t *parents, in
     if (source < 0 || source >= g->n) return fail(GBC_EINVAL, "source out of range");
     GBC_CUDA_TRY(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
+    g->ctx = ctx;
+    GBC_TRY(graph_alloc_bfs(g));
     int64_t *dp = parents, *dl = levels;
-    Workspace ws(ctx);
-    if (where == GBC_HOST || !parents) GBC_TRY(ws.alloc_n(&dp, g->n));
-    if (where == GBC_HOST || !levels) GBC_TRY(ws.alloc_n(&dl, g->n));
-    GBC_TRY(bfs_device(g, source, dp, dl, st, where == GBC_DEVICE && parents && levels));
+    if (where == GBC_HOST || !parents || !levels) {
+        // the graph's own device outputs: the captured traversal is reused
+        dp = g->own_parents;
+        dl = g->own_levels;
+    }
+    GBC_TRY(bfs_device(g, source, dp, dl, st, true));
     if (where == GBC_HOST) {
         if (parents) GBC_CUDA_TRY(cudaMemcpyAsync(parents, dp, g->n * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
         if (levels) GBC_CUDA_TRY(cudaMemcpyAsync(levels, dl, g->n * sizeof(int64_t), cudaMemcpyDeviceToHost, s));

@@ -321,6 +321,8 @@ typedef struct {
     int64_t reached;    /* vertices with a parent, plus the source */
     int64_t edges;      /* undirected edges of the reached vertices: sum(deg)/2 */
     double ms;          /* device time of the BFS */
+    int64_t host_checks; /* host round trips inside the level loop: 0 when the
+                            whole traversal ran as one graph (a while node) */
 } gbc_bfs_stats;
 
 int gbc_graph_create(gbc_context *ctx, const gbc_matrix *A, gbc_graph **g);
@@ -389,6 +391,7 @@ typedef struct {
     int64_t reached;  /* reached (root, vertex) pairs, roots included */
     int64_t edges;    /* sum over roots of undirected edges of the reached vertices */
     double ms;        /* device time */
+    int64_t host_checks; /* host round trips inside the level loop (0: one graph) */
 } gbc_msbfs_stats;
 
 int gbc_msbfs(gbc_context *ctx, gbc_graph *g, const int64_t *roots, int64_t nroots, int64_t *parents, int where,

@@ -33,6 +33,7 @@ def test_bfs_rmat_vs_oracle(gpu_ctx, oracle_lib, scale, ef):
         epar, elev, eit = O.port_bfs(A, int(s))
         assert np.array_equal(par, epar) and np.array_equal(lev, elev)
         assert st.iterations == eit
+        assert st.host_checks == 0  # the whole traversal ran as one graph (while node)
         reached = (par >= 0) | (np.arange(A.ncol) == s)
         assert st.reached == reached.sum()
         assert st.edges == deg[reached].sum() // 2

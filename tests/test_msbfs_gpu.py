@@ -30,6 +30,7 @@ def test_msbfs_rmat_vs_oracle(gpu_ctx, oracle_lib, scale, ef, nroots):
     par, st = B.msbfs(g, roots)
     ref, levels = O.port_msbfs(A, roots)
     assert np.array_equal(par, ref)
+    assert st.host_checks == 0  # every level on the device, one graph launch
     reached = par >= 0
     assert st.reached == int(reached.sum())
     assert st.edges == int((reached * deg[None, :]).sum()) // 2
