@@ -51,7 +51,7 @@ SEED = 1
 BFS_ROOTS = 64
 # DRAM bytes of k_numeric_x measured by ncu on a scale-20 column sample
 # (profiles/k_numeric_x_s20_cols4096.txt), used to scale roofline.traffic
-NUMERIC_DRAM_READ_PER_MULT = 6.16
+NUMERIC_DRAM_READ_PER_MULT = 6.17
 NUMERIC_DRAM_WRITE_PER_ENTRY = 17.22
 # DRAM bytes of the multi-source BFS kernels per scanned edge (expand +
 # finalize, profiles/launches_msbfs22.txt)

@@ -62,14 +62,39 @@ def test_mcl_planted_vs_oracle(gpu_ctx, oracle_lib, n, cluster):
 MCL_RECOVERY = ((1e-2, 30, 40, 0.9), (5e-3, 20, 30, 0.95), (2e-2, 10, 25, 0.8), (3e-2, 5, 12, 0.9))
 
 
+class _Sizing:
+    """Learned sizing needs a model on the context: one trained on A*A's
+    exact counts, dropped afterwards."""
+
+    def __init__(self, sizing_mode, A):
+        self.m = None
+        if sizing_mode == "learned":
+            from combblas_gb300 import sizing
+
+            feat, _, nnz = sizing.features(A, A)
+            self.m = sizing.SizingModel(seed=0)
+            self.m.fit(feat, nnz, steps=300)
+
+    def __enter__(self):
+        if self.m is not None:
+            self.m.use()
+        return self
+
+    def __exit__(self, *exc):
+        if self.m is not None:
+            self.m.close()
+
+
 @pytest.mark.parametrize("sizing", ["exact", "learned"])
 def test_mcl_recovery_golden(gpu_ctx, oracle_lib, golden, sizing):
     """recoverNum > 0 (ParFriends.h:290-330), bit-exact against the
     reference's own MemEfficientSpGEMM output."""
     O = oracle_lib
     M = golden_matrix(golden, "mcl4096")
-    for thr, k, rn, pct in MCL_RECOVERY:
-        R, _ = mcl.mcl_expand(M, thr, k, sizing=sizing, recoverNum=rn, recoverPct=pct)
+    with _Sizing(sizing, M):
+        results = [mcl.mcl_expand(M, thr, k, sizing=sizing, recoverNum=rn, recoverPct=pct)[0]
+                   for thr, k, rn, pct in MCL_RECOVERY]
+    for (thr, k, rn, pct), R in zip(MCL_RECOVERY, results):
         cp, rows, vals = O.canonical_csc(*R.to_csc())
         key = f"mclrec/mcl4096/{thr:g}/{k}/{rn}/{pct:g}"
         gcp, grows, gvals = O.tuples_to_csc(golden[f"{key}/rows"], golden[f"{key}/cols"], golden[f"{key}/vals"],
@@ -148,7 +173,8 @@ def test_mcl_loop_planted_vs_oracle(gpu_ctx, oracle_lib, sizing):
     iterations, against the restated loop."""
     O = oracle_lib
     M = G.mcl_planted(1 << 14, 256, 24, 6, seed=11)
-    R, it, chaos = mcl.HipMCL(M, 2.0, 1e-4, 1100, 1400, 0.9, sizing=sizing, max_iter=3)
+    with _Sizing(sizing, M):
+        R, it, chaos = mcl.HipMCL(M, 2.0, 1e-4, 1100, 1400, 0.9, sizing=sizing, max_iter=3)
     cp, rows, vals = O.canonical_csc(*R.to_csc())
     (pcp, prow, pval), pit, pchaos = O.port_mcl_iterate(M, 2.0, 1e-4, 1100, 1400, 0.9, 3)
     assert it == pit == 3 and np.float32(chaos) == np.float32(pchaos)
