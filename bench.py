@@ -52,6 +52,11 @@ BFS_ROOTS = 64
 # DRAM bytes of k_numeric_x measured by ncu on a scale-20 column sample
 # (profiles/k_numeric_x_s20_cols4096.txt), used to scale roofline.traffic
 NUMERIC_DRAM_READ_PER_MULT = 6.17
+# The compiled reference's own hybrid path (heap columns below compression
+# ratio 2, hash above, mtSpGEMM.h:310-311) against the restatement timed here,
+# same samples and threads (8 x86 cores): s20 A*A(:, 4096 columns) 4.05 s vs
+# 3.82 s, s14 A*A 0.487 s vs 0.468 s.
+CPU_CALIBRATION = "the compiled reference's hybrid path needs 1.04-1.06x the port's time on the same samples"
 NUMERIC_DRAM_WRITE_PER_ENTRY = 17.22
 # DRAM bytes of the multi-source BFS kernels per scanned edge (expand +
 # finalize, profiles/launches_msbfs22.txt)
@@ -581,8 +586,8 @@ def bench_msbfs(args, world, A, ctx, stream, hbm, peak_kind, scale, ef):
         "metric": metric_name(args.workload, scale, ef), "value": value, "unit": "GTEPS",
         "ms_per_step": ms / args.steps, "gpu_launches": launches, "clocks": ck,
         "msbfs": {"roots": MS_ROOTS, "levels": st.levels, "reached_pairs": st.reached, "edges_per_step": st.edges,
-                  "loop": "masked Select2ndMin product into a per-(root, vertex) candidate array; one captured "
-                          "CUDA graph per level"},
+                  "loop": "masked Select2ndMin product into a per-(root, vertex) candidate array; one CUDA "
+                          "graph per traversal (a conditional while node around the captured level)"},
         "roofline": {"bound": "hbm", "kernel": "k_ms_expand + k_ms_finalize", "achieved": achieved, "peak": hbm,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": MSBFS_DRAM_PER_SCANNED_EDGE * scanned, "algorithmic_bytes": bytes_trav,
@@ -1081,7 +1086,8 @@ def run_ours(args, world, rank, local):
         gteps = edges / (bfs_ms * 1e-3) / 1e9
         bfs_launches = _lib.lib().gbc_launch_count() - l0
         result["bfs"] = {"gteps": gteps, "roots": len(roots), "ms_total": bfs_ms, "edges": edges,
-                         "semiring": "SelectMin (min parent)", "loop": "captured CUDA graph per level"}
+                         "semiring": "SelectMin (min parent)",
+                         "loop": "one CUDA graph per traversal: a conditional while node around the captured level"}
         if args.workload == "bfs20":
             result.update({"metric": metric_name(args.workload, scale, ef), "value": gteps * world,
                            "unit": "GTEPS", "ms_per_step": bfs_ms / len(roots), "gpu_launches": bfs_launches,
@@ -1170,7 +1176,8 @@ def run_ours(args, world, rank, local):
         else:
             v, desc, th = cpu_spgemm_rate(A, 15.0)
             result["cpu_baseline"] = {"value": v, "unit": "Gmults/s", "cores": th, "kind": "port",
-                                      "sample": desc + " (oracle/oracle.c: the reference's hash-path algorithm)"}
+                                      "sample": desc + " (oracle/oracle.c: the reference's hash-path algorithm)",
+                                      "calibration": CPU_CALIBRATION}
     line = {
         "metric": result["metric"], "value": result["value"], "unit": result["unit"], "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": result["ms_per_step"], "higher_is_better": True,

@@ -808,27 +808,24 @@ __global__ void __launch_bounds__(NT, 2)
                         dst = tmp;
                     }
                     XPROF_LAP(5);
-                    // runs of one row: thread tid owns the sorted keys [8 tid,
-                    // 8 tid + 8); it sums (exactly) and writes every run whose
-                    // first key it owns, reading past its own keys to finish
-                    // its last run.  Output positions: one block prefix of the
-                    // runs started per thread.
-                    {
-                        const int k0t = 8 * tid, k1t = min(prods, k0t + 8);
-                        int heads = 0;
-                        for (int u = k0t; u < k1t; ++u)
-                            heads += (u == 0 || (src[u - 1] >> 12) != (src[u] >> 12)) ? 1 : 0;
+                    // runs of one row, one sorted key per thread and round:
+                    // the thread holding a run's first key sums the run
+                    // exactly (runs are short: a range's rows rarely repeat)
+                    // and writes it; output positions from a block prefix of
+                    // the run heads, so consecutive threads write
+                    // consecutive entries
+                    for (int u0 = 0; u0 < prods; u0 += NT) {
+                        const int u = u0 + tid;
+                        const bool act = u < prods;
+                        const uint32_t key = act ? src[u] : 0u;
+                        const bool head = act && (u == 0 || (src[u - 1] >> 12) != (key >> 12));
                         int tot;
-                        int64_t q = out + block_prefix(heads, &tot);
-                        int u = k0t;
-                        // keys continuing a run that an earlier thread started
-                        while (u < k1t && u > 0 && (src[u - 1] >> 12) == (src[u] >> 12)) ++u;
-                        while (u < k1t) {
-                            const uint32_t row = src[u] >> 12;
+                        const int64_t q = out + block_prefix(head ? 1 : 0, &tot);
+                        if (head) {
+                            const uint32_t row = key >> 12;
                             uint64_t hi = 0, lo = 0;
                             uint32_t fl = 0;
-                            int v = u;
-                            for (; v < prods; ++v) {
+                            for (int v = u; v < prods; ++v) {
                                 const uint32_t kv = src[v];
                                 if ((kv >> 12) != row) break;
                                 if (!x_acc128(hi, lo, fl, __longlong_as_double((long long)rval[kv & 4095]), ebase))
@@ -840,8 +837,6 @@ __global__ void __launch_bounds__(NT, 2)
                             } else {
                                 over = true;
                             }
-                            ++q;
-                            u = v;
                         }
                         out += tot;
                     }
