@@ -39,6 +39,7 @@ struct Graph {
     uint32_t *fbits[2] = {nullptr, nullptr};  // frontier bitmaps (current / next)
     int64_t *off = nullptr;                   // [n+1] prefix of frontier degrees
     int64_t *tile = nullptr;                  // per-tile sums of that prefix
+    int32_t *chunk_f0 = nullptr;              // [nnz / kEdgeChunk + 2] frontier entry holding each chunk's first edge
     int64_t *ctl = nullptr;  // device control block (see CTL_*)
     int64_t *h_ctl = nullptr;  // pinned mirror
     cudaGraphExec_t level_exec = nullptr;
@@ -290,7 +291,7 @@ __global__ void k_bfs_deg_scan(int64_t *ctl, int64_t *tile)
 }
 
 __global__ void k_bfs_deg_rescan(const uint32_t *cp32, const int64_t *ctl, int32_t *const *fronts,
-                                 const int64_t *tile, int64_t *off)
+                                 const int64_t *tile, int64_t *off, int32_t *chunk_f0)
 {
     if (ctl[CTL_DIR] != 0) return;
     const int64_t nf = ctl[CTL_NF];
@@ -314,7 +315,13 @@ __global__ void k_bfs_deg_rescan(const uint32_t *cp32, const int64_t *ctl, int32
 #pragma unroll
     for (int u = 0; u < PER; ++u) {
         const int64_t f = b0 + int64_t(threadIdx.x) * PER + u;
-        if (f < nf) off[f] = run;
+        if (f < nf) {
+            off[f] = run;
+            // the edge chunks that start inside this entry's edges
+            if (d[u] > 0)
+                for (int64_t c = (run + kEdgeChunk - 1) / kEdgeChunk; c <= (run + d[u] - 1) / kEdgeChunk; ++c)
+                    chunk_f0[c] = (int32_t)f;
+        }
         run += d[u];
     }
     if (b0 + kScanTile >= nf && threadIdx.x == kThreads - 1) off[nf] = run;
@@ -323,7 +330,8 @@ __global__ void k_bfs_deg_rescan(const uint32_t *cp32, const int64_t *ctl, int32
 // Top-down expansion over fixed edge chunks.
 __global__ void __launch_bounds__(kThreads) k_bfs_td(const uint32_t *cp32, const int32_t *row,
                                                      const uint32_t *visited, int32_t *cand, int64_t *ctl,
-                                                     int32_t *const *fronts, const int64_t *off)
+                                                     int32_t *const *fronts, const int64_t *off,
+                                                     const int32_t *chunk_f0)
 {
     __shared__ int64_t s_off[kEdgeChunk + 2];
     __shared__ uint32_t s_st[kEdgeChunk + 2];
@@ -347,20 +355,13 @@ __global__ void __launch_bounds__(kThreads) k_bfs_td(const uint32_t *cp32, const
             s_chunk = (int64_t)atomicAdd((unsigned long long *)&ctl[CTL_WORK], 1ull);
             const int64_t e0 = s_chunk * kEdgeChunk;
             if (e0 < E) {
-                // first and last frontier entries holding edges of this chunk
-                int64_t lo = 0, hi = nf;  // off[lo] <= e0 < off[hi]
-                while (hi - lo > 1) {
-                    const int64_t mid = (lo + hi) >> 1;
-                    if (off[mid] <= e0) lo = mid; else hi = mid;
-                }
-                const int64_t e1 = min(E, e0 + kEdgeChunk) - 1;
-                int64_t lo2 = lo, hi2 = nf;
-                while (hi2 - lo2 > 1) {
-                    const int64_t mid = (lo2 + hi2) >> 1;
-                    if (off[mid] <= e1) lo2 = mid; else hi2 = mid;
-                }
+                // first frontier entry of this chunk and of the next one
+                // (the last entry holding edges of this chunk is that one or
+                // the one before), from the rescan's chunk table
+                const int64_t lo = chunk_f0[s_chunk];
+                const int64_t lo2 = e0 + kEdgeChunk < E ? chunk_f0[s_chunk + 1] : nf - 1;
                 s_f0 = lo;
-                s_k = (int)(lo2 - lo + 1);
+                s_k = (int)(lo2 - lo + 1);  // <= nf < 2^31
             }
         }
         __syncthreads();
@@ -368,14 +369,19 @@ __global__ void __launch_bounds__(kThreads) k_bfs_td(const uint32_t *cp32, const
         if (e0 >= E) break;
         const int K = s_k;
         const int64_t f0 = s_f0;
-        for (int k = tid; k <= K; k += kThreads) {
-            s_off[k] = off[f0 + k];  // off has nf + 1 entries and f0 + K <= nf
-            if (k < K) {
-                const int32_t c = front[f0 + k];
-                s_c[k] = c;
-                s_st[k] = cp32[c];
+        // a chunk spans at most kEdgeChunk non-empty entries; empty entries
+        // (columns without entries, in a non-symmetric pattern) between
+        // them can make K larger, and such a chunk searches off in memory
+        const bool staged = K <= kEdgeChunk + 1;  // block-uniform
+        if (staged)
+            for (int k = tid; k <= K; k += kThreads) {
+                s_off[k] = off[f0 + k];  // off has nf + 1 entries and f0 + K <= nf
+                if (k < K) {
+                    const int32_t c = front[f0 + k];
+                    s_c[k] = c;
+                    s_st[k] = cp32[c];
+                }
             }
-        }
         __syncthreads();
         const int64_t e1 = min(E, e0 + kEdgeChunk);
         for (int64_t e = e0 + tid; e < e0 + kEdgeChunk; e += kThreads) {
@@ -383,13 +389,23 @@ __global__ void __launch_bounds__(kThreads) k_bfs_td(const uint32_t *cp32, const
             int32_t r = 0;
             if (e < e1) {
                 int lo = 0, hi = K;
-                while (hi - lo > 1) {
-                    const int mid = (lo + hi) >> 1;
-                    if (s_off[mid] <= e) lo = mid; else hi = mid;
+                int32_t c;
+                if (staged) {
+                    while (hi - lo > 1) {
+                        const int mid = (lo + hi) >> 1;
+                        if (s_off[mid] <= e) lo = mid; else hi = mid;
+                    }
+                    c = s_c[lo];
+                    r = row[s_st[lo] + (e - s_off[lo])];
+                } else {
+                    while (hi - lo > 1) {
+                        const int mid = (lo + hi) >> 1;
+                        if (off[f0 + mid] <= e) lo = mid; else hi = mid;
+                    }
+                    c = front[f0 + lo];
+                    r = row[cp32[c] + (e - off[f0 + lo])];
                 }
-                r = row[s_st[lo] + (e - s_off[lo])];
                 if (!(visited[r >> 5] & (1u << (r & 31)))) {
-                    const int32_t c = s_c[lo];
                     if (c < cand[r]) {
                         const int32_t old = atomicMin(&cand[r], c);
                         fresh = old == kNoCand;
@@ -656,6 +672,7 @@ static int graph_alloc_bfs(Graph *g)
     GBC_TRY(device_alloc(ctx, (void **)&g->fbits[1], words * sizeof(uint32_t)));
     GBC_TRY(device_alloc(ctx, (void **)&g->off, (g->n + 2) * sizeof(int64_t)));
     GBC_TRY(device_alloc(ctx, (void **)&g->tile, ((g->n + kScanTile - 1) / kScanTile + 2) * sizeof(int64_t)));
+    GBC_TRY(device_alloc(ctx, (void **)&g->chunk_f0, (g->nnz / kEdgeChunk + 2) * sizeof(int32_t)));
     GBC_TRY(device_alloc(ctx, (void **)&g->ctl, (kCtlWords + 8) * sizeof(int64_t)));
     GBC_TRY(device_alloc(ctx, (void **)&g->own_parents, (g->n + 1) * sizeof(int64_t)));
     GBC_TRY(device_alloc(ctx, (void **)&g->own_levels, (g->n + 1) * sizeof(int64_t)));
@@ -679,8 +696,9 @@ static int launch_level(Graph *g, int64_t *parents, int64_t *levels, cudaStream_
     k_bfs_direction<<<1, 1, 0, s>>>(g->ctl, g->n);
     k_bfs_deg_tiles<<<tiles, kThreads, 0, s>>>(g->cp32, g->ctl, fronts_dev(g), g->tile);
     k_bfs_deg_scan<<<1, kThreads, 0, s>>>(g->ctl, g->tile);
-    k_bfs_deg_rescan<<<tiles, kThreads, 0, s>>>(g->cp32, g->ctl, fronts_dev(g), g->tile, g->off);
-    k_bfs_td<<<grid, kThreads, 0, s>>>(g->cp32, g->row, g->visited, g->cand, g->ctl, fronts_dev(g), g->off);
+    k_bfs_deg_rescan<<<tiles, kThreads, 0, s>>>(g->cp32, g->ctl, fronts_dev(g), g->tile, g->off, g->chunk_f0);
+    k_bfs_td<<<grid, kThreads, 0, s>>>(g->cp32, g->row, g->visited, g->cand, g->ctl, fronts_dev(g), g->off,
+                                       g->chunk_f0);
     k_bfs_finalize<<<grid, 256, 0, s>>>(g->cand, g->visited, parents, levels, g->cp, g->ctl, fronts_dev(g),
                                         fbits_dev(g));
     k_bfs_bu<<<grid, kThreads, 0, s>>>(g->cp, g->row, g->visited, parents, levels, g->n, g->ctl, fronts_dev(g),
@@ -1172,6 +1190,7 @@ int gbc_graph_destroy(gbc_graph *g)
     device_free(c, g->fbits[1]);
     device_free(c, g->off);
     device_free(c, g->tile);
+    device_free(c, g->chunk_f0);
     device_free(c, g->ctl);
     device_free(c, g->own_parents);
     device_free(c, g->own_levels);
