@@ -1031,22 +1031,30 @@ struct Plan {
 };
 
 // PlusTimes fp64 under GBC_FOLD_EXACT: every admitted column is summed
-// exactly (big columns by k_numeric_x, whose accumulator tile is kXRows
-// high; the tile height is a tuning knob only, so it is fixed here).
+// exactly (big columns by k_numeric_x).  Its accumulator tile is kXRows
+// high by default (8192-row tiles, one 1024-thread block per SM, made the
+// scale-20 product 19 % slower) and kXRowsBig at most; the tile height is a
+// tuning knob only, so a larger request is lowered.
 template <class SR>
 static void plan_fold(Context *ctx, Plan &P)
 {
     if (std::is_same<SR, PlusTimes<double>>::value && ctx->fold == GBC_FOLD_EXACT) {
         P.want_aexp = true;
-        P.tile_rows = kXRows;
+        if (P.tile_rows == 0)
+            P.tile_rows = kXRows;
+        else if (P.tile_rows > kXRowsBig)
+            P.tile_rows = kXRowsBig;
     }
 }
 
 template <class SR>
 static bool use_exact(const Plan &P)
 {
-    return std::is_same<SR, PlusTimes<double>>::value && P.want_aexp && P.max_R <= kXRows;
+    return std::is_same<SR, PlusTimes<double>>::value && P.want_aexp && P.max_R <= kXRowsBig;
 }
+
+// shared memory of k_numeric_x for a tile of RS rows
+static size_t x_smem(int RS) { return (size_t)kXW * RS * 4 + RS; }
 
 struct Lists {
     const int64_t *l[3] = {nullptr, nullptr, nullptr};  // small1, small2, big
@@ -1098,7 +1106,7 @@ static int plan_add(Workspace &ws, Plan &P, const DevMatrix &A, const DevMatrix 
             note_launch();
         }
         a.aexp = aexp;
-        if (a.T <= kXTMax && A.ncol > 0) {
+        if (a.T <= (1 << 20) / std::max(a.R, kXRows) && A.ncol > 0) {
             // per-column tile lists of A (bucketing in the exact kernel)
             int64_t *kptr = nullptr;
             GBC_TRY(ws.alloc_n(&kptr, (size_t)A.ncol + 1));
@@ -1142,9 +1150,16 @@ static int plan_finalize(Workspace &ws, Plan &P)
         GBC_TRY(ws.alloc_n(&P.fb_items, (size_t)P.total_cols + 1));
         GBC_TRY(ws.alloc_n(&P.fb_cnt, 1));
         // bucketing scratch of the exact kernel: kXScap segments per resident block
-        const size_t smem = (size_t)kXW * kXRows * 4 + kXRows;
-        GBC_TRY(set_smem(k_numeric_x<kXThreads, kXRows>, smem));
-        P.x_blocks = ws.ctx->num_sms * resident_blocks(k_numeric_x<kXThreads, kXRows>, kXThreads, smem, 2);
+        if (P.max_R > kXRows) {
+            const size_t smem = x_smem(kXRowsBig);
+            GBC_TRY(set_smem(k_numeric_x<kXThreadsBig, kXRowsBig>, smem));
+            P.x_blocks = ws.ctx->num_sms *
+                         resident_blocks(k_numeric_x<kXThreadsBig, kXRowsBig>, kXThreadsBig, smem, 1);
+        } else {
+            const size_t smem = x_smem(kXRows);
+            GBC_TRY(set_smem(k_numeric_x<kXThreads, kXRows>, smem));
+            P.x_blocks = ws.ctx->num_sms * resident_blocks(k_numeric_x<kXThreads, kXRows>, kXThreads, smem, 2);
+        }
         GBC_TRY(ws.alloc_n(&P.xscratch, (size_t)P.x_blocks * kXScap));
     }
     GBC_CUDA_TRY(cudaMemcpyAsync(P.d, P.h.data(), P.h.size() * sizeof(SpgemmArgs), cudaMemcpyHostToDevice,
@@ -1300,14 +1315,17 @@ static int launch_big_exact(Context *ctx, Plan &P, const Lists &L, const int64_t
                             const int64_t *cap, int64_t *out_cnt, int32_t *overflow, int64_t *cir, void *cval)
 {
     cudaStream_t s = ctx->stream;
-    constexpr int NT = kXThreads;
-    const size_t smem = (size_t)kXW * kXRows * 4 + kXRows;
     const int grid = (int)std::min<int64_t>(P.x_blocks, L.n[2]);  // the scratch holds P.x_blocks blocks
     GBC_CUDA_TRY(cudaMemsetAsync(P.work + 1, 0, 2 * sizeof(unsigned long long), s));
     GBC_CUDA_TRY(cudaMemsetAsync(P.fb_cnt, 0, sizeof(unsigned long long), s));
-    k_numeric_x<NT, kXRows><<<grid, NT, smem, s>>>(P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir,
-                                           static_cast<double *>(cval), P.work + 1, P.fb_items, P.fb_cnt,
-                                           P.xscratch);
+    if (P.max_R > kXRows)
+        k_numeric_x<kXThreadsBig, kXRowsBig><<<grid, kXThreadsBig, x_smem(kXRowsBig), s>>>(
+            P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir, static_cast<double *>(cval),
+            P.work + 1, P.fb_items, P.fb_cnt, P.xscratch);
+    else
+        k_numeric_x<kXThreads, kXRows><<<grid, kXThreads, x_smem(kXRows), s>>>(
+            P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir, static_cast<double *>(cval),
+            P.work + 1, P.fb_items, P.fb_cnt, P.xscratch);
     note_launch();
     GBC_CUDA_TRY(cudaGetLastError());
     return launch_big_ordered<SR>(ctx, P, P.fb_items, L.n[2], P.fb_cnt, ccp, ccp_base, cap, out_cnt, overflow, cir,

@@ -42,11 +42,13 @@ constexpr int kXW = 6;                       // words per row
 constexpr uint32_t kXMask = (1u << kXP) - 1;
 constexpr int kXOMax = kXP * kXW - 53;       // largest product exponent above the base (61)
 constexpr int kXNorm = 2047;                 // B entries between carry normalisations
-// Accumulator tile and block shape of k_numeric_x: kXRows rows (24 B of
-// words + 1 flag byte each) in shared memory, kXThreads threads, two blocks
-// per SM.
+// Accumulator tiles and block shapes of k_numeric_x: RS rows (24 B of words
+// + 1 flag byte each) in shared memory; 4096 rows with 512 threads (two
+// blocks per SM) or 8192 rows with 1024 threads (one block per SM).
 constexpr int kXRows = 4096;
 constexpr int kXThreads = 512;
+constexpr int kXRowsBig = 8192;
+constexpr int kXThreadsBig = 1024;
 
 // Phase clocks of k_numeric_x for profiling builds (-DGBC_XPROF): thread 0
 // of every block adds the cycles between two block barriers to a counter.
@@ -390,18 +392,19 @@ constexpr int64_t kXScap = int64_t(1) << 18;  // bucketed segments of one column
 //     radix sorted by row (stable LSD, 7-bit digits), and each run of one
 //     row is summed exactly (x_acc128) and rounded (x_round).
 // Columns with more than kXScap segments, or matrices with more than
-// kXTMax tiles, visit every touched tile and look up their B entries' A
+// 2^20 / RS tiles, visit every touched tile and look up their B entries' A
 // segments per tile (tptr) instead of step 1.  Columns outside the exact
 // window are appended to fb_items for the ordered kernel.
 template <int NT, int RS>
-__global__ void __launch_bounds__(NT, 2)
+__global__ void __launch_bounds__(NT, 1024 / NT)
     k_numeric_x(const SpgemmArgs *args, const int64_t *items, int64_t nitems, const int64_t *ccp, int64_t ccp_base,
                 const int64_t *cap, int64_t *out_cnt, int32_t *overflow, int64_t *cir, double *cval,
                 unsigned long long *work, int64_t *fb_items, unsigned long long *fb_count, XSeg *scratch_all)
 {
     constexpr int NW = NT / 32;  // RS: rows of the tile = word stride
+    constexpr int TM = (1 << 20) / RS;  // tiles of a bucketed column
     static_assert(kXRange == 4096 && NT * 8 >= kXRange && (NW * 128) % NT == 0 && RS % (32 * NW) == 0 &&
-                      kXTMax * RS <= (1 << 20),
+                      TM * RS <= (1 << 20) && TM <= kXTMax,
                   "range keys: 20-bit row offset and 12-bit slot; eight sorted keys per thread");
     extern __shared__ __align__(16) int32_t xsm[];
     int32_t *acc = xsm;                                           // [kXW][RS]
@@ -416,7 +419,7 @@ __global__ void __launch_bounds__(NT, 2)
     __shared__ ChunkSmemN<NT> ch;
     static_assert(sizeof(ChunkSmemN<NT>) >= NW * 128 * 2, "write-out row lists fit the chunk table");
     __shared__ uint32_t ch_e[NT];
-    __shared__ int32_t s_segcnt[kXTMax], s_prodcnt[kXTMax], s_off[kXTMax + 1];
+    __shared__ int32_t s_segcnt[TM], s_prodcnt[TM], s_off[TM + 1];
     __shared__ int32_t s_wsum[NW];
     __shared__ int32_t s_band[RS / 256];  // touched rows per 256-row band of the dense tile
     __shared__ int32_t s_emin[NW], s_emax[NW];
@@ -615,7 +618,7 @@ __global__ void __launch_bounds__(NT, 2)
         };
 
         // ------------------------------------------------ 1. bucketing
-        bool bucketed = a.T <= kXTMax && a.ktl_ptr != nullptr;  // block-uniform
+        bool bucketed = a.T <= TM && a.ktl_ptr != nullptr;  // block-uniform
         if (bucketed) {
             for (int u = tid; u < a.T; u += NT) {
                 s_segcnt[u] = 0;
