@@ -56,6 +56,7 @@ struct Graph {
     uint32_t *ms_visited = nullptr;   // [roots * n / 32]
     int64_t *ms_front[2] = {nullptr, nullptr};  // frontier entries (root << 32 | vertex)
     int64_t *ms_ctl = nullptr;        // device control block (MS_*)
+    int64_t *ms_rcnt = nullptr, *ms_roff = nullptr;  // root counts / offsets of the frontier sort
     int64_t *h_ms_ctl = nullptr;      // pinned mirror
     cudaGraphExec_t ms_exec = nullptr;
     long long ms_kernels = 0;
@@ -824,8 +825,14 @@ enum {
     MS_EDGES = 4,    // sum of degrees of reached (root, vertex) pairs
     MS_REACHED = 5,  // reached (root, vertex) pairs
     MS_CUR = 6,      // which frontier buffer is current
+    MS_ROOTS = 7,    // roots of this traversal
     MS_N
 };
+// Traversals of at most this many roots keep each frontier sorted by root
+// (a counting sort after the expansion): the blocks in flight then work on
+// a few roots' slices of cand / visited, which stay in L2, instead of
+// touching every root's slice at random.
+constexpr int64_t kMsSortRoots = 4096;
 constexpr int kMsCtlWords = 8;  // then the frontier pointer table [2]
 
 __global__ void __launch_bounds__(kThreads) k_ms_expand(const uint32_t *cp32, const int32_t *row, int64_t n,
@@ -916,12 +923,77 @@ __global__ void __launch_bounds__(kThreads) k_ms_expand(const uint32_t *cp32, co
     }
 }
 
-// parents.Set(fringe) for the new frontier entries, visited update and the
-// reached-edge sums.
-__global__ void k_ms_finalize(int32_t *cand, uint32_t *visited, int64_t *parents, const uint32_t *cp32, int64_t n,
-                              int64_t *ctl, int64_t *const *fronts)
+// Counting sort of the next frontier by root into the current buffer (its
+// entries are consumed): the root counts of contiguous slices (one per
+// block, counted in shared memory) are added up, scanned, and every block
+// reserves its range of each root once and scatters into it.  The order
+// inside one root is arbitrary (the product is a min, order-free).
+__global__ void __launch_bounds__(256) k_ms_rhist(const int64_t *ctl, int64_t *const *fronts, int64_t *rcnt)
 {
+    extern __shared__ int32_t s_hist[];  // [roots]
+    const int64_t R = ctl[MS_ROOTS], nn = ctl[MS_NNEXT];
     const int64_t *next = fronts[ctl[MS_CUR] ^ 1];
+    for (int64_t r = threadIdx.x; r < R; r += blockDim.x) s_hist[r] = 0;
+    __syncthreads();
+    const int64_t per = (nn + gridDim.x - 1) / gridDim.x;
+    const int64_t i0 = int64_t(blockIdx.x) * per, i1 = min(nn, i0 + per);
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) atomicAdd(&s_hist[next[i] >> 32], 1);
+    __syncthreads();
+    for (int64_t r = threadIdx.x; r < R; r += blockDim.x)
+        if (s_hist[r]) atomicAdd((unsigned long long *)&rcnt[r], (unsigned long long)s_hist[r]);
+}
+
+__global__ void k_ms_rscan(const int64_t *ctl, int64_t *rcnt, int64_t *roff)
+{
+    const int64_t R = ctl[MS_ROOTS];
+    int64_t carry = 0;
+    for (int64_t b = 0; b < R; b += kThreads) {
+        const int64_t r = b + threadIdx.x;
+        const int64_t v = r < R ? rcnt[r] : 0;
+        int64_t tot;
+        const int64_t ex = block_exclusive_sum64(v, &tot);
+        if (r < R) {
+            roff[r] = carry + ex;
+            rcnt[r] = 0;  // ready for the next level
+        }
+        carry += tot;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_ms_rscatter(const int64_t *ctl, int64_t *const *fronts, int64_t *roff)
+{
+    extern __shared__ int64_t s_base[];  // [roots] then int32 counts [roots]
+    const int64_t R = ctl[MS_ROOTS], nn = ctl[MS_NNEXT];
+    int32_t *s_cnt = reinterpret_cast<int32_t *>(s_base + R);
+    const int cur = (int)ctl[MS_CUR];
+    const int64_t *next = fronts[cur ^ 1];
+    int64_t *out = fronts[cur];
+    for (int64_t r = threadIdx.x; r < R; r += blockDim.x) s_cnt[r] = 0;
+    __syncthreads();
+    const int64_t per = (nn + gridDim.x - 1) / gridDim.x;
+    const int64_t i0 = int64_t(blockIdx.x) * per, i1 = min(nn, i0 + per);
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) atomicAdd(&s_cnt[next[i] >> 32], 1);
+    __syncthreads();
+    for (int64_t r = threadIdx.x; r < R; r += blockDim.x) {
+        const int c = s_cnt[r];
+        if (c) s_base[r] = (int64_t)atomicAdd((unsigned long long *)&roff[r], (unsigned long long)c);
+        s_cnt[r] = 0;
+    }
+    __syncthreads();
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const int64_t x = next[i];
+        const int64_t r = x >> 32;
+        out[s_base[r] + atomicAdd(&s_cnt[r], 1)] = x;
+    }
+}
+
+// parents.Set(fringe) for the new frontier entries, visited update and the
+// reached-edge sums.  `sorted`: the entries were sorted into the current
+// buffer.
+__global__ void k_ms_finalize(int32_t *cand, uint32_t *visited, int64_t *parents, const uint32_t *cp32, int64_t n,
+                              int64_t *ctl, int64_t *const *fronts, int sorted)
+{
+    const int64_t *next = fronts[ctl[MS_CUR] ^ (sorted ? 0 : 1)];
     const int64_t nn = ctl[MS_NNEXT];
     int64_t deg = 0, reached = 0;
     for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < nn; i += int64_t(gridDim.x) * blockDim.x) {
@@ -945,13 +1017,13 @@ __global__ void k_ms_finalize(int32_t *cand, uint32_t *visited, int64_t *parents
     }
 }
 
-__global__ void k_ms_advance(int64_t *ctl)
+__global__ void k_ms_advance(int64_t *ctl, int sorted)
 {
     if (ctl[MS_NF] == 0) return;
     ctl[MS_NF] = ctl[MS_NNEXT];
     ctl[MS_NNEXT] = 0;
     ctl[MS_WORK] = 0;
-    ctl[MS_CUR] ^= 1;
+    if (!sorted) ctl[MS_CUR] ^= 1;  // a sorted frontier is already in the current buffer
     ctl[MS_LEVEL] += 1;
 }
 
@@ -991,6 +1063,9 @@ static void ms_free(Graph *g)
     device_free(c, g->ms_front[0]);
     device_free(c, g->ms_front[1]);
     device_free(c, g->ms_ctl);
+    device_free(c, g->ms_rcnt);
+    device_free(c, g->ms_roff);
+    g->ms_rcnt = g->ms_roff = nullptr;
     if (g->h_ms_ctl) cudaFreeHost(g->h_ms_ctl);
     g->ms_cand = nullptr;
     g->ms_visited = nullptr;
@@ -1013,6 +1088,9 @@ static int ms_alloc(Graph *g, int64_t nroots)
     GBC_TRY(device_alloc(ctx, (void **)&g->ms_front[0], cells * sizeof(int64_t) + 16));
     GBC_TRY(device_alloc(ctx, (void **)&g->ms_front[1], cells * sizeof(int64_t) + 16));
     GBC_TRY(device_alloc(ctx, (void **)&g->ms_ctl, (kMsCtlWords + 4) * sizeof(int64_t)));
+    GBC_TRY(device_alloc(ctx, (void **)&g->ms_rcnt, (nroots + 1) * sizeof(int64_t)));
+    GBC_TRY(device_alloc(ctx, (void **)&g->ms_roff, (nroots + 1) * sizeof(int64_t)));
+    GBC_CUDA_TRY(cudaMemsetAsync(g->ms_rcnt, 0, (nroots + 1) * sizeof(int64_t), ctx->stream));
     GBC_CUDA_TRY(cudaMallocHost(&g->h_ms_ctl, (kMsCtlWords + 4) * sizeof(int64_t)));
     void *tab[2] = {g->ms_front[0], g->ms_front[1]};
     GBC_CUDA_TRY(cudaMemcpyAsync(g->ms_ctl + kMsCtlWords, tab, sizeof(tab), cudaMemcpyHostToDevice, ctx->stream));
@@ -1026,12 +1104,21 @@ static int ms_alloc(Graph *g, int64_t nroots)
 static int ms_launch_level(Graph *g, int64_t *parents, cudaStream_t s)
 {
     const int grid = g->ctx->num_sms * 4;
+    const int sorted = g->ms_roots <= kMsSortRoots ? 1 : 0;
     k_ms_expand<<<grid, kThreads, 0, s>>>(g->cp32, g->row, g->n, g->ms_visited, g->ms_cand, g->ms_ctl,
                                           ms_fronts_dev(g));
+    note_launch();
+    if (sorted) {
+        k_ms_rhist<<<grid, 256, g->ms_roots * sizeof(int32_t), s>>>(g->ms_ctl, ms_fronts_dev(g), g->ms_rcnt);
+        k_ms_rscan<<<1, kThreads, 0, s>>>(g->ms_ctl, g->ms_rcnt, g->ms_roff);
+        k_ms_rscatter<<<grid, 256, g->ms_roots * (sizeof(int64_t) + sizeof(int32_t)), s>>>(
+            g->ms_ctl, ms_fronts_dev(g), g->ms_roff);
+        note_launches(3);
+    }
     k_ms_finalize<<<grid, 256, 0, s>>>(g->ms_cand, g->ms_visited, parents, g->cp32, g->n, g->ms_ctl,
-                                       ms_fronts_dev(g));
-    k_ms_advance<<<1, 1, 0, s>>>(g->ms_ctl);
-    note_launches(3);
+                                       ms_fronts_dev(g), sorted);
+    k_ms_advance<<<1, 1, 0, s>>>(g->ms_ctl, sorted);
+    note_launches(2);
     GBC_CUDA_TRY(cudaGetLastError());
     return GBC_OK;
 }
@@ -1086,6 +1173,7 @@ static int msbfs_device(Graph *g, const int64_t *d_roots, int64_t nroots, int64_
     note_launch();
     int64_t nf = nroots;
     GBC_CUDA_TRY(cudaMemcpyAsync(g->ms_ctl + MS_NF, &nf, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    GBC_CUDA_TRY(cudaMemcpyAsync(g->ms_ctl + MS_ROOTS, &nf, sizeof(int64_t), cudaMemcpyHostToDevice, s));
     GBC_CUDA_TRY(cudaGetLastError());
     GBC_TRY(ms_level_graph(g, parents));
     if (g->ms_loop_exec) {
