@@ -59,8 +59,11 @@ NUMERIC_DRAM_READ_PER_MULT = 6.17
 CPU_CALIBRATION = "the compiled reference's hybrid path needs 1.04-1.06x the port's time on the same samples"
 NUMERIC_DRAM_WRITE_PER_ENTRY = 17.22
 # DRAM bytes of the multi-source BFS kernels per scanned edge (expand +
-# finalize, profiles/launches_msbfs22.txt)
-MSBFS_DRAM_PER_SCANNED_EDGE = 19.5
+# finalize) as last captured, when each level was a separate graph launch
+# (profiles/launches_msbfs22.txt); the traversal is now one graph whose
+# level kernels run inside a conditional while node, which ncu does not
+# list as launches, so the line reports no traffic of its own.
+MSBFS_DRAM_PER_SCANNED_EDGE_LEVEL_REPLAY = 19.5
 MS_ROOTS = 512
 
 
@@ -590,9 +593,11 @@ def bench_msbfs(args, world, A, ctx, stream, hbm, peak_kind, scale, ef):
                           "graph per traversal (a conditional while node around the captured level)"},
         "roofline": {"bound": "hbm", "kernel": "k_ms_expand + k_ms_finalize", "achieved": achieved, "peak": hbm,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": MSBFS_DRAM_PER_SCANNED_EDGE * scanned, "algorithmic_bytes": bytes_trav,
-                     "traffic_note": "DRAM bytes per traversal scaled by scanned edges from "
-                                     "profiles/launches_msbfs22.txt"},
+                     "traffic": None, "algorithmic_bytes": bytes_trav,
+                     "traffic_note": "the level kernels run inside the traversal graph's while node, which ncu "
+                                     "does not list as launches; the last level-by-level capture measured "
+                                     f"{MSBFS_DRAM_PER_SCANNED_EDGE_LEVEL_REPLAY} DRAM B per scanned edge "
+                                     "(profiles/launches_msbfs22.txt)"},
     }
     # e2e: graph upload from host + traversal + parents read back into pinned host memory
     hp = torch.empty((MS_ROOTS, A.ncol), dtype=torch.int64, pin_memory=True)
