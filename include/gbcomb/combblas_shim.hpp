@@ -350,25 +350,6 @@ combblas::SpTuples<IT, NT> *MultiwayMerge(std::vector<combblas::SpTuples<IT, NT>
     }
 }
 
-// y <- y (+) A x with dense vectors.  A row-major plan is built and
-// dropped per call; callers that multiply the same matrix repeatedly keep a
-// gbc_spmv_plan instead.
-template <class SR, class IU, class NU, class RHS, class LHS>
-void dcsc_gespmv(const combblas::SpDCCols<IU, NU> &A, const RHS *x, LHS *y)
-{
-    if constexpr (!detail::offloaded<SR, NU, IU, RHS, LHS>()) {
-        combblas::dcsc_gespmv<SR>(A, x, y);
-    } else {
-        if (A.isZero()) return;
-        const gbc_matrix g = detail::view(A);
-        gbc_spmv_plan *p = nullptr;
-        detail::check(gbc_spmv_plan_create(detail::context(), semiring_of<SR>::vt, &g, &p), "gbc_spmv_plan_create");
-        const int rc = gbc_spmv(detail::context(), p, semiring_of<SR>::sr, x, y, GBC_HOST);
-        gbc_spmv_plan_destroy(p);
-        detail::check(rc, "gbc_spmv");
-    }
-}
-
 // ------------------------------------------------------------------ SpMSpV
 // Semiring code for the sparse-vector multiplies: the stock boolean
 // Select2ndSRing (TopDownBFS, BFSFriends.h:198-207) and SelectMaxSRing, or a
@@ -423,6 +404,24 @@ inline int64_t sample_of(const int64_t *cp, int64_t ncp, const int64_t *ir, int6
     for (int64_t k = 0; k < 64 && ncp > 0; ++k) mix((uint64_t)cp[(ncp - 1) * k / 63]);
     for (int64_t k = 0; k < 64 && nz > 0; ++k) mix((uint64_t)ir[(nz - 1) * k / 63]);
     return (int64_t)h;
+}
+
+inline std::map<PlanKey, gbc_spmv_plan *> &spmv_plan_cache()
+{
+    static std::map<PlanKey, gbc_spmv_plan *> cache;
+    return cache;
+}
+
+inline gbc_spmv_plan *spmv_plan(const gbc_matrix &g, int vt)
+{
+    const PlanKey key{g.cp, g.ir, g.num, g.nrow, g.ncol, g.nnz, sample_of(g.cp, g.nzc + 1, g.ir, g.nnz), vt};
+    auto it = spmv_plan_cache().find(key);
+    if (it != spmv_plan_cache().end()) return it->second;
+    gbc_spmv_plan *p = nullptr;
+    check(gbc_spmv_plan_create(context(), vt, &g, &p), "gbc_spmv_plan_create");
+    ++plan_builds();
+    spmv_plan_cache()[key] = p;
+    return p;
 }
 
 inline gbc_spmspv_plan *spmspv_plan(const gbc_matrix &g, int vt)
@@ -497,6 +496,23 @@ inline void forget_matrices()
 {
     for (auto &e : detail::plan_cache()) gbc_spmspv_plan_destroy(e.second);
     detail::plan_cache().clear();
+    for (auto &e : detail::spmv_plan_cache()) gbc_spmv_plan_destroy(e.second);
+    detail::spmv_plan_cache().clear();
+}
+
+// y <- y (+) A x with dense vectors (Friends.h:63-77): the row-major plan of
+// A is built on the first product with A and kept (forget_matrices drops it).
+template <class SR, class IU, class NU, class RHS, class LHS>
+void dcsc_gespmv(const combblas::SpDCCols<IU, NU> &A, const RHS *x, LHS *y)
+{
+    if constexpr (!detail::offloaded<SR, NU, IU, RHS, LHS>()) {
+        combblas::dcsc_gespmv<SR>(A, x, y);
+    } else {
+        if (A.isZero()) return;
+        const gbc_matrix g = detail::view(A);
+        gbc_spmv_plan *p = detail::spmv_plan(g, semiring_of<SR>::vt);
+        detail::check(gbc_spmv(detail::context(), p, semiring_of<SR>::sr, x, y, GBC_HOST), "gbc_spmv");
+    }
 }
 
 // y = A x (SpImpl.h:115-124, the PreAllocatedSPA overload that reaches

@@ -346,10 +346,16 @@ int main()
         for (int j = 0; j < 400; ++j) x[j] = (j * 37) % 101;
         for (int r = 0; r < 900; ++r) yg[r] = yc[r] = 50 + (r * 13) % 77;
         const int fb = fallback_calls();
+        const long long builds = gbcomb::detail::plan_builds();
         gbcomb::dcsc_gespmv<MP>(*M, x.data(), yg.data());
         EXPECT(fallback_calls() == fb);
         combblas::dcsc_gespmv<MP>(*M, x.data(), yc.data());
         EXPECT(yg == yc);
+        // a second product with the same matrix reuses its device plan
+        gbcomb::dcsc_gespmv<MP>(*M, x.data(), yg.data());
+        combblas::dcsc_gespmv<MP>(*M, x.data(), yc.data());
+        EXPECT(yg == yc && gbcomb::detail::plan_builds() == builds + 1);
+        gbcomb::forget_matrices();  // before the matrix's memory is freed
         delete M;
     }
     delete B2;
