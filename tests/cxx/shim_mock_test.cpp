@@ -200,6 +200,7 @@ int main()
             EXPECT(k < indy.size() && indy[k] == e.first && numy[k] == e.second);
             ++k;
         }
+        gbcomb::forget_matrices();  // before the matrix's memory is freed
     }
     // 7b. the other SpMXSpV semirings on a rectangular matrix (300 x 900):
     // SelectMax and PlusTimes through the Csc overload, Select2nd through the
