@@ -374,7 +374,10 @@ struct XSeg {
 
 constexpr int kXTMax = 256;                   // row tiles of a bucketed column (rows <= 256 * kXRows)
 constexpr int kXRange = 4096;                 // products of one sorted range visit
-constexpr int kXDense = 512;                  // a tile with more products is a dense visit
+#ifndef GBC_XDENSE
+#define GBC_XDENSE 512
+#endif
+constexpr int kXDense = GBC_XDENSE;           // a tile with more products is a dense visit
 constexpr int64_t kXScap = int64_t(1) << 18;  // bucketed segments of one column (per-block scratch)
 
 // Numeric pass for the columns of the big list, one block per column
