@@ -57,6 +57,7 @@ class gbc_spgemm_stats(C.Structure):
     _fields_ = [
         ("flops", C.c_int64), ("nnz", C.c_int64), ("overflow_cols", C.c_int64), ("alloc_entries", C.c_int64),
         ("ms_total", C.c_double), ("ms_symbolic", C.c_double), ("ms_numeric", C.c_double),
+        ("tile_visits_dense", C.c_int64), ("tile_visits_range", C.c_int64),
     ]
 
 

@@ -1144,6 +1144,7 @@ static int plan_finalize(Workspace &ws, Plan &P)
 {
     GBC_TRY(ws.alloc_n(&P.d, P.h.size() + 1));
     GBC_TRY(ws.alloc_n(&P.work, 16));
+    GBC_CUDA_TRY(cudaMemsetAsync(P.work, 0, 16 * sizeof(unsigned long long), ws.ctx->stream));
     GBC_TRY(ws.alloc_n(&P.lbuf, (2 + kBigBins) * ((size_t)P.total_cols + 1)));
     GBC_TRY(ws.alloc_n(&P.lcnt, 2 + kBigBins));
     if (P.want_aexp) {
@@ -1316,7 +1317,7 @@ static int launch_big_exact(Context *ctx, Plan &P, const Lists &L, const int64_t
 {
     cudaStream_t s = ctx->stream;
     const int grid = (int)std::min<int64_t>(P.x_blocks, L.n[2]);  // the scratch holds P.x_blocks blocks
-    GBC_CUDA_TRY(cudaMemsetAsync(P.work + 1, 0, 2 * sizeof(unsigned long long), s));
+    GBC_CUDA_TRY(cudaMemsetAsync(P.work + 1, 0, 3 * sizeof(unsigned long long), s));
     GBC_CUDA_TRY(cudaMemsetAsync(P.fb_cnt, 0, sizeof(unsigned long long), s));
     if (P.max_R > kXRows)
         k_numeric_x<kXThreadsBig, kXRowsBig><<<grid, kXThreadsBig, x_smem(kXRowsBig), s>>>(
@@ -1482,6 +1483,12 @@ static int spgemm_exact(Context *ctx, const DevMatrix &A, const DevMatrix &B, co
         st->ms_total = t04;
         st->ms_symbolic = t12;
         st->ms_numeric = t23;
+        st->tile_visits_dense = 0;
+        st->tile_visits_range = 0;
+        if (use_exact<SR>(P)) {
+            GBC_TRY(read_i64(ctx, reinterpret_cast<const int64_t *>(P.work + 2), &st->tile_visits_dense));
+            GBC_TRY(read_i64(ctx, reinterpret_cast<const int64_t *>(P.work + 3), &st->tile_visits_range));
+        }
     }
     *Cout = C;
     return GBC_OK;
@@ -2069,6 +2076,7 @@ int spgemm_learned(Context *ctx, const DevMatrix &A, const DevMatrix &B, const g
         st->ms_total = t04;
         st->ms_symbolic = O.ms_predict;
         st->ms_numeric = O.ms_numeric + O.ms_rerun;
+        st->tile_visits_dense = st->tile_visits_range = 0;
     }
     *Cout = C;
     return GBC_OK;
@@ -2155,6 +2163,7 @@ int mcl_expand(gbc_context *ctx, const gbc_matrix *Am, float thr, int64_t select
             st->ms_total = t;
             st->ms_symbolic = O.ms_predict;
             st->ms_numeric = O.ms_numeric + O.ms_rerun;
+            st->tile_visits_dense = st->tile_visits_range = 0;
         }
         return GBC_OK;
     }

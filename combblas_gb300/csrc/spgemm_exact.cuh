@@ -716,6 +716,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
                     dense_writeout(row0);
                     XPROF_LAP(3);
                     XPROF_ADD(8, 1);
+                    if (tid == 0) atomicAdd(&work[1], 1ull);  // dense visits (statistics)
                     ++t;
                 } else {
                     // range visit of light tiles t .. t1 (at most kXRange products)
@@ -756,6 +757,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
                     }
                     XPROF_LAP(4);
                     XPROF_ADD(9, 1);
+                    if (tid == 0) atomicAdd(&work[2], 1ull);  // range visits (statistics)
                     XPROF_ADD(13, prods);
                     // stable LSD radix sort of the keys by row, 7-bit digits:
                     // warp w owns a contiguous run of keys, counts its digits,

@@ -100,6 +100,9 @@ typedef struct {
     double ms_total;        /* device time of the call (CUDA events) */
     double ms_symbolic;
     double ms_numeric;
+    int64_t tile_visits_dense; /* exact-fold big columns: (column, row tile) visits through the
+                                  dense accumulator (gbc_spgemm only; 0 otherwise) */
+    int64_t tile_visits_range; /* ... and runs of light tiles summed through a sorted range */
 } gbc_spgemm_stats;
 
 /* ---------------------------------------------------------------- context */

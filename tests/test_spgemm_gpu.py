@@ -302,3 +302,26 @@ def test_phased_learned_identical_to_exact(gpu_ctx, oracle_lib, margin, fold):
                 assert le.overflow_cols > 0
     finally:
         m.close()
+
+
+def test_exact_kernel_visits_both_tile_paths(gpu_ctx, oracle_lib):
+    """The exact-fold kernel's two tile paths -- dense accumulator visits and
+    sorted ranges of light tiles -- both run on an R-MAT product with
+    4096-row tiles, and the product is bit-exact against the oracle's exact
+    fold (the two paths' thresholds change which tiles take which path, not
+    the values: the bench records identical content hashes across them)."""
+    O = oracle_lib
+    A = G.rmat(16, 16, seed=21)
+    cols = np.sort(np.random.default_rng(3).choice(A.ncol, 3000, replace=False))
+    cnt = np.diff(A.colptr)[cols]
+    cp = np.concatenate([[0], np.cumsum(cnt)]).astype(np.int64)
+    idx = np.concatenate([np.arange(A.colptr[c], A.colptr[c + 1]) for c in cols])
+    B = G.CSC(A.nrow, len(cols), cp, A.rowidx[idx], A.values[idx])
+    R = local.spgemm(A, B, fold="exact", tile_rows=4096)
+    st = R.stats
+    assert st.tile_visits_dense > 0 and st.tile_visits_range > 0, (st.tile_visits_dense, st.tile_visits_range)
+    got = R.to_csc()
+    exp = O.port_spgemm(A, B, O.SR_PLUSTIMES_F64, fold="exact")
+    assert all(np.array_equal(np.asarray(x).view(np.int64) if np.asarray(x).dtype == np.float64 else x,
+                              np.asarray(y).view(np.int64) if np.asarray(y).dtype == np.float64 else y)
+               for x, y in zip(got, exp))
