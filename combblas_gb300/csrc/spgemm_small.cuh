@@ -8,7 +8,7 @@
 //                   matter for a count).
 //  k_small_numeric  gathers the column's products (row, A(row,k)*B(k,j)) in
 //                   k-major order, sorts them by row with a stable LSD radix
-//                   sort (ranks within a 32-item chunk from __match_any_sync,
+//                   sort (ranks within a 32-item chunk from eight ballots,
 //                   so equal digits keep their order), then folds each run of
 //                   equal rows left to right: acc = add(mrhs, acc) over k
 //                   ascending, the reference's hash-path order.  Rows come out
@@ -251,8 +251,15 @@ __global__ void __launch_bounds__(WPB * 32) k_small_numeric(const SpgemmArgs *ar
                 const int p = p0 + lane;
                 const bool act = p < n;
                 const uint32_t key = act ? ks[p] : 0u;
-                const int dg = act ? (int)((key >> shift) & 255) : (256 + lane);
-                const unsigned grp = __match_any_sync(0xffffffffu, dg);
+                const int dg = act ? (int)((key >> shift) & 255) : 0;
+                // lanes holding the same digit: eight ballots (much cheaper
+                // than __match_any_sync on this part)
+                unsigned grp = __ballot_sync(0xffffffffu, act);
+#pragma unroll
+                for (int bit = 0; bit < 8; ++bit) {
+                    const unsigned bb = __ballot_sync(0xffffffffu, act && ((dg >> bit) & 1));
+                    grp &= ((dg >> bit) & 1) ? bb : ~bb;
+                }
                 if (act) {
                     const int dst = hist[dg] + __popc(grp & lt);
                     kd[dst] = key;
