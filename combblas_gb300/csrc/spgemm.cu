@@ -191,6 +191,13 @@ __global__ void k_flop_mask(int64_t nb, const int64_t *bcp, const int32_t *brow,
 // to its own output range, so the order does not affect the result.
 constexpr int kSmall1 = 256;
 constexpr int kSmall2 = 4096;
+// Warp-kernel columns of at most kSmallMid multiplications run a kernel
+// sized for kSmallMid products (a quarter of the shared memory per warp:
+// four times the resident warps); the rest up to s2 the kSmall2 one.
+constexpr int kSmallMid = 1024;
+#ifndef GBC_SMALL2
+#define GBC_SMALL2 kSmall2
+#endif
 
 // Big columns are binned by flop (> 2^23, > 2^21, > 2^19, the rest) and
 // listed heaviest bin first, so the longest columns start early and do not
@@ -199,7 +206,7 @@ constexpr int kSmall2 = 4096;
 constexpr int kBigBins = 4;
 
 __global__ void k_classify(const int64_t *flop, int pid, int64_t col_base, int64_t j0, int64_t j1, int64_t s1,
-                           int64_t s2, int64_t *l1, int64_t *l2, int64_t *lb, int64_t lb_stride,
+                           int64_t s2, int64_t *l1, int64_t *l2, int64_t *lb, int64_t lb_stride, int64_t *lm,
                            unsigned long long *counts, int64_t *cnt_zero, const int32_t *only_flagged)
 {
     const int64_t i = j0 + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -211,21 +218,23 @@ __global__ void k_classify(const int64_t *flop, int pid, int64_t col_base, int64
             if (cnt_zero) cnt_zero[col_base + i] = 0;
         } else if (f <= s1) {
             cls = 0;
-        } else if (f <= s2) {
+        } else if (f <= s2 && f <= kSmallMid) {
             cls = 1;
+        } else if (f <= s2) {
+            cls = 2 + kBigBins;  // the larger warp kernel's list
         } else {
             cls = f > (1ll << 23) ? 2 : f > (1ll << 21) ? 3 : f > (1ll << 19) ? 4 : 5;
         }
     }
 #pragma unroll
-    for (int c = 0; c < 2 + kBigBins; ++c) {
+    for (int c = 0; c < 3 + kBigBins; ++c) {
         const unsigned m = __ballot_sync(0xffffffffu, cls == c);
         if (!m) continue;
         const int leader = __ffs(m) - 1;
         unsigned long long base = 0;
         if (lane == leader) base = atomicAdd(&counts[c], (unsigned long long)__popc(m));
         base = __shfl_sync(0xffffffffu, base, leader);
-        int64_t *list = c == 0 ? l1 : c == 1 ? l2 : lb + (c - 2) * lb_stride;
+        int64_t *list = c == 0 ? l1 : c == 1 ? l2 : c == 2 + kBigBins ? lm : lb + (c - 2) * lb_stride;
         if (cls == c) list[base + __popc(m & ((1u << lane) - 1))] = make_item(pid, i);
     }
 }
@@ -1017,10 +1026,11 @@ struct Plan {
     int64_t total_cols = 0;           // stored columns of all B's
     int max_R = 0, max_key_bits = 0;
     size_t max_sym_smem = 0;
-    int64_t s1 = kSmall1, s2 = kSmall2;  // flop thresholds of the column classes
+    int64_t s1 = kSmall1, s2 = GBC_SMALL2;  // flop thresholds of the column classes
     int tile_rows = 0;                   // accumulator tile height (0: default)
     unsigned long long *work = nullptr;  // kernel work counters
-    int64_t *lbuf = nullptr;             // column lists ((2 + kBigBins) x (total_cols + 1))
+    int64_t *lbuf = nullptr;             // column lists ((3 + kBigBins) x (total_cols + 1))
+    bool s2_set = false;                 // the caller chose s2
     unsigned long long *lcnt = nullptr;  // list lengths
     bool want_aexp = false;              // PlusTimes fp64, exact accumulation (k_numeric_x)
     int64_t *fb_items = nullptr;         // big columns the exact kernel hands to the ordered one
@@ -1044,6 +1054,9 @@ static void plan_fold(Context *ctx, Plan &P)
             P.tile_rows = kXRows;
         else if (P.tile_rows > kXRowsBig)
             P.tile_rows = kXRowsBig;
+        // columns of more than kSmallMid multiplications go to the exact
+        // block kernel (R-MAT s14: 2.1x faster than the larger warp kernel)
+        if (!P.s2_set) P.s2 = std::min<int64_t>(P.s2, kSmallMid);
     }
 }
 
@@ -1057,8 +1070,10 @@ static bool use_exact(const Plan &P)
 static size_t x_smem(int RS) { return (size_t)kXW * RS * 4 + RS; }
 
 struct Lists {
-    const int64_t *l[3] = {nullptr, nullptr, nullptr};  // small1, small2, big
-    int64_t n[3] = {0, 0, 0};
+    // [0] up to s1 multiplications, [1] up to kSmallMid, [2] the big list,
+    // [3] up to s2 (the larger warp kernel)
+    const int64_t *l[4] = {nullptr, nullptr, nullptr, nullptr};
+    int64_t n[4] = {0, 0, 0, 0};
 };
 
 // Prepare one product (A*B) and append it to the plan.
@@ -1145,8 +1160,8 @@ static int plan_finalize(Workspace &ws, Plan &P)
     GBC_TRY(ws.alloc_n(&P.d, P.h.size() + 1));
     GBC_TRY(ws.alloc_n(&P.work, 16));
     GBC_CUDA_TRY(cudaMemsetAsync(P.work, 0, 16 * sizeof(unsigned long long), ws.ctx->stream));
-    GBC_TRY(ws.alloc_n(&P.lbuf, (2 + kBigBins) * ((size_t)P.total_cols + 1)));
-    GBC_TRY(ws.alloc_n(&P.lcnt, 2 + kBigBins));
+    GBC_TRY(ws.alloc_n(&P.lbuf, (3 + kBigBins) * ((size_t)P.total_cols + 1)));
+    GBC_TRY(ws.alloc_n(&P.lcnt, 3 + kBigBins));
     if (P.want_aexp) {
         GBC_TRY(ws.alloc_n(&P.fb_items, (size_t)P.total_cols + 1));
         GBC_TRY(ws.alloc_n(&P.fb_cnt, 1));
@@ -1172,7 +1187,10 @@ static void plan_options(Plan &P, const gbc_spgemm_opts &opt)
 {
     P.tile_rows = opt.tile_rows;
     if (opt.tiny_limit >= 0) P.s1 = std::min<int64_t>(opt.tiny_limit, kSmall1);
-    if (opt.small_limit >= 0) P.s2 = std::min<int64_t>(std::max(opt.small_limit, P.s1), kSmall2);
+    if (opt.small_limit >= 0) {
+        P.s2 = std::min<int64_t>(std::max(opt.small_limit, P.s1), kSmall2);
+        P.s2_set = true;
+    }
 }
 
 static int plan_build(Workspace &ws, const DevMatrix &A, const DevMatrix &B, Plan &P)
@@ -1187,17 +1205,18 @@ static int plan_build(Workspace &ws, const DevMatrix &A, const DevMatrix &B, Pla
 static int plan_classify(Plan &P, cudaStream_t s, int pid, int64_t j0, int64_t j1, Lists &L, int64_t *cnt_zero,
                          const int32_t *flagged = nullptr)
 {
-    constexpr int NL = 2 + kBigBins;
+    constexpr int NL = 3 + kBigBins;
     GBC_CUDA_TRY(cudaMemsetAsync(P.lcnt, 0, NL * sizeof(unsigned long long), s));
     const int64_t stride = P.total_cols + 1;
     int64_t *l0 = P.lbuf, *l1 = P.lbuf + stride, *l2 = P.lbuf + 2 * stride;
+    int64_t *lm = P.lbuf + (2 + kBigBins) * stride;
     for (int q = 0; q < (int)P.h.size(); ++q) {
         if (pid >= 0 && q != pid) continue;
         const SpgemmArgs &a = P.h[q];
         const int64_t lo = pid >= 0 ? j0 : 0, hi = (pid >= 0 && j1 >= 0) ? j1 : a.nb;
         if (hi > lo) {
             k_classify<<<(unsigned)((hi - lo + 255) / 256), 256, 0, s>>>(a.flop, q, a.col_base, lo, hi, P.s1, P.s2,
-                                                                         l0, l1, l2, stride, P.lcnt, cnt_zero,
+                                                                         l0, l1, l2, stride, lm, P.lcnt, cnt_zero,
                                                                          flagged);
             note_launch();
         }
@@ -1217,9 +1236,11 @@ static int plan_classify(Plan &P, cudaStream_t s, int pid, int64_t j0, int64_t j
     L.l[0] = l0;
     L.l[1] = l1;
     L.l[2] = l2;
+    L.l[3] = lm;
     L.n[0] = (int64_t)h[0];
     L.n[1] = (int64_t)h[1];
     L.n[2] = nbig;
+    L.n[3] = (int64_t)h[2 + kBigBins];
     return GBC_OK;
 }
 
@@ -1237,12 +1258,21 @@ static int run_symbolic(Context *ctx, Plan &P, const Lists &L, int64_t *cnt)
         note_launch();
     }
     if (L.n[1] > 0) {
-        constexpr int WPB = 4, TS = 2 * kSmall2;
+        constexpr int WPB = 8, TS = 2 * kSmallMid;
         const size_t sm = (size_t)WPB * TS * 4;
         GBC_TRY(set_smem(k_small_count<TS, WPB>, sm));
         int per_sm = std::max(1, (int)(ctx->smem_optin / (sm + 1024)));
         k_small_count<TS, WPB><<<grid_for(ctx, (L.n[1] + WPB - 1) / WPB, per_sm), WPB * 32, sm, s>>>(
             P.d, L.l[1], L.n[1], cnt);
+        note_launch();
+    }
+    if (L.n[3] > 0) {
+        constexpr int WPB = 4, TS = 2 * kSmall2;
+        const size_t sm = (size_t)WPB * TS * 4;
+        GBC_TRY(set_smem(k_small_count<TS, WPB>, sm));
+        int per_sm = std::max(1, (int)(ctx->smem_optin / (sm + 1024)));
+        k_small_count<TS, WPB><<<grid_for(ctx, (L.n[3] + WPB - 1) / WPB, per_sm), WPB * 32, sm, s>>>(
+            P.d, L.l[3], L.n[3], cnt);
         note_launch();
     }
     if (L.n[2] > 0) {
@@ -1352,10 +1382,18 @@ static int run_numeric(Context *ctx, Plan &P, const Lists &L, const int64_t *ccp
     }
     if (L.n[1] > 0) {
         if (pack)
-            GBC_TRY((launch_small<SR, kSmall2, 2, true>(ctx, P, L.l[1], L.n[1], ccp, ccp_base, cap, out_cnt, overflow,
+            GBC_TRY((launch_small<SR, kSmallMid, 4, true>(ctx, P, L.l[1], L.n[1], ccp, ccp_base, cap, out_cnt,
+                                                           overflow, cir, cval)));
+        else
+            GBC_TRY((launch_small<SR, kSmallMid, 4, false>(ctx, P, L.l[1], L.n[1], ccp, ccp_base, cap, out_cnt,
+                                                            overflow, cir, cval)));
+    }
+    if (L.n[3] > 0) {
+        if (pack)
+            GBC_TRY((launch_small<SR, kSmall2, 2, true>(ctx, P, L.l[3], L.n[3], ccp, ccp_base, cap, out_cnt, overflow,
                                                          cir, cval)));
         else
-            GBC_TRY((launch_small<SR, kSmall2, 2, false>(ctx, P, L.l[1], L.n[1], ccp, ccp_base, cap, out_cnt,
+            GBC_TRY((launch_small<SR, kSmall2, 2, false>(ctx, P, L.l[3], L.n[3], ccp, ccp_base, cap, out_cnt,
                                                           overflow, cir, cval)));
     }
     if (L.n[2] > 0) {
@@ -1844,7 +1882,7 @@ static int spgemm_phased(Context *ctx, const DevMatrix &A, const DevMatrix &B, i
         if (learned) {
             Lists Lo;
             GBC_TRY(plan_classify(P, s, 0, j0, j1, Lo, nullptr, flag));
-            const int64_t no = Lo.n[0] + Lo.n[1] + Lo.n[2];
+            const int64_t no = Lo.n[0] + Lo.n[1] + Lo.n[2] + Lo.n[3];
             overflow_cols += no;
             if (no > 0) {
                 cudaEventRecord(ctx->ev[3], s);
@@ -1993,7 +2031,7 @@ static int learned_into_slots(Context *ctx, Workspace &ws, const DevMatrix &A, c
         cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]);
         O.ms_numeric = ms;
     }
-    O.overflow_cols = Lo.n[0] + Lo.n[1] + Lo.n[2];
+    O.overflow_cols = Lo.n[0] + Lo.n[1] + Lo.n[2] + Lo.n[3];
     GBC_TRY(ws.alloc_n(&O.beg1, nb + 1));
     if (O.overflow_cols > 0) {
         cudaEventRecord(ctx->ev[5], s);
@@ -2519,7 +2557,8 @@ int gbc_batch_create(gbc_context *ctx, int sr, int vt, int nprob, const gbc_matr
     b->np = nprob;
     b->vsize = value_size(vt);
     b->P.s1 = s1 >= 0 ? std::min<int64_t>(s1, kSmall1) : kSmall1;
-    b->P.s2 = s2 >= 0 ? std::min<int64_t>(std::max(s2, b->P.s1), kSmall2) : kSmall2;
+    b->P.s2 = s2 >= 0 ? std::min<int64_t>(std::max(s2, b->P.s1), kSmall2) : GBC_SMALL2;
+    b->P.s2_set = s2 >= 0;
     std::vector<DevMatrix> dA(nprob), dB(nprob);
     int rc = GBC_OK;
     for (int p = 0; p < nprob && rc == GBC_OK; ++p) {

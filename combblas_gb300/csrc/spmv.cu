@@ -102,8 +102,14 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const uint32_t *key_i
         const int64_t it = w0 + r * 32 + lane;
         const bool act = it < n;
         const uint32_t k = act ? key_in[it] : 0;
-        const int d = act ? (int)((k >> shift) & (kRsRadix - 1)) : kRsRadix + lane;
-        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const int d = act ? (int)((k >> shift) & (kRsRadix - 1)) : 0;
+        // lanes holding the same digit, from eight ballots
+        unsigned peers = __ballot_sync(0xffffffffu, act);
+#pragma unroll
+        for (int bit = 0; bit < 8; ++bit) {
+            const unsigned bb = __ballot_sync(0xffffffffu, act && ((d >> bit) & 1));
+            peers &= ((d >> bit) & 1) ? bb : ~bb;
+        }
         if (act) {
             const int64_t dst = base[w][d] + __popc(peers & lt);
             key_out[dst] = k;

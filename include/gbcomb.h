@@ -88,8 +88,9 @@ typedef struct {
                         two, 16384 one */
     int64_t tiny_limit;  /* columns with <= this many multiplications use the
                             smallest warp kernel (<= 256; -1 = default 256) */
-    int64_t small_limit; /* ... <= this many the larger warp kernel (<= 4096;
-                            -1 = default 4096); above it the block kernel */
+    int64_t small_limit; /* ... <= this many the larger warp kernels (<= 4096;
+                            -1 = default: 4096, or 1024 for PlusTimes fp64 under
+                            the exact fold); above it the block kernel */
 } gbc_spgemm_opts;
 
 typedef struct {
