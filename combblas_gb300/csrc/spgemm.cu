@@ -185,16 +185,19 @@ __global__ void k_flop_mask(int64_t nb, const int64_t *bcp, const int32_t *brow,
 }
 
 // Split stored columns j0..j1-1 of one product by their flop count: empty
-// (count 0), small (<= s1 and <= s2 multiplications: warp kernels) and big
-// (block kernels).  The thresholds are tuning parameters (s1 <= kSmall1,
-// s2 <= kSmall2).  Lists are appended in any order; every column is written
-// to its own output range, so the order does not affect the result.
+// (count 0), small (up to s2 multiplications: warp kernels, in four sizes)
+// and big (block kernels).  The thresholds are tuning parameters (s1 <=
+// kSmall1, s2 <= kSmall2).  Lists are appended in any order; every column is
+// written to its own output range, so the order does not affect the result.
 constexpr int kSmall1 = 256;
 constexpr int kSmall2 = 4096;
-// Warp-kernel columns of at most kSmallMid multiplications run a kernel
-// sized for kSmallMid products (a quarter of the shared memory per warp:
-// four times the resident warps); the rest up to s2 the kSmall2 one.
+// Warp-kernel classes: at most s1, kSmallMid, kSmallMid2 and s2
+// multiplications, each run by a kernel sized for its largest column (a
+// smaller kernel keeps more warps resident: shared memory per warp is
+// proportional to the products it holds).
 constexpr int kSmallMid = 1024;
+constexpr int kSmallMid2 = 2048;
+constexpr int kWarpClasses = 4;
 #ifndef GBC_SMALL2
 #define GBC_SMALL2 kSmall2
 #endif
@@ -204,10 +207,12 @@ constexpr int kSmallMid = 1024;
 // run alone at the end of a launch (a scale-20 R-MAT hub column holds up to
 // 2*10^7 products, most of one block's share of a phase).
 constexpr int kBigBins = 4;
+constexpr int kBigList = kWarpClasses;            // index of the big list in Lists
+constexpr int kLists = kWarpClasses + kBigBins;  // list slots while classifying
 
 __global__ void k_classify(const int64_t *flop, int pid, int64_t col_base, int64_t j0, int64_t j1, int64_t s1,
-                           int64_t s2, int64_t *l1, int64_t *l2, int64_t *lb, int64_t lb_stride, int64_t *lm,
-                           unsigned long long *counts, int64_t *cnt_zero, const int32_t *only_flagged)
+                           int64_t s2, int64_t *lbuf, int64_t stride, unsigned long long *counts, int64_t *cnt_zero,
+                           const int32_t *only_flagged)
 {
     const int64_t i = j0 + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
@@ -218,23 +223,21 @@ __global__ void k_classify(const int64_t *flop, int pid, int64_t col_base, int64
             if (cnt_zero) cnt_zero[col_base + i] = 0;
         } else if (f <= s1) {
             cls = 0;
-        } else if (f <= s2 && f <= kSmallMid) {
-            cls = 1;
         } else if (f <= s2) {
-            cls = 2 + kBigBins;  // the larger warp kernel's list
+            cls = f <= kSmallMid ? 1 : f <= kSmallMid2 ? 2 : 3;
         } else {
-            cls = f > (1ll << 23) ? 2 : f > (1ll << 21) ? 3 : f > (1ll << 19) ? 4 : 5;
+            cls = kWarpClasses + (f > (1ll << 23) ? 0 : f > (1ll << 21) ? 1 : f > (1ll << 19) ? 2 : 3);
         }
     }
 #pragma unroll
-    for (int c = 0; c < 3 + kBigBins; ++c) {
+    for (int c = 0; c < kLists; ++c) {
         const unsigned m = __ballot_sync(0xffffffffu, cls == c);
         if (!m) continue;
         const int leader = __ffs(m) - 1;
         unsigned long long base = 0;
         if (lane == leader) base = atomicAdd(&counts[c], (unsigned long long)__popc(m));
         base = __shfl_sync(0xffffffffu, base, leader);
-        int64_t *list = c == 0 ? l1 : c == 1 ? l2 : c == 2 + kBigBins ? lm : lb + (c - 2) * lb_stride;
+        int64_t *list = lbuf + c * stride;
         if (cls == c) list[base + __popc(m & ((1u << lane) - 1))] = make_item(pid, i);
     }
 }
@@ -1029,7 +1032,7 @@ struct Plan {
     int64_t s1 = kSmall1, s2 = GBC_SMALL2;  // flop thresholds of the column classes
     int tile_rows = 0;                   // accumulator tile height (0: default)
     unsigned long long *work = nullptr;  // kernel work counters
-    int64_t *lbuf = nullptr;             // column lists ((3 + kBigBins) x (total_cols + 1))
+    int64_t *lbuf = nullptr;             // column lists (kLists x (total_cols + 1))
     bool s2_set = false;                 // the caller chose s2
     unsigned long long *lcnt = nullptr;  // list lengths
     bool want_aexp = false;              // PlusTimes fp64, exact accumulation (k_numeric_x)
@@ -1070,10 +1073,16 @@ static bool use_exact(const Plan &P)
 static size_t x_smem(int RS) { return (size_t)kXW * RS * 4 + RS; }
 
 struct Lists {
-    // [0] up to s1 multiplications, [1] up to kSmallMid, [2] the big list,
-    // [3] up to s2 (the larger warp kernel)
-    const int64_t *l[4] = {nullptr, nullptr, nullptr, nullptr};
-    int64_t n[4] = {0, 0, 0, 0};
+    // [0, kWarpClasses): the warp-kernel classes (up to s1, kSmallMid,
+    // kSmallMid2, s2 multiplications); [kBigList]: the big list
+    const int64_t *l[kWarpClasses + 1] = {};
+    int64_t n[kWarpClasses + 1] = {};
+    int64_t total() const
+    {
+        int64_t t = 0;
+        for (int c = 0; c <= kWarpClasses; ++c) t += n[c];
+        return t;
+    }
 };
 
 // Prepare one product (A*B) and append it to the plan.
@@ -1160,8 +1169,8 @@ static int plan_finalize(Workspace &ws, Plan &P)
     GBC_TRY(ws.alloc_n(&P.d, P.h.size() + 1));
     GBC_TRY(ws.alloc_n(&P.work, 16));
     GBC_CUDA_TRY(cudaMemsetAsync(P.work, 0, 16 * sizeof(unsigned long long), ws.ctx->stream));
-    GBC_TRY(ws.alloc_n(&P.lbuf, (3 + kBigBins) * ((size_t)P.total_cols + 1)));
-    GBC_TRY(ws.alloc_n(&P.lcnt, 3 + kBigBins));
+    GBC_TRY(ws.alloc_n(&P.lbuf, kLists * ((size_t)P.total_cols + 1)));
+    GBC_TRY(ws.alloc_n(&P.lcnt, kLists));
     if (P.want_aexp) {
         GBC_TRY(ws.alloc_n(&P.fb_items, (size_t)P.total_cols + 1));
         GBC_TRY(ws.alloc_n(&P.fb_cnt, 1));
@@ -1205,19 +1214,17 @@ static int plan_build(Workspace &ws, const DevMatrix &A, const DevMatrix &B, Pla
 static int plan_classify(Plan &P, cudaStream_t s, int pid, int64_t j0, int64_t j1, Lists &L, int64_t *cnt_zero,
                          const int32_t *flagged = nullptr)
 {
-    constexpr int NL = 3 + kBigBins;
+    constexpr int NL = kLists;
     GBC_CUDA_TRY(cudaMemsetAsync(P.lcnt, 0, NL * sizeof(unsigned long long), s));
     const int64_t stride = P.total_cols + 1;
-    int64_t *l0 = P.lbuf, *l1 = P.lbuf + stride, *l2 = P.lbuf + 2 * stride;
-    int64_t *lm = P.lbuf + (2 + kBigBins) * stride;
+    int64_t *lbig = P.lbuf + kWarpClasses * stride;
     for (int q = 0; q < (int)P.h.size(); ++q) {
         if (pid >= 0 && q != pid) continue;
         const SpgemmArgs &a = P.h[q];
         const int64_t lo = pid >= 0 ? j0 : 0, hi = (pid >= 0 && j1 >= 0) ? j1 : a.nb;
         if (hi > lo) {
             k_classify<<<(unsigned)((hi - lo + 255) / 256), 256, 0, s>>>(a.flop, q, a.col_base, lo, hi, P.s1, P.s2,
-                                                                         l0, l1, l2, stride, lm, P.lcnt, cnt_zero,
-                                                                         flagged);
+                                                                         P.lbuf, stride, P.lcnt, cnt_zero, flagged);
             note_launch();
         }
     }
@@ -1226,21 +1233,33 @@ static int plan_classify(Plan &P, cudaStream_t s, int pid, int64_t j0, int64_t j
     GBC_CUDA_TRY(cudaMemcpyAsync(h, P.lcnt, sizeof(h), cudaMemcpyDeviceToHost, s));
     GBC_CUDA_TRY(cudaStreamSynchronize(s));
     // the big list: bin 0 (heaviest) in place, the other bins appended
-    int64_t nbig = (int64_t)h[2];
+    int64_t nbig = (int64_t)h[kWarpClasses];
     for (int c = 1; c < kBigBins; ++c) {
-        const int64_t nc = (int64_t)h[2 + c];
+        const int64_t nc = (int64_t)h[kWarpClasses + c];
         if (nc > 0)
-            GBC_CUDA_TRY(cudaMemcpyAsync(l2 + nbig, l2 + c * stride, nc * sizeof(int64_t), cudaMemcpyDeviceToDevice, s));
+            GBC_CUDA_TRY(
+                cudaMemcpyAsync(lbig + nbig, lbig + c * stride, nc * sizeof(int64_t), cudaMemcpyDeviceToDevice, s));
         nbig += nc;
     }
-    L.l[0] = l0;
-    L.l[1] = l1;
-    L.l[2] = l2;
-    L.l[3] = lm;
-    L.n[0] = (int64_t)h[0];
-    L.n[1] = (int64_t)h[1];
-    L.n[2] = nbig;
-    L.n[3] = (int64_t)h[2 + kBigBins];
+    for (int c = 0; c < kWarpClasses; ++c) {
+        L.l[c] = P.lbuf + c * stride;
+        L.n[c] = (int64_t)h[c];
+    }
+    L.l[kBigList] = lbig;
+    L.n[kBigList] = nbig;
+    return GBC_OK;
+}
+
+// Warp-kernel counts of one class's columns (a TS-slot table per warp).
+template <int TS, int WPB>
+static int launch_small_count(Context *ctx, Plan &P, const int64_t *items, int64_t n, int64_t *cnt)
+{
+    const size_t sm = (size_t)WPB * TS * 4;
+    GBC_TRY(set_smem(k_small_count<TS, WPB>, sm));
+    const int per_sm = std::max(1, (int)(ctx->smem_optin / (sm + 1024)));
+    k_small_count<TS, WPB><<<grid_for(ctx, (n + WPB - 1) / WPB, per_sm), WPB * 32, sm, ctx->stream>>>(P.d, items, n,
+                                                                                                      cnt);
+    note_launch();
     return GBC_OK;
 }
 
@@ -1257,31 +1276,16 @@ static int run_symbolic(Context *ctx, Plan &P, const Lists &L, int64_t *cnt)
                                                                                                  cnt);
         note_launch();
     }
-    if (L.n[1] > 0) {
-        constexpr int WPB = 8, TS = 2 * kSmallMid;
-        const size_t sm = (size_t)WPB * TS * 4;
-        GBC_TRY(set_smem(k_small_count<TS, WPB>, sm));
-        int per_sm = std::max(1, (int)(ctx->smem_optin / (sm + 1024)));
-        k_small_count<TS, WPB><<<grid_for(ctx, (L.n[1] + WPB - 1) / WPB, per_sm), WPB * 32, sm, s>>>(
-            P.d, L.l[1], L.n[1], cnt);
-        note_launch();
-    }
-    if (L.n[3] > 0) {
-        constexpr int WPB = 4, TS = 2 * kSmall2;
-        const size_t sm = (size_t)WPB * TS * 4;
-        GBC_TRY(set_smem(k_small_count<TS, WPB>, sm));
-        int per_sm = std::max(1, (int)(ctx->smem_optin / (sm + 1024)));
-        k_small_count<TS, WPB><<<grid_for(ctx, (L.n[3] + WPB - 1) / WPB, per_sm), WPB * 32, sm, s>>>(
-            P.d, L.l[3], L.n[3], cnt);
-        note_launch();
-    }
-    if (L.n[2] > 0) {
+    if (L.n[1] > 0) GBC_TRY((launch_small_count<2 * kSmallMid, 8>(ctx, P, L.l[1], L.n[1], cnt)));
+    if (L.n[2] > 0) GBC_TRY((launch_small_count<2 * kSmallMid2, 4>(ctx, P, L.l[2], L.n[2], cnt)));
+    if (L.n[3] > 0) GBC_TRY((launch_small_count<2 * kSmall2, 4>(ctx, P, L.l[3], L.n[3], cnt)));
+    if (L.n[kBigList] > 0) {
         const size_t sym_smem = P.max_sym_smem;
         GBC_TRY(set_smem(k_symbolic, sym_smem));
         const int per_sm = resident_blocks(k_symbolic, kThreads, sym_smem, 8);
         GBC_CUDA_TRY(cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), s));
-        k_symbolic<<<grid_for(ctx, L.n[2], per_sm), kThreads, sym_smem, s>>>(P.d, L.l[2], L.n[2], cnt,
-                                                                                             P.work);
+        k_symbolic<<<grid_for(ctx, L.n[kBigList], per_sm), kThreads, sym_smem, s>>>(P.d, L.l[kBigList],
+                                                                                     L.n[kBigList], cnt, P.work);
         note_launch();
     }
     GBC_CUDA_TRY(cudaGetLastError());
@@ -1346,20 +1350,20 @@ static int launch_big_exact(Context *ctx, Plan &P, const Lists &L, const int64_t
                             const int64_t *cap, int64_t *out_cnt, int32_t *overflow, int64_t *cir, void *cval)
 {
     cudaStream_t s = ctx->stream;
-    const int grid = (int)std::min<int64_t>(P.x_blocks, L.n[2]);  // the scratch holds P.x_blocks blocks
+    const int grid = (int)std::min<int64_t>(P.x_blocks, L.n[kBigList]);  // the scratch holds P.x_blocks blocks
     GBC_CUDA_TRY(cudaMemsetAsync(P.work + 1, 0, 3 * sizeof(unsigned long long), s));
     GBC_CUDA_TRY(cudaMemsetAsync(P.fb_cnt, 0, sizeof(unsigned long long), s));
     if (P.max_R > kXRows)
         k_numeric_x<kXThreadsBig, kXRowsBig><<<grid, kXThreadsBig, x_smem(kXRowsBig), s>>>(
-            P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir, static_cast<double *>(cval),
+            P.d, L.l[kBigList], L.n[kBigList], ccp, ccp_base, cap, out_cnt, overflow, cir, static_cast<double *>(cval),
             P.work + 1, P.fb_items, P.fb_cnt, P.xscratch);
     else
         k_numeric_x<kXThreads, kXRows><<<grid, kXThreads, x_smem(kXRows), s>>>(
-            P.d, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt, overflow, cir, static_cast<double *>(cval),
+            P.d, L.l[kBigList], L.n[kBigList], ccp, ccp_base, cap, out_cnt, overflow, cir, static_cast<double *>(cval),
             P.work + 1, P.fb_items, P.fb_cnt, P.xscratch);
     note_launch();
     GBC_CUDA_TRY(cudaGetLastError());
-    return launch_big_ordered<SR>(ctx, P, P.fb_items, L.n[2], P.fb_cnt, ccp, ccp_base, cap, out_cnt, overflow, cir,
+    return launch_big_ordered<SR>(ctx, P, P.fb_items, L.n[kBigList], P.fb_cnt, ccp, ccp_base, cap, out_cnt, overflow, cir,
                                   cval);
 }
 
@@ -1388,6 +1392,14 @@ static int run_numeric(Context *ctx, Plan &P, const Lists &L, const int64_t *ccp
             GBC_TRY((launch_small<SR, kSmallMid, 4, false>(ctx, P, L.l[1], L.n[1], ccp, ccp_base, cap, out_cnt,
                                                             overflow, cir, cval)));
     }
+    if (L.n[2] > 0) {
+        if (pack)
+            GBC_TRY((launch_small<SR, kSmallMid2, 2, true>(ctx, P, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt,
+                                                            overflow, cir, cval)));
+        else
+            GBC_TRY((launch_small<SR, kSmallMid2, 2, false>(ctx, P, L.l[2], L.n[2], ccp, ccp_base, cap, out_cnt,
+                                                             overflow, cir, cval)));
+    }
     if (L.n[3] > 0) {
         if (pack)
             GBC_TRY((launch_small<SR, kSmall2, 2, true>(ctx, P, L.l[3], L.n[3], ccp, ccp_base, cap, out_cnt, overflow,
@@ -1396,11 +1408,12 @@ static int run_numeric(Context *ctx, Plan &P, const Lists &L, const int64_t *ccp
             GBC_TRY((launch_small<SR, kSmall2, 2, false>(ctx, P, L.l[3], L.n[3], ccp, ccp_base, cap, out_cnt,
                                                           overflow, cir, cval)));
     }
-    if (L.n[2] > 0) {
+    if (L.n[kBigList] > 0) {
         if (use_exact<SR>(P))
             GBC_TRY(launch_big_exact<SR>(ctx, P, L, ccp, ccp_base, cap, out_cnt, overflow, cir, cval));
         else
-            GBC_TRY(launch_big_ordered<SR>(ctx, P, L.l[2], L.n[2], nullptr, ccp, ccp_base, cap, out_cnt, overflow,
+            GBC_TRY(launch_big_ordered<SR>(ctx, P, L.l[kBigList], L.n[kBigList], nullptr, ccp, ccp_base, cap,
+                                           out_cnt, overflow,
                                            cir, cval));
     }
     GBC_CUDA_TRY(cudaGetLastError());
@@ -1882,7 +1895,7 @@ static int spgemm_phased(Context *ctx, const DevMatrix &A, const DevMatrix &B, i
         if (learned) {
             Lists Lo;
             GBC_TRY(plan_classify(P, s, 0, j0, j1, Lo, nullptr, flag));
-            const int64_t no = Lo.n[0] + Lo.n[1] + Lo.n[2] + Lo.n[3];
+            const int64_t no = Lo.total();
             overflow_cols += no;
             if (no > 0) {
                 cudaEventRecord(ctx->ev[3], s);
@@ -2031,7 +2044,7 @@ static int learned_into_slots(Context *ctx, Workspace &ws, const DevMatrix &A, c
         cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]);
         O.ms_numeric = ms;
     }
-    O.overflow_cols = Lo.n[0] + Lo.n[1] + Lo.n[2] + Lo.n[3];
+    O.overflow_cols = Lo.total();
     GBC_TRY(ws.alloc_n(&O.beg1, nb + 1));
     if (O.overflow_cols > 0) {
         cudaEventRecord(ctx->ev[5], s);
