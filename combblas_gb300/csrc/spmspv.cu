@@ -688,22 +688,36 @@ static int graph_alloc_bfs(Graph *g)
 static int32_t *const *fronts_dev(Graph *g) { return reinterpret_cast<int32_t *const *>(g->ctl + kCtlWords); }
 static uint32_t *const *fbits_dev(Graph *g) { return reinterpret_cast<uint32_t *const *>(g->ctl + kCtlWords + 2); }
 
+// A persistent grid of `kernel`: as many blocks as the occupancy query
+// allows on every SM (at least one).
+static int occ_grid(const Context *ctx, const void *kernel, int threads, size_t smem)
+{
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, threads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        nb = 4;
+    }
+    return ctx->num_sms * std::max(nb, 1);
+}
+
 static int launch_level(Graph *g, int64_t *parents, int64_t *levels, cudaStream_t s)
 {
     Context *ctx = g->ctx;
     const int grid = ctx->num_sms * 4;
+    const int grid_td = occ_grid(ctx, (const void *)k_bfs_td, kThreads, 0);
+    const int grid_bu = occ_grid(ctx, (const void *)k_bfs_bu, kThreads, 0);
     const int64_t words = (g->n + 31) / 32;
     const unsigned tiles = (unsigned)((g->n + kScanTile - 1) / kScanTile);
     k_bfs_direction<<<1, 1, 0, s>>>(g->ctl, g->n);
     k_bfs_deg_tiles<<<tiles, kThreads, 0, s>>>(g->cp32, g->ctl, fronts_dev(g), g->tile);
     k_bfs_deg_scan<<<1, kThreads, 0, s>>>(g->ctl, g->tile);
     k_bfs_deg_rescan<<<tiles, kThreads, 0, s>>>(g->cp32, g->ctl, fronts_dev(g), g->tile, g->off, g->chunk_f0);
-    k_bfs_td<<<grid, kThreads, 0, s>>>(g->cp32, g->row, g->visited, g->cand, g->ctl, fronts_dev(g), g->off,
-                                       g->chunk_f0);
+    k_bfs_td<<<grid_td, kThreads, 0, s>>>(g->cp32, g->row, g->visited, g->cand, g->ctl, fronts_dev(g), g->off,
+                                          g->chunk_f0);
     k_bfs_finalize<<<grid, 256, 0, s>>>(g->cand, g->visited, parents, levels, g->cp, g->ctl, fronts_dev(g),
                                         fbits_dev(g));
-    k_bfs_bu<<<grid, kThreads, 0, s>>>(g->cp, g->row, g->visited, parents, levels, g->n, g->ctl, fronts_dev(g),
-                                       fbits_dev(g));
+    k_bfs_bu<<<grid_bu, kThreads, 0, s>>>(g->cp, g->row, g->visited, parents, levels, g->n, g->ctl,
+                                          fronts_dev(g), fbits_dev(g));
     k_bfs_bu_mark<<<grid, 256, 0, s>>>(g->visited, g->ctl, fronts_dev(g));
     k_bfs_advance<<<1, 1, 0, s>>>(g->ctl);
     k_bfs_clear_bits<<<grid, 256, 0, s>>>(g->ctl, fbits_dev(g), words);
@@ -1105,7 +1119,7 @@ static int ms_launch_level(Graph *g, int64_t *parents, cudaStream_t s)
 {
     const int grid = g->ctx->num_sms * 4;
     const int sorted = g->ms_roots <= kMsSortRoots ? 1 : 0;
-    k_ms_expand<<<grid, kThreads, 0, s>>>(g->cp32, g->row, g->n, g->ms_visited, g->ms_cand, g->ms_ctl,
+    k_ms_expand<<<occ_grid(g->ctx, (const void *)k_ms_expand, kThreads, 0), kThreads, 0, s>>>(g->cp32, g->row, g->n, g->ms_visited, g->ms_cand, g->ms_ctl,
                                           ms_fronts_dev(g));
     note_launch();
     if (sorted) {
