@@ -758,7 +758,7 @@ static int level_graph(Graph *g, int64_t *parents, int64_t *levels)
     if (g->loop_exec) cudaGraphExecDestroy(g->loop_exec);
     g->loop_exec = nullptr;
     // the whole traversal as one while node (replays of the level graph with
-    // a host check every few levels remain the path where the driver cannot
+    // a host check every few levels remain the path where the CUDA driver cannot
     // build conditional nodes)
     loop_graph([&](cudaStream_t cs) { return launch_level(g, parents, levels, cs); }, g->ctl + CTL_NF,
                g->ctl + CTL_ITER, g->n + 2, &g->loop_exec, &g->loop_kernels);
