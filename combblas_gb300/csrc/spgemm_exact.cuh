@@ -372,8 +372,8 @@ struct XSeg {
     uint32_t start, len, e;
 };
 
-constexpr int kXTMax = 256;                   // row tiles of a bucketed column (rows <= 256 * kXRows)
-constexpr int kXRange = 4096;                 // products of one sorted range visit
+constexpr int kXTMax = 256;                   // row tiles of a bucketed column
+constexpr int kXRange = 4096;                 // products of one sorted range visit (at most; RS for smaller tiles)
 #ifndef GBC_XDENSE
 #define GBC_XDENSE 512
 #endif
@@ -387,10 +387,11 @@ constexpr int64_t kXScap = int64_t(1) << 18;  // bucketed segments of one column
 //     into the block's scratch grouped by tile (a counting sort; the exact
 //     sum makes the order irrelevant).  Each tile is then visited with its
 //     own segments only, instead of looking up every B entry per tile.
-//  2. visits in row order -- a tile with more than kXRange products is a
+//  2. visits in row order -- a tile with more than kXDense products is a
 //     dense visit: products added with x_add into the shared-memory word
 //     accumulator, touched rows written in row order.  Consecutive lighter
-//     tiles are merged into one range of at most kXRange products: the
+//     tiles are merged into one range of at most kXRange products (RS for
+//     smaller tiles): the
 //     products (x_mul) are staged in shared memory with (row, slot) keys,
 //     radix sorted by row (stable LSD, 7-bit digits), and each run of one
 //     row is summed exactly (x_acc128) and rounded (x_round).
@@ -405,20 +406,22 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
                 unsigned long long *work, int64_t *fb_items, unsigned long long *fb_count, XSeg *scratch_all)
 {
     constexpr int NW = NT / 32;  // RS: rows of the tile = word stride
-    constexpr int TM = (1 << 20) / RS;  // tiles of a bucketed column
-    static_assert(kXRange == 4096 && NT * 8 >= kXRange && (NW * 128) % NT == 0 && RS % (32 * NW) == 0 &&
-                      TM * RS <= (1 << 20) && TM <= kXTMax,
+    constexpr int TM = (1 << 20) / RS;             // tiles of a bucketed column
+    constexpr int XR = RS < kXRange ? RS : kXRange;  // products of one range visit
+    // TM <= NT: the bucketing's block-wide prefix gives every tile its offset
+    static_assert(XR <= 4096 && XR >= kXDense && (NW * 128) % NT == 0 && RS % (32 * NW) == 0 &&
+                      TM * RS <= (1 << 20) && TM <= kXTMax && TM <= NT,
                   "range keys: 20-bit row offset and 12-bit slot; eight sorted keys per thread");
     extern __shared__ __align__(16) int32_t xsm[];
     int32_t *acc = xsm;                                           // [kXW][RS]
     uint32_t *tw = reinterpret_cast<uint32_t *>(xsm + kXW * RS);  // [RS/4] flag bytes
     uint8_t *tfb = reinterpret_cast<uint8_t *>(tw);
     // range visits reuse the word area (it is cleared again before a dense visit)
-    uint32_t *rk0 = reinterpret_cast<uint32_t *>(xsm);               // [kXRange] keys
-    uint32_t *rk1 = rk0 + kXRange;                                   // [kXRange] keys (sort buffer)
-    uint64_t *rval = reinterpret_cast<uint64_t *>(rk1 + kXRange);    // [kXRange] products
-    uint32_t *rwh = reinterpret_cast<uint32_t *>(rval + kXRange);    // [NW][128] digit counts per warp
-    static_assert(2 * kXRange * 4 + kXRange * 8 + NW * 128 * 4 <= kXW * RS * 4, "range area inside the words");
+    uint32_t *rk0 = reinterpret_cast<uint32_t *>(xsm);          // [XR] keys
+    uint32_t *rk1 = rk0 + XR;                                   // [XR] keys (sort buffer)
+    uint64_t *rval = reinterpret_cast<uint64_t *>(rk1 + XR);    // [XR] products
+    uint32_t *rwh = reinterpret_cast<uint32_t *>(rval + XR);    // [NW][128] digit counts per warp
+    static_assert(2 * XR * 4 + XR * 8 + NW * 128 * 4 <= kXW * RS * 4, "range area inside the words");
     __shared__ ChunkSmemN<NT> ch;
     static_assert(sizeof(ChunkSmemN<NT>) >= NW * 128 * 2, "write-out row lists fit the chunk table");
     __shared__ uint32_t ch_e[NT];
@@ -722,7 +725,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
                     // range visit of light tiles t .. t1 (at most kXRange products)
                     int t1 = t, prods = s_prodcnt[t];
                     while (t1 + 1 < a.T && (s_segcnt[t1 + 1] == 0 ||
-                                            (s_prodcnt[t1 + 1] <= kXDense && prods + s_prodcnt[t1 + 1] <= kXRange))) {
+                                            (s_prodcnt[t1 + 1] <= kXDense && prods + s_prodcnt[t1 + 1] <= XR))) {
                         ++t1;
                         prods += s_prodcnt[t1];
                     }
