@@ -714,7 +714,8 @@ static int launch_level(Graph *g, int64_t *parents, int64_t *levels, cudaStream_
     k_bfs_deg_rescan<<<tiles, kThreads, 0, s>>>(g->cp32, g->ctl, fronts_dev(g), g->tile, g->off, g->chunk_f0);
     k_bfs_td<<<grid_td, kThreads, 0, s>>>(g->cp32, g->row, g->visited, g->cand, g->ctl, fronts_dev(g), g->off,
                                           g->chunk_f0);
-    k_bfs_finalize<<<grid, 256, 0, s>>>(g->cand, g->visited, parents, levels, g->cp, g->ctl, fronts_dev(g),
+    k_bfs_finalize<<<occ_grid(ctx, (const void *)k_bfs_finalize, 256, 0), 256, 0, s>>>(
+        g->cand, g->visited, parents, levels, g->cp, g->ctl, fronts_dev(g),
                                         fbits_dev(g));
     k_bfs_bu<<<grid_bu, kThreads, 0, s>>>(g->cp, g->row, g->visited, parents, levels, g->n, g->ctl,
                                           fronts_dev(g), fbits_dev(g));
@@ -1129,7 +1130,8 @@ static int ms_launch_level(Graph *g, int64_t *parents, cudaStream_t s)
             g->ms_ctl, ms_fronts_dev(g), g->ms_roff);
         note_launches(3);
     }
-    k_ms_finalize<<<grid, 256, 0, s>>>(g->ms_cand, g->ms_visited, parents, g->cp32, g->n, g->ms_ctl,
+    k_ms_finalize<<<occ_grid(g->ctx, (const void *)k_ms_finalize, 256, 0), 256, 0, s>>>(
+        g->ms_cand, g->ms_visited, parents, g->cp32, g->n, g->ms_ctl,
                                        ms_fronts_dev(g), sorted);
     k_ms_advance<<<1, 1, 0, s>>>(g->ms_ctl, sorted);
     note_launches(2);
