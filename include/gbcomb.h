@@ -83,9 +83,9 @@ typedef struct {
     int keep_empty;  /* 1: one output column per stored column of B (SpTuples
                         view); 0: drop empty output columns (SpDCCols view) */
     int tile_rows;   /* rows of the block kernel's accumulator tile: 0 = 4096
-                        up to 2^18 rows of A and 8192 above, or 4096 / 8192 /
-                        16384; 4096-row tiles run four blocks per SM, 8192
-                        two, 16384 one */
+                        up to 2^18 rows of A and 8192 above (4096 for PlusTimes
+                        fp64 under the exact fold), or 4096 / 8192 / 16384
+                        (at most 8192 under the exact fold) */
     int64_t tiny_limit;  /* columns with <= this many multiplications use the
                             smallest warp kernel (<= 256; -1 = default 256) */
     int64_t small_limit; /* ... <= this many the larger warp kernels (<= 4096;
