@@ -775,6 +775,15 @@ def _timed(stream, fn, reps):
     return e0.elapsed_time(e1) / reps
 
 
+def _pinned_result_buffers(R):
+    """Pinned host arrays for a result's cp, jc, ir and values."""
+    import torch
+
+    vt = torch.float64 if np.dtype(R.dtype) == np.float64 else torch.float32
+    return [torch.empty(max(n, 1), dtype=t).pin_memory()
+            for n, t in ((R.nzc + 1, torch.int64), (R.nzc, torch.int64), (R.nnz, torch.int64), (R.nnz, vt))]
+
+
 def _same(a, b):
     """Bit-exact equality of (colptr, rows, values) triples."""
     return all(np.array_equal(np.asarray(x).view(np.int64) if np.asarray(x).dtype == np.float64 else x,
@@ -836,16 +845,21 @@ def bench_c1(args, ctx, stream, hbm, peak_kind):
     exact_ok = _same(got, O.port_spgemm(A, A, O.SR_PLUSTIMES_F64, fold="exact"))
     ordered_ok = _same(LC.spgemm(Ad, Ad, ctx=ctx, fold="ordered").to_csc(), (pcp, prow, pval))
     ba = bytes_alg(A.nnz, A.ncol, s0.nnz)
-    # e2e: host CSC in (pinned), the whole product read back
+    # e2e: host CSC in (pinned), the whole product read back into pinned
+    # host arrays (allocated once, like the caller's output buffers)
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
     Ah = G.CSC(A.nrow, A.ncol, pin(A.colptr), pin(A.rowidx), pin(A.values))
+    R = LC.spgemm(Ah, Ah, ctx=ctx)
+    outs = _pinned_result_buffers(R)
+    R.free()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(reps):
         R = LC.spgemm(Ah, Ah, ctx=ctx)
-        R.to_csc()
+        R.copy_to(*[o.data_ptr() for o in outs])
         R.free()
     e2e_s = (time.perf_counter() - t0) / reps
+    d2h = sum(o.numel() * o.element_size() for o in outs)
     return {
         "workload": "R-MAT s14 ef8 A*A, PlusTimes fp64 (exact fold), exact two-phase, inputs resident",
         "value": s0.flops / (ms * 1e-3) / 1e9, "unit": "Gmults/s", "ms_per_step": ms, "flops": s0.flops,
@@ -857,8 +871,9 @@ def bench_c1(args, ctx, stream, hbm, peak_kind):
                          "kind": "port", "sample": "the whole product (oracle/oracle.c, the reference's hash path)"},
         "e2e": {"value": s0.flops / e2e_s / 1e9, "unit": "Gmults/s",
                 "h2d_bytes_per_step": int(2 * (A.colptr.nbytes + A.rowidx.nbytes + A.values.nbytes)),
-                "d2h_bytes_per_step": int(s0.nnz * 16 + (A.ncol + 1) * 8),
-                "path": "gbc_spgemm with pinned host CSC inputs, the product copied back to the host"},
+                "d2h_bytes_per_step": int(d2h),
+                "path": "gbc_spgemm with pinned host CSC inputs, the product (cp, jc, ir, num) copied back "
+                        "into pinned host arrays"},
         "parity": {"ok": bool(exact_ok and ordered_ok), "exact_fold_vs_oracle": bool(exact_ok),
                    "ordered_fold_vs_oracle": bool(ordered_ok), "check": "whole product, bit-exact"},
     }
@@ -945,15 +960,22 @@ def bench_c3(ctx, hbm, peak_kind):
     cpu_s = time.perf_counter() - t0
     exp = O.canonical_csc(scp, srow, sval)
     ok = all(np.array_equal(x, y) for x, y in zip(got, exp))
-    # e2e: the host matrix in, the selected product back
+    # e2e: the host matrix in (pinned), the selected product back into
+    # pinned host arrays
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    Ap = G.CSC(A.nrow, A.ncol, pin(A.colptr), pin(A.rowidx), pin(np.asarray(A.values, np.float32)))
+    R, st_e = MCL.mcl_expand(Ap, 1e-4, 100, ctx=ctx)
+    outs = _pinned_result_buffers(R)
+    R.free()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     reps = 3
     for _ in range(reps):
-        R, st_e = MCL.mcl_expand(A, 1e-4, 100, ctx=ctx)
-        R.to_csc()
+        R, st_e = MCL.mcl_expand(Ap, 1e-4, 100, ctx=ctx)
+        R.copy_to(*[o.data_ptr() for o in outs])
         R.free()
     e2e_s = (time.perf_counter() - t0) / reps
+    d2h = sum(o.numel() * o.element_size() for o in outs)
     ex = out["exact"]
     nnz_sel = len(exp[1])
     ba = 2 * (A.nnz * 12 + (n + 1) * 8) + ex["nnz_c"] * 12 + ex["nnz_c"] * 12 + nnz_sel * 12
@@ -967,8 +989,9 @@ def bench_c3(ctx, hbm, peak_kind):
                          "kind": "port", "sample": "the whole step (hash-path product + MCLPruneRecoverySelect restatement)"},
         "e2e": {"value": st_e.flops / e2e_s / 1e9, "unit": "Gmults/s",
                 "h2d_bytes_per_step": int(A.colptr.nbytes + A.rowidx.nbytes + A.values.nbytes),
-                "d2h_bytes_per_step": int(nnz_sel * 12 + (n + 1) * 8),
-                "path": "gbc_mcl_expand_f32 from host CSC, the selected product copied back"},
+                "d2h_bytes_per_step": int(d2h),
+                "path": "gbc_mcl_expand_recover_f32 from pinned host CSC, the selected product (cp, jc, ir, num) "
+                        "copied back into pinned host arrays"},
         "parity": {"ok": bool(ok), "check": "the whole selected product bit-exact against the oracle "
                                             "(PlusTimes fp32 product in hash order + prune/select)"},
     })

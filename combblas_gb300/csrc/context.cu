@@ -362,7 +362,11 @@ int gbc_result_copy(const gbc_result *r, int64_t *cp, int64_t *jc, int64_t *ir, 
     cudaMemcpyKind k = where == GBC_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     cudaStream_t s = r->ctx->stream;
     if (cp) GBC_CUDA_TRY(cudaMemcpyAsync(cp, r->cp, (r->nzc + 1) * sizeof(int64_t), k, s));
-    if (jc && r->nzc) GBC_CUDA_TRY(cudaMemcpyAsync(jc, r->jc, r->nzc * sizeof(int64_t), k, s));
+    if (jc && r->nzc && r->jc) GBC_CUDA_TRY(cudaMemcpyAsync(jc, r->jc, r->nzc * sizeof(int64_t), k, s));
+    if (jc && r->nzc && !r->jc) {  // a CSC result: stored column i is column i
+        if (where == GBC_DEVICE) return fail(GBC_EINVAL, "the result has no column ids (CSC form)");
+        for (int64_t i = 0; i < r->nzc; ++i) jc[i] = i;
+    }
     if (ir && r->nnz) GBC_CUDA_TRY(cudaMemcpyAsync(ir, r->ir, r->nnz * sizeof(int64_t), k, s));
     if (num && r->nnz) GBC_CUDA_TRY(cudaMemcpyAsync(num, r->num, r->nnz * value_size(r->valtype), k, s));
     GBC_CUDA_TRY(cudaStreamSynchronize(s));
