@@ -26,12 +26,12 @@
 //    the GPU (different streams, or host threads racing) corrupt each other
 //    and must be serialised by the caller;
 //  * the first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (with that device current) and caches it; make
-//    that first call before any stream capture begins.  If the lookup
-//    reports an error the cache entry stays empty and the next call tries
-//    again;
+//    cudaGetSymbolAddress (with that device current) and caches it.  If
+//    the lookup reports an error the cache entry stays empty and the next
+//    call tries again;
 //  * every call reads its error flag and output count back to the host and
-//    waits for `stream` to finish before it returns.
+//    waits for `stream` to finish before it returns, so no call can be
+//    captured into a CUDA graph.
 #include <mutex>
 
 #include "gbc_internal.cuh"

@@ -418,9 +418,9 @@ int gbc_msbfs(gbc_context *ctx, gbc_graph *g, const int64_t *roots, int64_t nroo
  * lazy module loading (the default) during the first call on that device --
  * so make one warm-up call per device at start-up (nrow = 0, veclen = 0),
  * while the 8.4 MB are still free.  All calls share the array: calls that
- * overlap on the GPU race and must be serialised by the caller.  The first
- * call on a device looks up the array's address (cudaGetSymbolAddress) --
- * make it before any stream capture. */
+ * overlap on the GPU race and must be serialised by the caller.  Because
+ * every call reads the output count back and synchronises `stream`, no call
+ * can be captured into a CUDA graph: call it outside any stream capture. */
 int gbc_spmspv_select2ndmin_noalloc(int64_t nrow, int64_t ncol, int64_t nnz, const int64_t *cp, const int64_t *ir,
                                     const int32_t *indx, const int64_t *numx, int32_t veclen, int32_t *indy,
                                     int64_t *numy, int32_t *nnzy, void *stream);
