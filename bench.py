@@ -51,13 +51,13 @@ SEED = 1
 BFS_ROOTS = 64
 # DRAM bytes of k_numeric_x measured by ncu on a scale-20 column sample
 # (profiles/k_numeric_x_s20_cols4096.txt), used to scale roofline.traffic
-NUMERIC_DRAM_READ_PER_MULT = 6.17
+NUMERIC_DRAM_READ_PER_MULT = 6.23
+NUMERIC_DRAM_WRITE_PER_ENTRY = 17.34
 # The compiled reference's own hybrid path (heap columns below compression
 # ratio 2, hash above, mtSpGEMM.h:310-311) against the restatement timed here,
 # same samples and threads (8 x86 cores): s20 A*A(:, 4096 columns) 4.05 s vs
 # 3.82 s, s14 A*A 0.487 s vs 0.468 s.
 CPU_CALIBRATION = "the compiled reference's hybrid path needs 1.04-1.06x the port's time on the same samples"
-NUMERIC_DRAM_WRITE_PER_ENTRY = 17.22
 # DRAM bytes of the multi-source BFS kernels per scanned edge (expand +
 # finalize) as last captured, when each level was a separate graph launch
 # (profiles/launches_msbfs22.txt); the traversal is now one graph whose
