@@ -150,42 +150,134 @@ constexpr bool offloaded()
     }
 }
 
+// Host views of the reference's storage as C-ABI descriptors (no copies).
+// Dcsc (Dcsc.h): cp[nzc+1] pointers of the nzc nonempty columns jc[nzc],
+// ir / numx the entries.  Csc (csc.h): jc[n+1] holds the column pointers.
+// values = false leaves num null (pattern operands).
 template <class IT, class NT>
-gbc_matrix view(const combblas::SpDCCols<IT, NT> &M)
+gbc_matrix view_dcsc(const combblas::Dcsc<IT, NT> *d, int64_t nrow, int64_t ncol, bool values = true)
 {
     gbc_matrix g{};
-    g.nrow = M.getnrow();
-    g.ncol = M.getncol();
-    const combblas::Dcsc<IT, NT> *d = M.GetDCSC();
+    g.nrow = nrow;
+    g.ncol = ncol;
     g.nzc = d ? d->nzc : 0;
     g.nnz = d ? d->nz : 0;
     g.cp = d ? d->cp : nullptr;
     g.jc = d ? d->jc : nullptr;
     g.ir = d ? d->ir : nullptr;
-    g.num = d ? d->numx : nullptr;
+    g.num = d && values ? static_cast<const void *>(d->numx) : nullptr;
     g.where = GBC_HOST;
     return g;
 }
 
 template <class IT, class NT>
-gbc_matrix view(const combblas::SpCCols<IT, NT> &M)
+gbc_matrix view_csc(const combblas::Csc<IT, NT> *c, int64_t nrow, int64_t ncol, bool values = true)
 {
     gbc_matrix g{};
-    g.nrow = M.getnrow();
-    g.ncol = M.getncol();
-    const combblas::Csc<IT, NT> *c = M.GetCSC();
-    g.nzc = M.getncol();
+    g.nrow = nrow;
+    g.ncol = ncol;
+    g.nzc = ncol;
     g.nnz = c ? c->nz : 0;
     g.cp = c ? c->jc : nullptr;  // Csc::jc holds the column pointers
     g.jc = nullptr;
     g.ir = c ? c->ir : nullptr;
-    g.num = c ? c->num : nullptr;
+    g.num = c && values ? static_cast<const void *>(c->num) : nullptr;
     g.where = GBC_HOST;
     return g;
 }
 
-// Run the product and wrap it as the reference does: (row, col, value)
-// tuples in column-major order, rows ascending within a column.
+template <class IT, class NT>
+gbc_matrix view(const combblas::SpDCCols<IT, NT> &M)
+{
+    return view_dcsc(M.GetDCSC(), M.getnrow(), M.getncol());
+}
+
+template <class IT, class NT>
+gbc_matrix view(const combblas::SpCCols<IT, NT> &M)
+{
+    return view_csc(M.GetCSC(), M.getnrow(), M.getncol());
+}
+
+// A result's arrays (cp[nzc+1], jc[nzc] column ids, ir, num) as the
+// reference's tuple array: (row, col, value) in column-major order, rows
+// ascending within a column.  opnew: storage from ::operator new (the
+// SpTuples then takes isOpNew = true, as mtSpGEMM.h's products do), else
+// from new[] (MultiwayMerge.h's result).
+template <class IT, class NT>
+std::tuple<IT, IT, NT> *tuples_of(int64_t nzc, const int64_t *cp, const int64_t *jc, const int64_t *ir, const NT *num,
+                                  bool opnew)
+{
+    typedef std::tuple<IT, IT, NT> T;
+    const int64_t nnz = cp[nzc];
+    T *tuples = opnew ? static_cast<T *>(::operator new(sizeof(T) * (nnz > 0 ? nnz : 1)))
+                      : new T[nnz > 0 ? nnz : 1];
+    for (int64_t k = 0; k < nzc; ++k)
+        for (int64_t p = cp[k]; p < cp[k + 1]; ++p) {
+            if (opnew)
+                new (tuples + p) T((IT)ir[p], (IT)jc[k], num[p]);
+            else
+                tuples[p] = T((IT)ir[p], (IT)jc[k], num[p]);
+        }
+    return tuples;
+}
+
+// A column-sorted SpTuples as a host CSC (arrays owned by the struct).
+template <class NT>
+struct TupleCsc {
+    std::vector<int64_t> cp, ir;
+    std::unique_ptr<NT[]> num;  // NT may be bool: no std::vector
+    gbc_matrix g{};
+};
+
+template <class IT, class NT>
+void csc_of_tuples(const combblas::SpTuples<IT, NT> &T, IT mdim, IT ndim, TupleCsc<NT> &out)
+{
+    const int64_t nnz = T.getnnz();
+    out.cp.assign(ndim + 1, 0);
+    out.ir.resize(nnz);
+    out.num.reset(new NT[nnz > 0 ? nnz : 1]);
+    for (int64_t p = 0; p < nnz; ++p) {
+        ++out.cp[T.colindex(p) + 1];
+        out.ir[p] = T.rowindex(p);
+        out.num[p] = T.numvalue(p);
+    }
+    for (IT j = 0; j < ndim; ++j) out.cp[j + 1] += out.cp[j];
+    gbc_matrix &g = out.g;
+    g = gbc_matrix{};
+    g.nrow = mdim;
+    g.ncol = ndim;
+    g.nzc = ndim;
+    g.nnz = nnz;
+    g.cp = out.cp.data();
+    g.jc = nullptr;
+    g.ir = nnz ? out.ir.data() : nullptr;
+    g.num = nnz ? static_cast<const void *>(out.num.get()) : nullptr;
+    g.where = GBC_HOST;
+}
+
+// Rows of y = A x (ascending, global) split among p_c receivers as the
+// optbuf SpMXSpV does (SpImpl.cpp:222-272): owner = min(row / (mA / p_c),
+// p_c - 1); each receiver's rows ascending and local to its offset;
+// cnts[p] entries land at indy / numy + dspls[p].
+template <class OVT>
+void split_rows(const std::vector<int32_t> &r, const std::vector<OVT> &v, int32_t mA, int32_t *indy, OVT *numy,
+                int *cnts, const int *dspls, int p_c)
+{
+    const int32_t perproc = p_c > 0 ? mA / p_c : mA;
+    for (int p = 0; p < p_c; ++p) cnts[p] = 0;
+    size_t k = 0;
+    for (int p = 0; p < p_c; ++p) {
+        const int32_t offset = perproc * p;
+        while (k < r.size() && (p == p_c - 1 || perproc == 0 || r[k] / perproc <= p)) {
+            indy[dspls[p] + cnts[p]] = r[k] - offset;
+            numy[dspls[p] + cnts[p]] = v[k];
+            ++cnts[p];
+            ++k;
+        }
+    }
+}
+
+// Run the product and wrap it as the reference does (tuples_of).
 template <class SR, class NTO, class IT>
 combblas::SpTuples<IT, NTO> *multiply(const gbc_matrix &A, const gbc_matrix &B, int sorted)
 {
@@ -201,11 +293,9 @@ combblas::SpTuples<IT, NTO> *multiply(const gbc_matrix &A, const gbc_matrix &B, 
                              nnz ? static_cast<void *>(num.get()) : nullptr, GBC_HOST);
     gbc_result_free(C);
     check(rc, "gbc_result_copy");
-    typedef std::tuple<IT, IT, NTO> T;
-    T *tuples = static_cast<T *>(::operator new(sizeof(T) * (nnz > 0 ? nnz : 1)));
-    for (int64_t k = 0; k < nzc; ++k)
-        for (int64_t p = cp[k]; p < cp[k + 1]; ++p) new (tuples + p) T(ir[p], jc[k], num[p]);
-    return new combblas::SpTuples<IT, NTO>(nnz, (IT)A.nrow, (IT)B.ncol, tuples, true, true);
+    return new combblas::SpTuples<IT, NTO>(nnz, (IT)A.nrow, (IT)B.ncol,
+                                           tuples_of<IT, NTO>(nzc, cp.data(), jc.data(), ir.data(), num.get(), true),
+                                           true, true);
 }
 
 template <class SR, class NTO, class M1, class M2>
@@ -301,32 +391,11 @@ combblas::SpTuples<IT, NT> *MultiwayMerge(std::vector<combblas::SpTuples<IT, NT>
                 return new combblas::SpTuples<IT, NT>(0, 0, 0);
             }
         // each list as a host CSC (tuples are column sorted)
-        std::vector<std::vector<int64_t>> cps(nlists), irs(nlists);
-        std::vector<std::unique_ptr<NT[]>> nums(nlists);
+        std::vector<detail::TupleCsc<NT>> lists(nlists);
         std::vector<gbc_matrix> mats(nlists);
         for (int k = 0; k < nlists; ++k) {
-            const combblas::SpTuples<IT, NT> &T = *ArrSpTups[k];
-            const int64_t nnz = T.getnnz();
-            cps[k].assign(ndim + 1, 0);
-            irs[k].resize(nnz);
-            nums[k].reset(new NT[nnz > 0 ? nnz : 1]);
-            for (int64_t p = 0; p < nnz; ++p) {
-                ++cps[k][T.colindex(p) + 1];
-                irs[k][p] = T.rowindex(p);
-                nums[k][p] = T.numvalue(p);
-            }
-            for (IT j = 0; j < ndim; ++j) cps[k][j + 1] += cps[k][j];
-            gbc_matrix &g = mats[k];
-            g = gbc_matrix{};
-            g.nrow = mdim;
-            g.ncol = ndim;
-            g.nzc = ndim;
-            g.nnz = nnz;
-            g.cp = cps[k].data();
-            g.jc = nullptr;
-            g.ir = nnz ? irs[k].data() : nullptr;
-            g.num = nnz ? static_cast<const void *>(nums[k].get()) : nullptr;
-            g.where = GBC_HOST;
+            detail::csc_of_tuples(*ArrSpTups[k], mdim, ndim, lists[k]);
+            mats[k] = lists[k].g;
         }
         gbc_result *C = nullptr;
         detail::check(gbc_multiway_merge(detail::context(), semiring_of<SR>::sr, semiring_of<SR>::vt, nlists,
@@ -341,9 +410,7 @@ combblas::SpTuples<IT, NT> *MultiwayMerge(std::vector<combblas::SpTuples<IT, NT>
                                        nnz ? static_cast<void *>(num.get()) : nullptr, GBC_HOST);
         gbc_result_free(C);
         detail::check(rc, "gbc_result_copy");
-        auto *tuples = new std::tuple<IT, IT, NT>[nnz > 0 ? nnz : 1];
-        for (int64_t k = 0; k < nzc; ++k)
-            for (int64_t p = cp[k]; p < cp[k + 1]; ++p) tuples[p] = std::tuple<IT, IT, NT>(ir[p], jc[k], num[p]);
+        auto *tuples = detail::tuples_of<IT, NT>(nzc, cp.data(), jc.data(), ir.data(), num.get(), false);
         if (delarrs)
             for (int k = 0; k < nlists; ++k) delete ArrSpTups[k];
         return new combblas::SpTuples<IT, NT>(nnz, mdim, ndim, tuples, true, false);
@@ -528,15 +595,7 @@ void SpMXSpV(const combblas::Csc<IT, NUM> &Acsc, int32_t mA, const int32_t *indx
     if constexpr (vt < 0 || !std::is_same<IT, int64_t>::value) {
         combblas::SpMXSpV<SR>(Acsc, mA, indx, numx, veclen, indy, numy, SPA);
     } else {
-        gbc_matrix g{};
-        g.nrow = mA;
-        g.ncol = Acsc.n;
-        g.nzc = Acsc.n;
-        g.nnz = Acsc.nz;
-        g.cp = Acsc.jc;  // Csc::jc holds the column pointers
-        g.ir = Acsc.ir;
-        g.num = vt == GBC_BOOL ? nullptr : static_cast<const void *>(Acsc.num);
-        g.where = GBC_HOST;
+        const gbc_matrix g = detail::view_csc(&Acsc, mA, Acsc.n, vt != GBC_BOOL);
         std::vector<int32_t> r;
         std::vector<OVT> v;
         detail::spmspv_run<SR>(g, vt, indx, numx, veclen, r, v);
@@ -557,31 +616,13 @@ void SpMXSpV(const combblas::Dcsc<IT, NUM> &Adcsc, int32_t mA, const int32_t *in
     if constexpr (vt < 0 || !std::is_same<IT, int64_t>::value) {
         combblas::SpMXSpV<SR>(Adcsc, mA, indx, numx, veclen, indy, numy, cnts, dspls, p_c);
     } else {
-        gbc_matrix g{};
-        g.nrow = mA;
-        g.ncol = Adcsc.nzc > 0 ? Adcsc.jc[Adcsc.nzc - 1] + 1 : 0;
-        g.nzc = Adcsc.nzc;
-        g.nnz = Adcsc.nz;
-        g.cp = Adcsc.cp;
-        g.jc = Adcsc.jc;
-        g.ir = Adcsc.ir;
-        g.num = vt == GBC_BOOL ? nullptr : static_cast<const void *>(Adcsc.numx);
-        g.where = GBC_HOST;
+        // a Dcsc does not store its column count: its last nonempty column bounds it
+        const gbc_matrix g =
+            detail::view_dcsc(&Adcsc, mA, Adcsc.nzc > 0 ? Adcsc.jc[Adcsc.nzc - 1] + 1 : 0, vt != GBC_BOOL);
         std::vector<int32_t> r;
         std::vector<OVT> v;
         if (g.nnz > 0) detail::spmspv_run<SR>(g, vt, indx, numx, veclen, r, v);
-        const int32_t perproc = p_c > 0 ? mA / p_c : mA;
-        for (int p = 0; p < p_c; ++p) cnts[p] = 0;
-        size_t k = 0;
-        for (int p = 0; p < p_c; ++p) {
-            const int32_t offset = perproc * p;
-            while (k < r.size() && (p == p_c - 1 || perproc == 0 || r[k] / perproc <= p)) {
-                indy[dspls[p] + cnts[p]] = r[k] - offset;
-                numy[dspls[p] + cnts[p]] = v[k];
-                ++cnts[p];
-                ++k;
-            }
-        }
+        detail::split_rows(r, v, mA, indy, numy, cnts, dspls, p_c);
     }
 }
 

@@ -1,6 +1,8 @@
 """The C++ drop-in header (include/gbcomb/combblas_shim.hpp): compiled
-against the reference's own headers where they exist, and against the
-stand-in types everywhere; run on a GPU it must reproduce the CPU product."""
+against the reference's own headers where they exist, its host-side layout
+code run against the reference's own types there (CPU), and compiled against
+the stand-in types everywhere; run on a GPU it must reproduce the CPU
+product."""
 import os
 import shutil
 import subprocess
@@ -26,6 +28,15 @@ def test_shim_compiles_against_reference_headers():
     if out.strip().endswith("skip"):
         pytest.skip("reference sources not present")
     assert "refcheck-ok" in out
+
+
+def test_shim_layout_matches_reference_types():
+    """The shim's views, tuple wrapping, tuple-to-CSC reading and optbuf row
+    split, run against the reference's own classes and SpMXSpV on the CPU."""
+    out = make("reflayout")
+    if out.strip().endswith("skip"):
+        pytest.skip("reference sources not present")
+    assert "layout-ok" in out, out
 
 
 def test_shim_mock_builds():
