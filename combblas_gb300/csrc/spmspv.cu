@@ -47,6 +47,7 @@ struct Graph {
     cudaGraphExec_t loop_exec = nullptr;  // the whole traversal: a while node around one level
     long long loop_kernels = 0;           // kernels of one trip of its body
     int64_t *g_parents = nullptr, *g_levels = nullptr;  // pointers baked into the graph
+    int g_policy = -1;                                   // the direction policy it was captured for
     int64_t *own_parents = nullptr, *own_levels = nullptr;  // device outputs of host-array calls
     bool bfs_ready = false;
     int policy = 0;  // direction policy (see gbc_graph_set_policy)
@@ -240,8 +241,9 @@ __device__ __forceinline__ void queue_flush(int32_t *q, int &s_qn, unsigned long
     __syncthreads();
 }
 
-// Per level: pick the direction (one thread).
-__global__ void k_bfs_direction(int64_t *ctl, int64_t n)
+// Direction of the level about to run (one thread: the end of the previous
+// level, or the traversal's initialisation for the first level).
+__device__ void bfs_direction(int64_t *ctl, int64_t n)
 {
     const int64_t nf = ctl[CTL_NF];
     if (nf == 0) return;
@@ -533,39 +535,44 @@ __global__ void __launch_bounds__(kThreads) k_bfs_bu(const int64_t *cp, const in
     }
 }
 
-// Visited bits of the bottom-up level's new vertices are set after the
-// level, so a vertex found in this level is never taken as a parent in it
-// (only frontier bits are read there).
-__global__ void k_bfs_bu_mark(uint32_t *visited, const int64_t *ctl, int32_t *const *fronts)
+// End of a level whose direction may be bottom-up: the current frontier's
+// bitmap (read only by the bottom-up kernel) is cleared, so it can collect
+// the frontier after next; after a bottom-up level the new vertices are
+// marked visited -- after the level, so a vertex found in it is never taken
+// as a parent in it (only frontier bits are read there).
+__global__ void k_bfs_level_end(uint32_t *visited, const int64_t *ctl, int32_t *const *fronts,
+                                uint32_t *const *fbits, int64_t words)
 {
-    if (ctl[CTL_NF] == 0 || ctl[CTL_DIR] != 1) return;
-    const int32_t *next = fronts[ctl[CTL_CUR] ^ 1];
+    if (ctl[CTL_NF] == 0) return;
+    const int cur = (int)ctl[CTL_CUR];
+    const int64_t i0 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x, stride = int64_t(gridDim.x) * blockDim.x;
+    uint32_t *fb = fbits[cur];
+    for (int64_t w = i0; w < words; w += stride) fb[w] = 0;
+    if (ctl[CTL_DIR] != 1) return;
+    const int32_t *next = fronts[cur ^ 1];
     const int64_t nn = ctl[CTL_NNEXT];
-    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < nn; i += int64_t(gridDim.x) * blockDim.x)
-        atomicOr(&visited[next[i] >> 5], 1u << (next[i] & 31));
+    for (int64_t i = i0; i < nn; i += stride) atomicOr(&visited[next[i] >> 5], 1u << (next[i] & 31));
 }
 
-// Advance the level: the next frontier becomes current; the old current
-// frontier bitmap is cleared for reuse.
-__global__ void k_bfs_advance(int64_t *ctl)
+// Advance the level (the next frontier becomes current) and choose the next
+// level's direction.  Inside a traversal graph (set_cond) it also sets the
+// while node's condition: another level while the frontier is nonempty, at
+// most `cap` levels (a level loop over n vertices ends within n + 1 levels,
+// so the cap never cuts a traversal short).
+__global__ void k_bfs_advance(int64_t *ctl, int64_t n, int64_t cap, cudaGraphConditionalHandle h, int set_cond)
 {
-    if (ctl[CTL_NF] == 0) return;  // finished: later replays change nothing
-    ctl[CTL_NF] = ctl[CTL_NNEXT];
-    ctl[CTL_NNEXT] = 0;
-    ctl[CTL_WORK] = 0;
-    ctl[CTL_ITER] += 1;
-    ctl[CTL_CUR] ^= 1;
-    ctl[CTL_UE] -= ctl[CTL_FE_NEXT];
-    ctl[CTL_FE] = ctl[CTL_FE_NEXT];
-    ctl[CTL_FE_NEXT] = 0;
-}
-
-__global__ void k_bfs_clear_bits(const int64_t *ctl, uint32_t *const *fbits, int64_t words)
-{
-    // after advance: clear the bitmap that will collect the next frontier
-    uint32_t *nb = fbits[ctl[CTL_CUR] ^ 1];
-    for (int64_t w = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; w < words; w += int64_t(gridDim.x) * blockDim.x)
-        nb[w] = 0;
+    if (ctl[CTL_NF] != 0) {  // else finished: later replays change nothing
+        ctl[CTL_NF] = ctl[CTL_NNEXT];
+        ctl[CTL_NNEXT] = 0;
+        ctl[CTL_WORK] = 0;
+        ctl[CTL_ITER] += 1;
+        ctl[CTL_CUR] ^= 1;
+        ctl[CTL_UE] -= ctl[CTL_FE_NEXT];
+        ctl[CTL_FE] = ctl[CTL_FE_NEXT];
+        ctl[CTL_FE_NEXT] = 0;
+        bfs_direction(ctl, n);
+    }
+    if (set_cond) cudaGraphSetConditional(h, (ctl[CTL_NF] != 0 && ctl[CTL_ITER] < cap) ? 1u : 0u);
 }
 
 __global__ void k_bfs_init(int64_t n, int64_t nnz, int32_t *cand, uint32_t *visited, int64_t *parents,
@@ -606,6 +613,7 @@ __global__ void k_bfs_init2(int64_t n, int64_t nnz, int64_t *levels, int64_t sou
     ctl[CTL_UE] = nnz;  // the source is still unreached for the reference's loop
     ctl[CTL_DIR] = 0;
     ctl[CTL_E] = 0;
+    bfs_direction(ctl, n);  // the first level's
 }
 
 // Condition of a traversal's while node: another level while the frontier
@@ -616,12 +624,13 @@ __global__ void k_loop_cond(const int64_t *nf, const int64_t *level, int64_t cap
     cudaGraphSetConditional(h, (*nf != 0 && *level < cap) ? 1u : 0u);
 }
 
-// An executable graph of one while node whose body is what `body` launches
-// on the capturing stream, followed by the condition kernel.  The whole
-// traversal then runs from one graph launch with no host round trip.
+// An executable graph of one while node whose body is what `body(stream,
+// handle)` launches on the capturing stream, followed by the condition
+// kernel unless the body sets the condition itself (body_sets_cond).  The
+// whole traversal then runs from one graph launch with no host round trip.
 template <class F>
-static int loop_graph(F body, const int64_t *nf, const int64_t *level, int64_t cap, cudaGraphExec_t *exec,
-                      long long *kernels)
+static int loop_graph(F body, bool body_sets_cond, const int64_t *nf, const int64_t *level, int64_t cap,
+                      cudaGraphExec_t *exec, long long *kernels)
 {
     cudaGraph_t graph = nullptr;
     GBC_CUDA_TRY(cudaGraphCreate(&graph, 0));
@@ -640,9 +649,11 @@ static int loop_graph(F body, const int64_t *nf, const int64_t *level, int64_t c
     int rc = GBC_OK;
     if (e == cudaSuccess) {
         const long long c0 = launch_count();
-        rc = body(cs);
-        k_loop_cond<<<1, 1, 0, cs>>>(nf, level, cap, h);
-        note_launch();
+        rc = body(cs, h);
+        if (!body_sets_cond) {
+            k_loop_cond<<<1, 1, 0, cs>>>(nf, level, cap, h);
+            note_launch();
+        }
         *kernels = launch_count() - c0;
         note_launches(-*kernels);  // captured, not run
         e = cudaStreamEndCapture(cs, &bodyg);
@@ -700,29 +711,40 @@ static int occ_grid(const Context *ctx, const void *kernel, int threads, size_t 
     return ctx->num_sms * std::max(nb, 1);
 }
 
-static int launch_level(Graph *g, int64_t *parents, int64_t *levels, cudaStream_t s)
+// One level.  The policy fixes which kernels can do work: always top-down
+// leaves out the bottom-up kernels (the frontier bitmaps are then never
+// read), always bottom-up leaves out the top-down ones; "auto" launches
+// both sets, the direction flag in the control block enabling one.  In a
+// traversal graph (set_cond) the advance kernel sets the while node's
+// condition h.
+static int launch_level(Graph *g, int64_t *parents, int64_t *levels, cudaStream_t s, cudaGraphConditionalHandle h,
+                        int set_cond)
 {
     Context *ctx = g->ctx;
     const int grid = ctx->num_sms * 4;
-    const int grid_td = occ_grid(ctx, (const void *)k_bfs_td, kThreads, 0);
-    const int grid_bu = occ_grid(ctx, (const void *)k_bfs_bu, kThreads, 0);
     const int64_t words = (g->n + 31) / 32;
     const unsigned tiles = (unsigned)((g->n + kScanTile - 1) / kScanTile);
-    k_bfs_direction<<<1, 1, 0, s>>>(g->ctl, g->n);
-    k_bfs_deg_tiles<<<tiles, kThreads, 0, s>>>(g->cp32, g->ctl, fronts_dev(g), g->tile);
-    k_bfs_deg_scan<<<1, kThreads, 0, s>>>(g->ctl, g->tile);
-    k_bfs_deg_rescan<<<tiles, kThreads, 0, s>>>(g->cp32, g->ctl, fronts_dev(g), g->tile, g->off, g->chunk_f0);
-    k_bfs_td<<<grid_td, kThreads, 0, s>>>(g->cp32, g->row, g->visited, g->cand, g->ctl, fronts_dev(g), g->off,
-                                          g->chunk_f0);
-    k_bfs_finalize<<<occ_grid(ctx, (const void *)k_bfs_finalize, 256, 0), 256, 0, s>>>(
-        g->cand, g->visited, parents, levels, g->cp, g->ctl, fronts_dev(g),
-                                        fbits_dev(g));
-    k_bfs_bu<<<grid_bu, kThreads, 0, s>>>(g->cp, g->row, g->visited, parents, levels, g->n, g->ctl,
-                                          fronts_dev(g), fbits_dev(g));
-    k_bfs_bu_mark<<<grid, 256, 0, s>>>(g->visited, g->ctl, fronts_dev(g));
-    k_bfs_advance<<<1, 1, 0, s>>>(g->ctl);
-    k_bfs_clear_bits<<<grid, 256, 0, s>>>(g->ctl, fbits_dev(g), words);
-    note_launches(10);
+    int launched = 1;
+    if (g->policy != 2) {
+        const int grid_td = occ_grid(ctx, (const void *)k_bfs_td, kThreads, 0);
+        k_bfs_deg_tiles<<<tiles, kThreads, 0, s>>>(g->cp32, g->ctl, fronts_dev(g), g->tile);
+        k_bfs_deg_scan<<<1, kThreads, 0, s>>>(g->ctl, g->tile);
+        k_bfs_deg_rescan<<<tiles, kThreads, 0, s>>>(g->cp32, g->ctl, fronts_dev(g), g->tile, g->off, g->chunk_f0);
+        k_bfs_td<<<grid_td, kThreads, 0, s>>>(g->cp32, g->row, g->visited, g->cand, g->ctl, fronts_dev(g), g->off,
+                                              g->chunk_f0);
+        k_bfs_finalize<<<occ_grid(ctx, (const void *)k_bfs_finalize, 256, 0), 256, 0, s>>>(
+            g->cand, g->visited, parents, levels, g->cp, g->ctl, fronts_dev(g), fbits_dev(g));
+        launched += 5;
+    }
+    if (g->policy != 1) {
+        const int grid_bu = occ_grid(ctx, (const void *)k_bfs_bu, kThreads, 0);
+        k_bfs_bu<<<grid_bu, kThreads, 0, s>>>(g->cp, g->row, g->visited, parents, levels, g->n, g->ctl,
+                                              fronts_dev(g), fbits_dev(g));
+        k_bfs_level_end<<<grid, 256, 0, s>>>(g->visited, g->ctl, fronts_dev(g), fbits_dev(g), words);
+        launched += 2;
+    }
+    k_bfs_advance<<<1, 1, 0, s>>>(g->ctl, g->n, g->n + 2, h, set_cond);
+    note_launches(launched);
     GBC_CUDA_TRY(cudaGetLastError());
     return GBC_OK;
 }
@@ -730,7 +752,8 @@ static int launch_level(Graph *g, int64_t *parents, int64_t *levels, cudaStream_
 // Capture one level into a graph once per (graph, output buffers).
 static int level_graph(Graph *g, int64_t *parents, int64_t *levels)
 {
-    if (g->level_exec && g->g_parents == parents && g->g_levels == levels) return GBC_OK;
+    if (g->level_exec && g->g_parents == parents && g->g_levels == levels && g->g_policy == g->policy)
+        return GBC_OK;
     if (g->level_exec) {
         cudaGraphExecDestroy(g->level_exec);
         g->level_exec = nullptr;
@@ -744,7 +767,7 @@ static int level_graph(Graph *g, int64_t *parents, int64_t *levels)
         cudaStreamDestroy(cs);
         return fail(GBC_ECUDA, std::string("capture: ") + cudaGetErrorString(e));
     }
-    int rc = launch_level(g, parents, levels, cs);
+    int rc = launch_level(g, parents, levels, cs, 0, 0);
     e = cudaStreamEndCapture(cs, &graph);
     g->level_kernels = launch_count() - c0;
     note_launches(-g->level_kernels);  // captured, not run
@@ -756,13 +779,14 @@ static int level_graph(Graph *g, int64_t *parents, int64_t *levels)
     if (e != cudaSuccess) return fail(GBC_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
     g->g_parents = parents;
     g->g_levels = levels;
+    g->g_policy = g->policy;
     if (g->loop_exec) cudaGraphExecDestroy(g->loop_exec);
     g->loop_exec = nullptr;
     // the whole traversal as one while node (replays of the level graph with
     // a host check every few levels remain the path where the CUDA driver cannot
     // build conditional nodes)
-    loop_graph([&](cudaStream_t cs) { return launch_level(g, parents, levels, cs); }, g->ctl + CTL_NF,
-               g->ctl + CTL_ITER, g->n + 2, &g->loop_exec, &g->loop_kernels);
+    loop_graph([&](cudaStream_t cs, cudaGraphConditionalHandle h) { return launch_level(g, parents, levels, cs, h, 1); },
+               true, g->ctl + CTL_NF, g->ctl + CTL_ITER, g->n + 2, &g->loop_exec, &g->loop_kernels);
     return GBC_OK;
 }
 
@@ -797,7 +821,7 @@ static int bfs_device(Graph *g, int64_t source, int64_t *parents, int64_t *level
                 GBC_CUDA_TRY(cudaGraphLaunch(g->level_exec, s));
                 note_launches(g->level_kernels);
             } else {
-                GBC_TRY(launch_level(g, parents, levels, s));
+                GBC_TRY(launch_level(g, parents, levels, s, 0, 0));
             }
         }
         GBC_CUDA_TRY(cudaMemcpyAsync(g->h_ctl, g->ctl, kCtlWords * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
@@ -1168,8 +1192,8 @@ static int ms_level_graph(Graph *g, int64_t *parents)
     g->ms_g_parents = parents;
     if (g->ms_loop_exec) cudaGraphExecDestroy(g->ms_loop_exec);
     g->ms_loop_exec = nullptr;
-    loop_graph([&](cudaStream_t cs) { return ms_launch_level(g, parents, cs); }, g->ms_ctl + MS_NF,
-               g->ms_ctl + MS_LEVEL, g->n + 2, &g->ms_loop_exec, &g->ms_loop_kernels);
+    loop_graph([&](cudaStream_t cs, cudaGraphConditionalHandle) { return ms_launch_level(g, parents, cs); }, false,
+               g->ms_ctl + MS_NF, g->ms_ctl + MS_LEVEL, g->n + 2, &g->ms_loop_exec, &g->ms_loop_kernels);
     return GBC_OK;
 }
 
