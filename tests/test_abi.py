@@ -32,8 +32,45 @@ def test_python_binding_covers_header():
 
 
 def test_library_has_no_torch_dependency():
-    # the C ABI stands alone: the shared object links the CUDA runtime only
+    # the C ABI stands alone: loaded into a fresh interpreter that never
+    # imports torch, it maps no torch library (its dependencies are the CUDA
+    # runtime and the C++ runtime)
+    import subprocess
+    import sys
+
     from combblas_gb300 import _lib
 
-    data = open(_lib.LIB_PATH, "rb").read()
-    assert b"libtorch" not in data and b"libc10" not in data
+    code = ("import ctypes, sys; ctypes.CDLL(sys.argv[1]); "
+            "print(open('/proc/self/maps').read())")
+    r = subprocess.run([sys.executable, "-c", code, _lib.LIB_PATH], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert "libgbcomb.so" in r.stdout
+    assert "libtorch" not in r.stdout and "libc10" not in r.stdout
+
+
+def test_product_code_does_not_use_the_oracle():
+    # the package (host side and CUDA sources) never imports, links or loads
+    # the oracle: only tests, smoke() and bench.py's CPU arms do
+    pkg = os.path.join(ROOT, "combblas_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        for f in files:
+            if not f.endswith((".py", ".cu", ".cuh", ".h", ".hpp")):
+                continue
+            src = open(os.path.join(dirpath, f)).read()
+            assert not re.search(r"^\s*(import|from)\s+oracle\b", src, re.M), f
+            assert "libgbc_oracle" not in src and "libcombblas_ref" not in src, f
+    for f in ("gbcomb.h", os.path.join("gbcomb", "combblas_shim.hpp")):
+        src = open(os.path.join(ROOT, "include", f)).read()
+        assert "oracle" not in src, f
+
+
+def test_missing_library_fails_loudly(monkeypatch):
+    # no CPU fallback: without the CUDA library every entry point raises
+    import pytest
+
+    from combblas_gb300 import _lib
+
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib, "LIB_PATH", os.path.join(ROOT, "combblas_gb300", "no-such-libgbcomb.so"))
+    with pytest.raises(ImportError):
+        _lib.lib()
