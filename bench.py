@@ -298,7 +298,8 @@ def run_reference(args, world, rank):
         "config": workload_config(args, scale, ef, world),
         "cpu_baseline": {"value": val, "unit": unit, "cores": threads, "kind": "port",
                          "sample": desc + " per step; the reference's CPU algorithm as restated in oracle/oracle.c "
-                                          "(the reference sources are not on this machine)"},
+                                          "(the compiled reference needs sources that the GPU hosts do not carry)",
+                         **({"calibration": CPU_CALIBRATION} if args.workload.startswith("spgemm") else {})},
         "e2e": {"value": val, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
