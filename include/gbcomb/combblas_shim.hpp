@@ -10,6 +10,7 @@
  *   gbcomb::LocalHybridSpGEMM<SR, NTO>(SpCCols A, SpCCols B, ...)  mtSpGEMM.h:1142-1152
  *   gbcomb::SpMXSpV<SR>(Csc, mA, indx, numx, veclen, indy, numy, SPA)  SpImpl.h:115-124
  *   gbcomb::SpMXSpV<SR>(Dcsc, mA, indx, numx, veclen, indy*, numy*, cnts, dspls, p_c)  SpImpl.h:59-65
+ *   gbcomb::SpMXSpV_ForThreading<SR>(Dcsc or Csc piece, ..., offset[, SPA buffers])  SpImpl.h:68-82, 126-142
  *   gbcomb::MultiwayMerge<SR>(ArrSpTups, mdim, ndim, delarrs)  MultiwayMerge.h:428-708
  *   gbcomb::dcsc_gespmv<SR>(A, x, y)                           Friends.h:63-77
  *
@@ -35,6 +36,7 @@
 #include <cstdio>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -525,12 +527,22 @@ constexpr int spmspv_vt()
     }
 }
 
+// Calls into the library from the SpMSpV drop-ins are serialised: the
+// reference calls SpMXSpV_ForThreading from an OpenMP loop over row pieces,
+// and the process has one device context and one plan cache.
+inline std::mutex &call_mutex()
+{
+    static std::mutex m;
+    return m;
+}
+
 // y = A x on the GPU into (row, value) arrays sorted by row; x entries whose
 // column is not below g.ncol hit nothing and are dropped first.
 template <class SR, class IVT, class OVT>
 void spmspv_run(const gbc_matrix &g, int vt, const int32_t *indx, const IVT *numx, int32_t veclen,
                 std::vector<int32_t> &rows, std::vector<OVT> &vals)
 {
+    std::lock_guard<std::mutex> lock(call_mutex());
     constexpr int sr = spmspv_of<SR>::sr;
     typedef typename std::conditional<sr == GBC_SR_PLUSTIMES, IVT, int64_t>::type XV;
     typedef typename std::conditional<sr == GBC_SR_PLUSTIMES, OVT, int64_t>::type YV;
@@ -555,12 +567,56 @@ void spmspv_run(const gbc_matrix &g, int vt, const int32_t *indx, const IVT *num
     for (int32_t k = 0; k < ny; ++k) vals[k] = static_cast<OVT>(yv[k]);
 }
 
+// A row piece's entries (rows ascending, local to the piece) as the
+// threaded SpMSpV returns them: each row plus the piece's offset; replacing
+// indy / numy (the boolean SPA version, SpImpl.cpp:311-317) or appended to
+// them (the heap version, SpImpl.cpp:362-384, whose callers pass them empty).
+template <class OVT>
+void shift_rows(const std::vector<int32_t> &r, const std::vector<OVT> &v, int32_t offset, std::vector<int32_t> &indy,
+                std::vector<OVT> &numy, bool append)
+{
+    if (!append) {
+        indy.clear();
+        numy.clear();
+    }
+    indy.reserve(indy.size() + r.size());
+    numy.reserve(numy.size() + r.size());
+    for (size_t k = 0; k < r.size(); ++k) {
+        indy.push_back(r[k] + offset);
+        numy.push_back(v[k]);
+    }
+}
+
+// Value code of a threaded SpMSpV over a Dcsc piece: the reference computes
+// it only for boolean matrices (SpImpl.cpp:276-324; other value types print
+// "not yet supported"), folding x values in column order like the optbuf
+// version.
+template <class SR, class NUM, class IVT, class OVT>
+constexpr int threaded_dcsc_vt()
+{
+    return std::is_same<NUM, bool>::value ? spmspv_vt<SR, NUM, IVT, OVT>() : -1;
+}
+
+// ... over a Csc piece: the heap version (SpImpl.cpp:345-386) combines equal
+// rows in heap order, so only semirings whose add does not depend on order
+// are offloaded (Select2ndMin, SelectMax, integer PlusTimes).
+template <class SR, class NUM, class IVT, class OVT>
+constexpr int threaded_csc_vt()
+{
+    constexpr int vt = spmspv_vt<SR, NUM, IVT, OVT>();
+    constexpr int sr = spmspv_of<SR>::sr;
+    return vt >= 0 && (sr == GBC_SR_SELECT2NDMIN || sr == GBC_SR_SELECTMAX || (sr == GBC_SR_PLUSTIMES && vt == GBC_I64))
+               ? vt
+               : -1;
+}
+
 }  // namespace detail
 
 // Drop the device copies of every matrix multiplied so far (call after
 // changing a matrix in place).
 inline void forget_matrices()
 {
+    std::lock_guard<std::mutex> lock(detail::call_mutex());
     for (auto &e : detail::plan_cache()) gbc_spmspv_plan_destroy(e.second);
     detail::plan_cache().clear();
     for (auto &e : detail::spmv_plan_cache()) gbc_spmv_plan_destroy(e.second);
@@ -577,6 +633,7 @@ void dcsc_gespmv(const combblas::SpDCCols<IU, NU> &A, const RHS *x, LHS *y)
     } else {
         if (A.isZero()) return;
         const gbc_matrix g = detail::view(A);
+        std::lock_guard<std::mutex> lock(detail::call_mutex());
         gbc_spmv_plan *p = detail::spmv_plan(g, semiring_of<SR>::vt);
         detail::check(gbc_spmv(detail::context(), p, semiring_of<SR>::sr, x, y, GBC_HOST), "gbc_spmv");
     }
@@ -624,6 +681,78 @@ void SpMXSpV(const combblas::Dcsc<IT, NUM> &Adcsc, int32_t mA, const int32_t *in
         if (g.nnz > 0) detail::spmspv_run<SR>(g, vt, indx, numx, veclen, r, v);
         detail::split_rows(r, v, mA, indy, numy, cnts, dspls, p_c);
     }
+}
+
+// y = A x over one row piece of a RowSplit matrix (SpImpl.h:68-82, called
+// per piece from an OpenMP loop by Friends.h:203-218 and BFSFriends.h:75-82):
+// indy / numy are replaced by the piece's entries, rows ascending, each row
+// plus `offset`.  Offloaded for boolean pieces under Select2nd, SelectMax and
+// a registered Select2ndMin, with int64 indices; concurrent calls are
+// serialised.  The overload with the caller's SPA buffers (localy, isthere,
+// nzinds) gives the same result and leaves the buffers as they were: the
+// device keeps its own working storage (the reference's result equals it
+// when the buffers start cleared).
+template <class SR, class IT, class NUM, class IVT, class OVT>
+void SpMXSpV_ForThreading(const combblas::Dcsc<IT, NUM> &Adcsc, int32_t mA, const int32_t *indx, const IVT *numx,
+                          int32_t veclen, std::vector<int32_t> &indy, std::vector<OVT> &numy, int32_t offset)
+{
+    constexpr int vt = detail::threaded_dcsc_vt<SR, NUM, IVT, OVT>();
+    if constexpr (vt < 0 || !std::is_same<IT, int64_t>::value) {
+        combblas::SpMXSpV_ForThreading<SR>(Adcsc, mA, indx, numx, veclen, indy, numy, offset);
+    } else {
+        const gbc_matrix g =
+            detail::view_dcsc(&Adcsc, mA, Adcsc.nzc > 0 ? Adcsc.jc[Adcsc.nzc - 1] + 1 : 0, false);
+        std::vector<int32_t> r;
+        std::vector<OVT> v;
+        if (g.nnz > 0) detail::spmspv_run<SR>(g, vt, indx, numx, veclen, r, v);
+        detail::shift_rows(r, v, offset, indy, numy, false);
+    }
+}
+
+template <class SR, class IT, class NUM, class IVT, class OVT>
+void SpMXSpV_ForThreading(const combblas::Dcsc<IT, NUM> &Adcsc, int32_t mA, const int32_t *indx, const IVT *numx,
+                          int32_t veclen, std::vector<int32_t> &indy, std::vector<OVT> &numy, int32_t offset,
+                          std::vector<OVT> &localy, combblas::BitMap &isthere, std::vector<uint32_t> &nzinds)
+{
+    constexpr int vt = detail::threaded_dcsc_vt<SR, NUM, IVT, OVT>();
+    if constexpr (vt < 0 || !std::is_same<IT, int64_t>::value)
+        combblas::SpMXSpV_ForThreading<SR>(Adcsc, mA, indx, numx, veclen, indy, numy, offset, localy, isthere,
+                                           nzinds);
+    else
+        gbcomb::SpMXSpV_ForThreading<SR>(Adcsc, mA, indx, numx, veclen, indy, numy, offset);
+}
+
+// The same over a Csc piece (SpImpl.h:126-142, the heap version): x values
+// multiplied into A's, the piece's entries appended to indy / numy with rows
+// plus `offset`.  Offloaded where the heap's combination order does not show
+// (threaded_csc_vt).
+template <class SR, class IT, class NUM, class IVT, class OVT>
+void SpMXSpV_ForThreading(const combblas::Csc<IT, NUM> &Acsc, int32_t mA, const int32_t *indx, const IVT *numx,
+                          int32_t veclen, std::vector<int32_t> &indy, std::vector<OVT> &numy, int32_t offset)
+{
+    constexpr int vt = detail::threaded_csc_vt<SR, NUM, IVT, OVT>();
+    if constexpr (vt < 0 || !std::is_same<IT, int64_t>::value) {
+        combblas::SpMXSpV_ForThreading<SR>(Acsc, mA, indx, numx, veclen, indy, numy, offset);
+    } else {
+        const gbc_matrix g = detail::view_csc(&Acsc, mA, Acsc.n, vt != GBC_BOOL);
+        std::vector<int32_t> r;
+        std::vector<OVT> v;
+        detail::spmspv_run<SR>(g, vt, indx, numx, veclen, r, v);
+        detail::shift_rows(r, v, offset, indy, numy, true);
+    }
+}
+
+template <class SR, class IT, class NUM, class IVT, class OVT>
+void SpMXSpV_ForThreading(const combblas::Csc<IT, NUM> &Acsc, int32_t mA, const int32_t *indx, const IVT *numx,
+                          int32_t veclen, std::vector<int32_t> &indy, std::vector<OVT> &numy, int32_t offset,
+                          std::vector<OVT> &localy, combblas::BitMap &isthere, std::vector<uint32_t> &nzinds)
+{
+    constexpr int vt = detail::threaded_csc_vt<SR, NUM, IVT, OVT>();
+    if constexpr (vt < 0 || !std::is_same<IT, int64_t>::value)
+        combblas::SpMXSpV_ForThreading<SR>(Acsc, mA, indx, numx, veclen, indy, numy, offset, localy, isthere,
+                                           nzinds);
+    else
+        gbcomb::SpMXSpV_ForThreading<SR>(Acsc, mA, indx, numx, veclen, indy, numy, offset);
 }
 
 }  // namespace gbcomb

@@ -132,6 +132,13 @@ class SpTuples {
 template <class OVT>
 struct PreAllocatedSPA {};
 
+struct BitMap {
+    std::vector<bool> bits;
+    explicit BitMap(uint64_t n = 0) : bits(n) {}
+    void set_bit(uint64_t i) { bits[i] = true; }
+    bool get_bit(uint64_t i) const { return bits[i]; }
+};
+
 // CPU product over column j of B in k order: acc = add(mrhs, acc), first
 // contribution stored as is; rows ascending.
 template <class SR, class NTO, class IT, class NT1, class NT2, class MA, class MB>
@@ -241,6 +248,63 @@ void SpMXSpV(const Dcsc<IT, NUM> &, int32_t, const int32_t *, const IVT *, int32
              int)
 {
     ++fallback_calls();
+}
+
+// the threaded SpMSpV over a row piece: SPA in column order for Dcsc (rows
+// ascending, plus offset, replacing the outputs); x multiplied in and
+// appended for Csc (a map stands in for the reference's heap)
+template <class SR, class IT, class NUM, class IVT, class OVT>
+void SpMXSpV_ForThreading(const Dcsc<IT, NUM> &d, int32_t, const int32_t *indx, const IVT *numx, int32_t veclen,
+                          std::vector<int32_t> &indy, std::vector<OVT> &numy, int32_t offset)
+{
+    ++fallback_calls();
+    std::map<int32_t, OVT> y;
+    for (IT q = 0; q < d.nzc; ++q)
+        for (int32_t k = 0; k < veclen; ++k)
+            if (indx[k] == d.jc[q])
+                for (IT p = d.cp[q]; p < d.cp[q + 1]; ++p) {
+                    auto it = y.find((int32_t)d.ir[p]);
+                    if (it == y.end()) y[(int32_t)d.ir[p]] = static_cast<OVT>(numx[k]);
+                    else it->second = SR::add(it->second, static_cast<OVT>(numx[k]));
+                }
+    indy.clear();
+    numy.clear();
+    for (auto &e : y) {
+        indy.push_back(e.first + offset);
+        numy.push_back(e.second);
+    }
+}
+template <class SR, class IT, class NUM, class IVT, class OVT>
+void SpMXSpV_ForThreading(const Dcsc<IT, NUM> &d, int32_t mA, const int32_t *indx, const IVT *numx, int32_t veclen,
+                          std::vector<int32_t> &indy, std::vector<OVT> &numy, int32_t offset, std::vector<OVT> &,
+                          BitMap &, std::vector<uint32_t> &)
+{
+    SpMXSpV_ForThreading<SR>(d, mA, indx, numx, veclen, indy, numy, offset);
+}
+template <class SR, class IT, class NUM, class IVT, class OVT>
+void SpMXSpV_ForThreading(const Csc<IT, NUM> &c, int32_t, const int32_t *indx, const IVT *numx, int32_t veclen,
+                          std::vector<int32_t> &indy, std::vector<OVT> &numy, int32_t offset)
+{
+    ++fallback_calls();
+    std::map<int32_t, OVT> y;
+    for (int32_t k = 0; k < veclen; ++k)
+        for (IT p = c.jc[indx[k]]; p < c.jc[indx[k] + 1]; ++p) {
+            const OVT v = SR::multiply(c.num[p], numx[k]);
+            auto it = y.find((int32_t)c.ir[p]);
+            if (it == y.end()) y[(int32_t)c.ir[p]] = v;
+            else it->second = SR::add(it->second, v);
+        }
+    for (auto &e : y) {
+        indy.push_back(e.first + offset);
+        numy.push_back(e.second);
+    }
+}
+template <class SR, class IT, class NUM, class IVT, class OVT>
+void SpMXSpV_ForThreading(const Csc<IT, NUM> &c, int32_t mA, const int32_t *indx, const IVT *numx, int32_t veclen,
+                          std::vector<int32_t> &indy, std::vector<OVT> &numy, int32_t offset, std::vector<OVT> &,
+                          BitMap &, std::vector<uint32_t> &)
+{
+    SpMXSpV_ForThreading<SR>(c, mA, indx, numx, veclen, indy, numy, offset);
 }
 
 }  // namespace combblas

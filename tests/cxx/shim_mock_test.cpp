@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstring>
 #include <random>
+#include <thread>
 
 #include "gbcomb/combblas_shim.hpp"
 
@@ -312,6 +313,117 @@ int main()
         EXPECT(fallback_calls() == fb);
         gbcomb::forget_matrices();
         EXPECT(gbcomb::detail::plan_cache().empty());
+    }
+    // 7c. SpMXSpV_ForThreading over one row piece (300 x 900): the boolean
+    // Dcsc piece under Select2nd (outputs replaced, rows plus the offset; the
+    // SPA buffers left as they were), the Csc piece under SelectMax (outputs
+    // appended), PlusTimes fp64 on a Csc piece falling through (the heap's
+    // order shows in fp sums), and four host threads calling at once
+    {
+        std::mt19937_64 rng(91);
+        const I m = 300, n = 900;
+        const int32_t off = 1200;
+        std::vector<I> cp{0}, ir, jc, dcp{0};
+        std::vector<double> val;
+        for (I j = 0; j < n; ++j) {
+            if (j % 4 == 2) {
+                cp.push_back((I)ir.size());
+                continue;
+            }
+            for (I r = 0; r < m; ++r)
+                if (rng() % 100 < 4) {
+                    ir.push_back(r);
+                    val.push_back(double(rng() % 1000) / 999.0);
+                }
+            cp.push_back((I)ir.size());
+            if (cp[j + 1] > cp[j]) {
+                jc.push_back(j);
+                dcp.push_back((I)ir.size());
+            }
+        }
+        std::unique_ptr<bool[]> bv(new bool[ir.size() + 1]);
+        for (size_t q = 0; q < ir.size(); ++q) bv[q] = true;
+        Dcsc<I, bool> d;
+        d.cp = dcp.data();
+        d.jc = jc.data();
+        d.ir = ir.data();
+        d.numx = bv.get();
+        d.nz = (I)ir.size();
+        d.nzc = (I)jc.size();
+        Csc<I, bool> bcsc;
+        bcsc.jc = cp.data();
+        bcsc.ir = ir.data();
+        bcsc.num = bv.get();
+        bcsc.n = n;
+        bcsc.nz = (I)ir.size();
+        Csc<I, double> csc;
+        csc.jc = cp.data();
+        csc.ir = ir.data();
+        csc.num = val.data();
+        csc.n = n;
+        csc.nz = (I)ir.size();
+        std::vector<int32_t> indx;
+        std::vector<int64_t> xi;
+        std::vector<double> xd;
+        for (int32_t c = 0; c < n; c += 1 + (int32_t)(rng() % 4)) {
+            indx.push_back(c);
+            xi.push_back((int64_t)(rng() % 100000) - 50000);
+            xd.push_back(double(rng() % 1000) / 997.0);
+        }
+        std::map<I, int64_t> elast, emax;
+        for (size_t t = 0; t < indx.size(); ++t)
+            for (I p = cp[indx[t]]; p < cp[indx[t] + 1]; ++p) {
+                const I r = ir[p];
+                emax[r] = emax.count(r) ? std::max(emax[r], xi[t]) : xi[t];
+                elast[r] = xi[t];
+            }
+        typedef SelectMaxSRing<bool, int64_t> SMAX;
+        typedef Select2ndSRing<bool, int64_t, int64_t> S2ND;
+        auto check_rows = [&](const std::map<I, int64_t> &e, const std::vector<int32_t> &iy,
+                              const std::vector<int64_t> &ny, size_t skip) {
+            EXPECT(iy.size() == e.size() + skip && ny.size() == iy.size());
+            size_t k = skip;
+            for (auto &x : e) {
+                EXPECT(k < iy.size() && iy[k] == (int32_t)x.first + off && ny[k] == x.second);
+                ++k;
+            }
+        };
+        const int fb = fallback_calls();
+        std::vector<int32_t> indy{-5, -6};
+        std::vector<int64_t> numy{7, 8};
+        gbcomb::SpMXSpV_ForThreading<S2ND>(d, (int32_t)m, indx.data(), xi.data(), (int32_t)indx.size(), indy, numy,
+                                           off);
+        check_rows(elast, indy, numy, 0);
+        std::vector<int64_t> localy(m, 42);
+        BitMap isthere(m);
+        std::vector<uint32_t> nzinds(5, 3u);
+        gbcomb::SpMXSpV_ForThreading<S2ND>(d, (int32_t)m, indx.data(), xi.data(), (int32_t)indx.size(), indy, numy,
+                                           off, localy, isthere, nzinds);
+        check_rows(elast, indy, numy, 0);
+        EXPECT(nzinds.size() == 5 && localy[0] == 42 && !isthere.get_bit(0));
+        std::vector<int32_t> cy{77};
+        std::vector<int64_t> cn{78};
+        gbcomb::SpMXSpV_ForThreading<SMAX>(bcsc, (int32_t)m, indx.data(), xi.data(), (int32_t)indx.size(), cy, cn,
+                                           off);
+        EXPECT(cy[0] == 77 && cn[0] == 78);
+        check_rows(emax, cy, cn, 1);
+        EXPECT(fallback_calls() == fb);
+        std::vector<int32_t> fy;
+        std::vector<double> fn;
+        gbcomb::SpMXSpV_ForThreading<PT>(csc, (int32_t)m, indx.data(), xd.data(), (int32_t)indx.size(), fy, fn, off);
+        EXPECT(fallback_calls() == fb + 1);
+        std::vector<std::vector<int32_t>> ty(4);
+        std::vector<std::vector<int64_t>> tn(4);
+        std::vector<std::thread> pool;
+        for (int t = 0; t < 4; ++t)
+            pool.emplace_back([&, t]() {
+                for (int rep = 0; rep < 3; ++rep)
+                    gbcomb::SpMXSpV_ForThreading<S2ND>(d, (int32_t)m, indx.data(), xi.data(), (int32_t)indx.size(),
+                                                       ty[t], tn[t], off);
+            });
+        for (auto &th : pool) th.join();
+        for (int t = 0; t < 4; ++t) check_rows(elast, ty[t], tn[t], 0);
+        gbcomb::forget_matrices();
     }
     // 8. MultiwayMerge of three products of one shape (GPU) against the CPU merge
     {

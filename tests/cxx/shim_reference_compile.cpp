@@ -66,6 +66,28 @@ template void gbcomb::SpMXSpV<S2ND, int32_t, bool, int64_t, int64_t>(const Dcsc<
                                                                      const int32_t *, const int64_t *, int32_t,
                                                                      int32_t *, int64_t *, int *, int *, int);
 
+// the threaded SpMSpV over row pieces: GPU for boolean Dcsc pieces (both
+// overloads) and order-free semirings on Csc pieces; fall-through for fp
+// PlusTimes and non-boolean Dcsc pieces
+template void gbcomb::SpMXSpV_ForThreading<S2ND, int64_t, bool, int64_t, int64_t>(
+    const Dcsc<int64_t, bool> &, int32_t, const int32_t *, const int64_t *, int32_t, std::vector<int32_t> &,
+    std::vector<int64_t> &, int32_t);
+template void gbcomb::SpMXSpV_ForThreading<S2ND, int64_t, bool, int64_t, int64_t>(
+    const Dcsc<int64_t, bool> &, int32_t, const int32_t *, const int64_t *, int32_t, std::vector<int32_t> &,
+    std::vector<int64_t> &, int32_t, std::vector<int64_t> &, BitMap &, std::vector<uint32_t> &);
+template void gbcomb::SpMXSpV_ForThreading<SMAX, int64_t, bool, int64_t, int64_t>(
+    const Csc<int64_t, bool> &, int32_t, const int32_t *, const int64_t *, int32_t, std::vector<int32_t> &,
+    std::vector<int64_t> &, int32_t);
+template void gbcomb::SpMXSpV_ForThreading<S2M, int64_t, bool, int64_t, int64_t>(
+    const Csc<int64_t, bool> &, int32_t, const int32_t *, const int64_t *, int32_t, std::vector<int32_t> &,
+    std::vector<int64_t> &, int32_t, std::vector<int64_t> &, BitMap &, std::vector<uint32_t> &);
+template void gbcomb::SpMXSpV_ForThreading<PTD, int64_t, double, double, double>(
+    const Csc<int64_t, double> &, int32_t, const int32_t *, const double *, int32_t, std::vector<int32_t> &,
+    std::vector<double> &, int32_t);
+template void gbcomb::SpMXSpV_ForThreading<PTD, int64_t, double, double, double>(
+    const Dcsc<int64_t, double> &, int32_t, const int32_t *, const double *, int32_t, std::vector<int32_t> &,
+    std::vector<double> &, int32_t);
+
 template SpTuples<int64_t, double> *gbcomb::MultiwayMerge<PTD, int64_t, double>(
     std::vector<SpTuples<int64_t, double> *> &, int64_t, int64_t, bool);
 template SpTuples<int32_t, double> *gbcomb::MultiwayMerge<PTD, int32_t, double>(

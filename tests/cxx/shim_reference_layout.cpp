@@ -11,7 +11,9 @@
 //    merge sends to the device;
 //  * detail::split_rows, applied to the reference's heap SpMXSpV output
 //    (SpImpl.cpp:166-209), gives the reference's optbuf output
-//    (SpImpl.cpp:222-272): counts, receiver-local rows and values.
+//    (SpImpl.cpp:222-272): counts, receiver-local rows and values;
+//    detail::shift_rows gives its threaded outputs over a row piece
+//    (SpImpl.cpp:276-324, 345-386).
 // A layout mismatch between the shim and the reference's classes fails here.
 // Prints "layout-ok" and exits 0 when every check passes.
 #include <algorithm>
@@ -212,6 +214,24 @@ void test_split_rows()
         std::snprintf(what, sizeof(what), "split_rows against the optbuf SpMXSpV, p_c = %d", p_c);
         check(same, what);
     }
+    // shift_rows against the threaded versions over a row piece: the boolean
+    // SPA one (outputs replaced) and the Csc heap one (outputs appended)
+    const int32_t off = 4096;
+    std::vector<int32_t> ty{9, 9, 9}, sy;
+    std::vector<int64_t> tv{1, 1, 1}, sv;
+    Impl::SpMXSpV_ForThreading(d, mA, indx.data(), numx.data(), veclen, ty, tv, off);
+    sy = {5};
+    sv = {6};
+    gbcomb::detail::shift_rows(heap_rows, heap_vals, off, sy, sv, false);
+    check(ty == sy && tv == sv, "shift_rows against the boolean threaded SpMXSpV");
+    SpTuples<int64_t, bool> *T2 = sptuples(pat, m, m, false);
+    SpCCols<int64_t, bool> Ac(*T2, false);
+    delete T2;
+    std::vector<int32_t> hy, gy;
+    std::vector<int64_t> hv, gv;
+    combblas::SpMXSpV_ForThreading<MinSR>(*Ac.GetCSC(), mA, indx.data(), numx.data(), veclen, hy, hv, off);
+    gbcomb::detail::shift_rows(heap_rows, heap_vals, off, gy, gv, true);
+    check(!hy.empty() && hy == gy && hv == gv, "shift_rows against the Csc heap threaded SpMXSpV");
 }
 
 }  // namespace
