@@ -9,6 +9,7 @@
  *   gbcomb::LocalSpGEMMHash<SR, NTO>(A, B, clearA, clearB, sort) mtSpGEMM.h:463-467
  *   gbcomb::LocalHybridSpGEMM<SR, NTO>(SpCCols A, SpCCols B, ...)  mtSpGEMM.h:1142-1152
  *   gbcomb::SpMXSpV<SR>(Csc, mA, indx, numx, veclen, indy, numy, SPA)  SpImpl.h:115-124
+ *   gbcomb::SpMXSpV<SR>(Dcsc, mA, indx, numx, veclen, indy, numy, SPA)  SpImpl.h:49-56
  *   gbcomb::SpMXSpV<SR>(Dcsc, mA, indx, numx, veclen, indy*, numy*, cnts, dspls, p_c)  SpImpl.h:59-65
  *   gbcomb::SpMXSpV_ForThreading<SR>(Dcsc or Csc piece, ..., offset[, SPA buffers])  SpImpl.h:68-82, 126-142
  *   gbcomb::MultiwayMerge<SR>(ArrSpTups, mdim, ndim, delarrs)  MultiwayMerge.h:428-708
@@ -597,11 +598,12 @@ constexpr int threaded_dcsc_vt()
     return std::is_same<NUM, bool>::value ? spmspv_vt<SR, NUM, IVT, OVT>() : -1;
 }
 
-// ... over a Csc piece: the heap version (SpImpl.cpp:345-386) combines equal
-// rows in heap order, so only semirings whose add does not depend on order
-// are offloaded (Select2ndMin, SelectMax, integer PlusTimes).
+// ... for the heap versions (the threaded Csc one, SpImpl.cpp:345-386, and
+// the Dcsc one with vector outputs, SpImpl.cpp:56-157 and 166-209), which
+// combine equal rows in heap order: only semirings whose add does not depend
+// on order are offloaded (Select2ndMin, SelectMax, integer PlusTimes).
 template <class SR, class NUM, class IVT, class OVT>
-constexpr int threaded_csc_vt()
+constexpr int heap_vt()
 {
     constexpr int vt = spmspv_vt<SR, NUM, IVT, OVT>();
     constexpr int sr = spmspv_of<SR>::sr;
@@ -658,6 +660,28 @@ void SpMXSpV(const combblas::Csc<IT, NUM> &Acsc, int32_t mA, const int32_t *indx
         detail::spmspv_run<SR>(g, vt, indx, numx, veclen, r, v);
         indy.insert(indy.end(), r.begin(), r.end());
         numy.insert(numy.end(), v.begin(), v.end());
+    }
+}
+
+// y = A x over a Dcsc with vector outputs (SpImpl.h:49-56, the heap merge of
+// SpImpl.cpp:56-157 and, for boolean matrices, 166-209; the call of
+// Friends.h's local SpMV on a SpDCCols): appended to indy / numy sorted by
+// row.  Offloaded where the heap's combination order does not show (heap_vt),
+// with int64 indices.
+template <class SR, class IT, class NUM, class IVT, class OVT>
+void SpMXSpV(const combblas::Dcsc<IT, NUM> &Adcsc, int32_t mA, const int32_t *indx, const IVT *numx, int32_t veclen,
+             std::vector<int32_t> &indy, std::vector<OVT> &numy, combblas::PreAllocatedSPA<OVT> &SPA)
+{
+    constexpr int vt = detail::heap_vt<SR, NUM, IVT, OVT>();
+    if constexpr (vt < 0 || !std::is_same<IT, int64_t>::value) {
+        combblas::SpMXSpV<SR>(Adcsc, mA, indx, numx, veclen, indy, numy, SPA);
+    } else {
+        const gbc_matrix g =
+            detail::view_dcsc(&Adcsc, mA, Adcsc.nzc > 0 ? Adcsc.jc[Adcsc.nzc - 1] + 1 : 0, vt != GBC_BOOL);
+        std::vector<int32_t> r;
+        std::vector<OVT> v;
+        if (g.nnz > 0) detail::spmspv_run<SR>(g, vt, indx, numx, veclen, r, v);
+        detail::shift_rows(r, v, 0, indy, numy, true);
     }
 }
 
@@ -725,12 +749,12 @@ void SpMXSpV_ForThreading(const combblas::Dcsc<IT, NUM> &Adcsc, int32_t mA, cons
 // The same over a Csc piece (SpImpl.h:126-142, the heap version): x values
 // multiplied into A's, the piece's entries appended to indy / numy with rows
 // plus `offset`.  Offloaded where the heap's combination order does not show
-// (threaded_csc_vt).
+// (heap_vt).
 template <class SR, class IT, class NUM, class IVT, class OVT>
 void SpMXSpV_ForThreading(const combblas::Csc<IT, NUM> &Acsc, int32_t mA, const int32_t *indx, const IVT *numx,
                           int32_t veclen, std::vector<int32_t> &indy, std::vector<OVT> &numy, int32_t offset)
 {
-    constexpr int vt = detail::threaded_csc_vt<SR, NUM, IVT, OVT>();
+    constexpr int vt = detail::heap_vt<SR, NUM, IVT, OVT>();
     if constexpr (vt < 0 || !std::is_same<IT, int64_t>::value) {
         combblas::SpMXSpV_ForThreading<SR>(Acsc, mA, indx, numx, veclen, indy, numy, offset);
     } else {
@@ -747,7 +771,7 @@ void SpMXSpV_ForThreading(const combblas::Csc<IT, NUM> &Acsc, int32_t mA, const 
                           int32_t veclen, std::vector<int32_t> &indy, std::vector<OVT> &numy, int32_t offset,
                           std::vector<OVT> &localy, combblas::BitMap &isthere, std::vector<uint32_t> &nzinds)
 {
-    constexpr int vt = detail::threaded_csc_vt<SR, NUM, IVT, OVT>();
+    constexpr int vt = detail::heap_vt<SR, NUM, IVT, OVT>();
     if constexpr (vt < 0 || !std::is_same<IT, int64_t>::value)
         combblas::SpMXSpV_ForThreading<SR>(Acsc, mA, indx, numx, veclen, indy, numy, offset, localy, isthere,
                                            nzinds);

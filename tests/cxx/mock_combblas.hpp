@@ -249,6 +249,12 @@ void SpMXSpV(const Dcsc<IT, NUM> &, int32_t, const int32_t *, const IVT *, int32
 {
     ++fallback_calls();
 }
+template <class SR, class IT, class NUM, class IVT, class OVT>
+void SpMXSpV(const Dcsc<IT, NUM> &, int32_t, const int32_t *, const IVT *, int32_t, std::vector<int32_t> &,
+             std::vector<OVT> &, PreAllocatedSPA<OVT> &)
+{
+    ++fallback_calls();
+}
 
 // the threaded SpMSpV over a row piece: SPA in column order for Dcsc (rows
 // ascending, plus offset, replacing the outputs); x multiplied in and

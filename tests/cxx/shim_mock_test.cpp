@@ -408,10 +408,28 @@ int main()
         EXPECT(cy[0] == 77 && cn[0] == 78);
         check_rows(emax, cy, cn, 1);
         EXPECT(fallback_calls() == fb);
+        // the Dcsc overload with vector outputs (appended, global rows)
+        PreAllocatedSPA<int64_t> spa;
+        std::vector<int32_t> dy{3};
+        std::vector<int64_t> dn{4};
+        gbcomb::SpMXSpV<SMAX>(d, (int32_t)m, indx.data(), xi.data(), (int32_t)indx.size(), dy, dn, spa);
+        EXPECT(dy.size() == emax.size() + 1 && dy[0] == 3 && dn[0] == 4);
+        {
+            size_t k = 1;
+            for (auto &x : emax) {
+                EXPECT(k < dy.size() && dy[k] == (int32_t)x.first && dn[k] == x.second);
+                ++k;
+            }
+        }
+        EXPECT(fallback_calls() == fb);
         std::vector<int32_t> fy;
         std::vector<double> fn;
         gbcomb::SpMXSpV_ForThreading<PT>(csc, (int32_t)m, indx.data(), xd.data(), (int32_t)indx.size(), fy, fn, off);
         EXPECT(fallback_calls() == fb + 1);
+        std::vector<int32_t> sy2;
+        std::vector<int64_t> sn2;
+        gbcomb::SpMXSpV<S2ND>(d, (int32_t)m, indx.data(), xi.data(), (int32_t)indx.size(), sy2, sn2, spa);
+        EXPECT(fallback_calls() == fb + 2);  // last writer in heap order: the reference runs
         std::vector<std::vector<int32_t>> ty(4);
         std::vector<std::vector<int64_t>> tn(4);
         std::vector<std::thread> pool;

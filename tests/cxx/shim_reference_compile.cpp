@@ -66,6 +66,15 @@ template void gbcomb::SpMXSpV<S2ND, int32_t, bool, int64_t, int64_t>(const Dcsc<
                                                                      const int32_t *, const int64_t *, int32_t,
                                                                      int32_t *, int64_t *, int *, int *, int);
 
+// the Dcsc overload with vector outputs: GPU for order-free semirings,
+// the reference's heap for Select2nd
+template void gbcomb::SpMXSpV<SMAX, int64_t, bool, int64_t, int64_t>(
+    const Dcsc<int64_t, bool> &, int32_t, const int32_t *, const int64_t *, int32_t, std::vector<int32_t> &,
+    std::vector<int64_t> &, PreAllocatedSPA<int64_t> &);
+template void gbcomb::SpMXSpV<S2ND, int64_t, bool, int64_t, int64_t>(
+    const Dcsc<int64_t, bool> &, int32_t, const int32_t *, const int64_t *, int32_t, std::vector<int32_t> &,
+    std::vector<int64_t> &, PreAllocatedSPA<int64_t> &);
+
 // the threaded SpMSpV over row pieces: GPU for boolean Dcsc pieces (both
 // overloads) and order-free semirings on Csc pieces; fall-through for fp
 // PlusTimes and non-boolean Dcsc pieces
